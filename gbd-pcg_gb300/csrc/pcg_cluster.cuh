@@ -1,0 +1,458 @@
+// Persistent thread-block-cluster PCG kernel for block-tridiagonal
+// Schur-complement systems (the hot path of Sdevaud/GBD-PCG,
+// include/pcg.cuh:54-218), written for sm_103a.
+//
+// Mapping
+//   * One cluster of C CTAs solves one system at a time and then pulls the next
+//     system from a device work queue (an atomic counter over a host-sorted,
+//     longest-first list).  C comes from the launch's cluster dimension.
+//   * CTA `rank` owns the contiguous knots [kb, ke), kb = rank*K, K = ceil(N/C).
+//   * Thread t of a CTA owns one matrix row: local knot t / n, row t % n.  Its
+//     row of S (3 blocks) and of Phi^-1 (1 or 3 blocks) is either held in
+//     registers for the whole solve (MREG) — the matvec is then a register tile
+//     fed by vectorised shared-memory loads of the p / r window — or staged in
+//     shared memory (for FP64 and large blocks, where registers do not fit).
+//   * Vectors p and r live in shared memory with one halo knot on each side.
+//     Neighbour CTAs exchange boundary vectors through distributed shared
+//     memory (DSMEM): instead of re-publishing p and r after every update (as
+//     the reference does through global memory, include/pcg.cuh:175,205 and 4
+//     grid.sync per iteration), each CTA pushes its boundary upsilon = S p and
+//     z = Phi^-1 r together with its dot-product partial, and the receiver
+//     applies the same fused multiply-add to its halo copy that the owner
+//     applies to the original (r_h -= alpha upsilon_h; p_h = z_h + beta p_h),
+//     so the halos stay bit-identical with two cluster barriers per iteration.
+//   * Dot products: warp shuffle butterfly -> per-warp partials in shared memory
+//     -> one CTA partial pushed to every CTA of the cluster -> barrier.cluster ->
+//     every thread sums the C partials in rank order.  All threads of the
+//     cluster therefore hold identical alpha, beta and exit decisions.
+// Arithmetic follows the reference: alpha = eta / p.Sp, lambda += alpha p,
+// r -= alpha Sp, beta = eta'/eta, p = z + beta p as fused multiply-adds; exit
+// on |r.z| < tol (include/pcg.cuh:195) or, optionally, on the relative
+// recursive residual ||r|| <= tol ||gamma||.  The iteration count includes the
+// converging pass, as the reference's does.
+#pragma once
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pcg_types.h"
+
+namespace gbdpcg {
+namespace cg = cooperative_groups;
+
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+__host__ __device__ constexpr size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+// Shared-memory plan of one CTA (element counts; every buffer 32-byte aligned).
+template <typename T, typename A, int NP, bool PTRI, bool MREG>
+struct SmemPlan {
+    static constexpr int NB_P = PTRI ? 3 : 1;
+    __host__ __device__ static size_t vec(uint32_t kmax) {
+        return round_up((size_t)(kmax + 2) * NP * sizeof(T), 32);
+    }
+    __host__ __device__ static size_t halo() { return round_up((size_t)2 * NP * sizeof(T), 32); }
+    __host__ __device__ static size_t mat_s(uint32_t kmax) {
+        return MREG ? 0 : round_up((size_t)kmax * 3 * NP * NP * sizeof(T), 32);
+    }
+    __host__ __device__ static size_t mat_p(uint32_t kmax) {
+        return MREG ? 0 : round_up((size_t)kmax * NB_P * NP * NP * sizeof(T), 32);
+    }
+    static constexpr size_t kWpart = 2 * 32 * 2 * sizeof(A);  // 2 buffers x 32 warps x 2 values
+    static constexpr size_t kRed = 2 * 16 * 2 * sizeof(A);    // 2 buffers x 16 ranks x 2 values
+    __host__ __device__ static size_t bytes(uint32_t kmax) {
+        return 2 * vec(kmax) + 2 * halo() + kWpart + kRed + 32 + mat_s(kmax) + mat_p(kmax);
+    }
+};
+
+// Load NP consecutive shared-memory elements into registers with the widest
+// aligned vector loads (base is NP-element aligned).
+template <typename T, int NP>
+__device__ __forceinline__ void lds_row(T (&x)[NP], const T *p) {
+    if constexpr (sizeof(T) == 4 && NP % 4 == 0) {
+#pragma unroll
+        for (int j = 0; j < NP; j += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(p + j);
+            x[j] = v.x; x[j + 1] = v.y; x[j + 2] = v.z; x[j + 3] = v.w;
+        }
+    } else if constexpr (NP % 2 == 0 && sizeof(T) == 4) {
+#pragma unroll
+        for (int j = 0; j < NP; j += 2) {
+            const float2 v = *reinterpret_cast<const float2 *>(p + j);
+            x[j] = v.x; x[j + 1] = v.y;
+        }
+    } else if constexpr (NP % 2 == 0 && sizeof(T) == 8) {
+#pragma unroll
+        for (int j = 0; j < NP; j += 2) {
+            const double2 v = *reinterpret_cast<const double2 *>(p + j);
+            x[j] = v.x; x[j + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < NP; ++j) x[j] = p[j];
+    }
+}
+
+// Register-tile block-row matvec: y = sum_b sum_j M[b][j] * x[b*NP + j].
+// One accumulator chain per block, summed in block order.
+template <typename T, int NP, int NB>
+__device__ __forceinline__ T reg_matvec(const T (&M)[NB * NP], const T *x) {
+    T acc[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        T xv[NP];
+        lds_row<T, NP>(xv, x + b * NP);
+        acc[b] = T(0);
+#pragma unroll
+        for (int j = 0; j < NP; ++j) acc[b] = fma_rn(M[b * NP + j], xv[j], acc[b]);
+    }
+    T y = acc[0];
+#pragma unroll
+    for (int b = 1; b < NB; ++b) y += acc[b];
+    return y;
+}
+
+// Shared-memory block-row matvec over the present blocks [b0, b1) of a
+// column-major n x (NB n) block row staged in shared memory; x points at the
+// window of block 0 (windows are NP apart).
+template <typename T, int NP, int NB>
+__device__ __forceinline__ T smem_matvec(const T *Mrow, int b0, int b1, const T *x, uint32_t n,
+                                         uint32_t i) {
+    T acc[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        acc[b] = T(0);
+        if (b >= b0 && b < b1) {
+            const T *col = Mrow + (size_t)b * n * n + i;
+            const T *xb = x + b * NP;
+#pragma unroll 4
+            for (uint32_t j = 0; j < n; ++j) acc[b] = fma_rn(col[(size_t)j * n], xb[j], acc[b]);
+        }
+    }
+    T y = acc[0];
+#pragma unroll
+    for (int b = 1; b < NB; ++b) y += acc[b];
+    return y;
+}
+
+template <typename A>
+__device__ __forceinline__ A warp_sum(A v) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Cluster-wide sum of NQ values.  Identical result in every thread of the
+// cluster.  `buf` alternates between call sites so that a buffer is rewritten
+// only after a barrier that every reader has passed.  Remote pushes made by
+// the caller before this call are visible to their targets afterwards.
+template <typename A, int NQ>
+__device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *wpart, A *red, int buf,
+                                                  const cg::cluster_group &cluster, uint32_t C,
+                                                  uint32_t rank) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t nwarps = blockDim.x >> 5;
+    A *wp = wpart + buf * 64;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) v[q] = warp_sum(v[q]);
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) wp[warp * 2 + q] = v[q];
+    }
+    __syncthreads();
+    if (C == 1) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            A s = A(0);
+            for (uint32_t w = 0; w < nwarps; ++w) s += wp[w * 2 + q];
+            v[q] = s;
+        }
+        return;
+    }
+    A *rd = red + buf * 32;
+    if (warp == 0) {
+        A s[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) s[q] = warp_sum(lane < nwarps ? wp[lane * 2 + q] : A(0));
+        if (lane < C) {
+            A *dst = cluster.map_shared_rank(rd, lane);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) dst[rank * 2 + q] = s[q];
+        }
+    }
+    cluster.sync();
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        A s = A(0);
+        for (uint32_t c = 0; c < C; ++c) s += rd[c * 2 + q];
+        v[q] = s;
+    }
+}
+
+__device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uint32_t C) {
+    if (C > 1)
+        cluster.sync();
+    else
+        __syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ bool finite_(T x) {
+    return isfinite(x);
+}
+
+// The solver.  T: storage and arithmetic type of matrices and vectors;
+// A: accumulation type of the dot products (T, or double for mixed precision);
+// NP: compile-time block size bound (n <= NP); PTRI: Phi^-1 is block-
+// tridiagonal; MREG: matrix rows held in registers (else in shared memory).
+template <typename T, typename A, int NP, bool PTRI, bool MREG>
+__global__ void pcg_cluster_kernel(const LaunchParams lp) {
+    using Plan = SmemPlan<T, A, NP, PTRI, MREG>;
+    constexpr int NBP = PTRI ? 3 : 1;
+    const cg::cluster_group cluster = cg::this_cluster();
+    const uint32_t C = cluster.num_blocks();
+    const uint32_t rank = cluster.block_rank();
+    const uint32_t tid = threadIdx.x, nthr = blockDim.x;
+
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char *sp = smem_raw;
+    T *vp = reinterpret_cast<T *>(sp); sp += Plan::vec(lp.kmax);
+    T *vr = reinterpret_cast<T *>(sp); sp += Plan::vec(lp.kmax);
+    T *uh = reinterpret_cast<T *>(sp); sp += Plan::halo();
+    T *zh = reinterpret_cast<T *>(sp); sp += Plan::halo();
+    A *wpart = reinterpret_cast<A *>(sp); sp += Plan::kWpart;
+    A *red = reinterpret_cast<A *>(sp); sp += Plan::kRed;
+    uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
+    T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
+    T *mp = reinterpret_cast<T *>(sp);
+    const size_t zero_elems = (2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T);
+
+    for (;;) {
+        // ---- pull the next system (cluster leader pops, broadcasts by DSMEM)
+        if (rank == 0 && tid == 0) {
+            const uint32_t it = atomicAdd(lp.queue, 1u);
+            for (uint32_t c = 0; c < C; ++c) *cluster.map_shared_rank(s_item, c) = it;
+        }
+        group_sync(cluster, C);
+        const uint32_t item = *reinterpret_cast<volatile uint32_t *>(s_item);
+        if (item >= lp.count) break;
+        const SysDesc d = lp.descs[lp.order[item]];
+        const uint32_t n = d.n, N = d.N;
+        const uint32_t K = (N + C - 1) / C;
+        if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (size_t)K * n > nthr) {
+            if (rank == 0 && tid == 0) {
+                SysResult res = {};
+                res.status = -1;
+                lp.results[d.result] = res;
+            }
+            group_sync(cluster, C);  // s_item is read by every CTA before the next pop
+            continue;                // uniform: every CTA of the cluster sees the same descriptor
+        }
+        const uint32_t kb = min(rank * K, N), ke = min(kb + K, N), nk = ke - kb;
+        const uint32_t lk = tid / n, i = tid - lk * n;
+        const bool act = lk < nk;
+        const uint32_t k = kb + lk;
+        const bool relres = (d.flags & SYS_EXIT_RELRES) != 0;
+        const T *__restrict__ S = static_cast<const T *>(d.S);
+        const T *__restrict__ P = static_cast<const T *>(d.P);
+        const T *__restrict__ gamma = static_cast<const T *>(d.gamma);
+        const T *__restrict__ lam0 =
+            (d.flags & SYS_LAMBDA0_ZERO) ? nullptr : static_cast<const T *>(d.lambda0);
+        const size_t blkS = (size_t)3 * n * n, blkP = (size_t)NBP * n * n;
+        const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
+
+        for (size_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
+
+        // ---- matrices: registers or shared memory
+        T Sr[MREG ? 3 * NP : 1];
+        T Pr[MREG ? NBP * NP : 1];
+        if constexpr (MREG) {
+            const T *Sk = S + (size_t)k * blkS;
+            const T *Pk = P + (size_t)k * blkP;
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const bool present = act && (b != 0 || k > 0) && (b != 2 || k + 1 < N);
+#pragma unroll
+                for (int j = 0; j < NP; ++j)
+                    Sr[b * NP + j] =
+                        (present && (uint32_t)j < n) ? __ldg(Sk + (size_t)(b * n + j) * n + i) : T(0);
+            }
+#pragma unroll
+            for (int b = 0; b < NBP; ++b) {
+                const bool present =
+                    act && (!PTRI || ((b != 0 || k > 0) && (b != 2 || k + 1 < N)));
+#pragma unroll
+                for (int j = 0; j < NP; ++j)
+                    Pr[b * NP + j] =
+                        (present && (uint32_t)j < n) ? __ldg(Pk + (size_t)(b * n + j) * n + i) : T(0);
+            }
+        } else {
+            const T *Sg = S + (size_t)kb * blkS;
+            const T *Pg = P + (size_t)kb * blkP;
+            for (size_t e = tid; e < nk * blkS; e += nthr) ms[e] = __ldg(Sg + e);
+            for (size_t e = tid; e < nk * blkP; e += nthr) mp[e] = __ldg(Pg + e);
+        }
+        const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
+        auto matS = [&](const T *x) -> T {
+            if constexpr (MREG) return reg_matvec<T, NP, 3>(Sr, x);
+            else return smem_matvec<T, NP, 3>(ms + lk * blkS, sb0, sb1, x, n, i);
+        };
+        auto matP = [&](const T *x) -> T {
+            if constexpr (MREG) {
+                if constexpr (PTRI) return reg_matvec<T, NP, 3>(Pr, x);
+                else return reg_matvec<T, NP, 1>(Pr, x + NP);
+            } else {
+                if constexpr (PTRI) return smem_matvec<T, NP, 3>(mp + lk * blkP, sb0, sb1, x, n, i);
+                else return smem_matvec<T, NP, 1>(mp + lk * blkP, 0, 1, x + NP, n, i);
+            }
+        };
+        __syncthreads();
+
+        // ---- r = gamma - S lambda0   (include/pcg.cuh:119-126)
+        T gam = T(0), lam = T(0);
+        if (act) {
+            gam = gamma[(size_t)k * n + i];
+            lam = lam0 ? lam0[(size_t)k * n + i] : T(0);
+            vp[(lk + 1) * NP + i] = lam;
+        }
+        if (lam0) {
+            for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                if (t < n && has_left) vp[t] = lam0[(size_t)(kb - 1) * n + t];
+                if (t >= n && has_right) vp[(nk + 1) * NP + (t - n)] = lam0[(size_t)ke * n + (t - n)];
+            }
+        }
+        __syncthreads();
+        T r = act ? gam - matS(vp + lk * NP) : T(0);
+        group_sync(cluster, C);  // all windows read before any neighbour writes into them
+
+        // ---- z = Phi^-1 r; p = z; eta = r.z   (include/pcg.cuh:131-149)
+        if (act) vr[(lk + 1) * NP + i] = r;
+        if constexpr (PTRI) {
+            if (act && lk == 0 && kb > 0) cluster.map_shared_rank(vr, rank - 1)[(K + 1) * NP + i] = r;
+            if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(vr, rank + 1)[i] = r;
+            group_sync(cluster, C);
+        } else {
+            __syncthreads();
+        }
+        T z = act ? matP(vr + lk * NP) : T(0);
+        T p = z;
+        if (act) vp[(lk + 1) * NP + i] = p;
+        if (act && lk == 0 && kb > 0) cluster.map_shared_rank(vp, rank - 1)[(K + 1) * NP + i] = z;
+        if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(vp, rank + 1)[i] = z;
+        A eta, gg;
+        {
+            A v2[2] = {act ? A(r) * A(z) : A(0), act ? A(gam) * A(gam) : A(0)};
+            cluster_allreduce<A, 2>(v2, wpart, red, 1, cluster, C, rank);
+            eta = v2[0];
+            gg = v2[1];
+        }
+        const A thr = A(d.tol * d.tol * (double)gg);
+        const A tol = A(d.tol);
+
+        // ---- main loop   (include/pcg.cuh:154-208)
+        uint32_t iter = 0;
+        int32_t status = ST_MAX_ITER;
+        A eta_new = A(0), rr = A(0);
+        for (; iter < d.max_iter;) {
+            const T y = act ? matS(vp + lk * NP) : T(0);
+            if constexpr (PTRI) {  // neighbours need this CTA's boundary upsilon for their r halo
+                if (act && lk == 0 && kb > 0) cluster.map_shared_rank(uh, rank - 1)[NP + i] = y;
+                if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(uh, rank + 1)[i] = y;
+            }
+            A pap;
+            {
+                A v1[1] = {act ? A(p) * A(y) : A(0)};
+                cluster_allreduce<A, 1>(v1, wpart, red, 0, cluster, C, rank);
+                pap = v1[0];
+            }
+            const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
+            lam = fma_rn(alpha, p, lam);
+            r = fma_rn(-alpha, y, r);
+            if (act) vr[(lk + 1) * NP + i] = r;
+            if constexpr (PTRI) {
+                for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                    if (t < n && has_left) vr[t] = fma_rn(-alpha, uh[t], vr[t]);
+                    if (t >= n && has_right) {
+                        T *h = vr + (nk + 1) * NP + (t - n);
+                        *h = fma_rn(-alpha, uh[NP + t - n], *h);
+                    }
+                }
+            }
+            __syncthreads();
+            z = act ? matP(vr + lk * NP) : T(0);
+            if (act && lk == 0 && kb > 0) cluster.map_shared_rank(zh, rank - 1)[NP + i] = z;
+            if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(zh, rank + 1)[i] = z;
+            {
+                A v2[2] = {act ? A(r) * A(z) : A(0), (act && relres) ? A(r) * A(r) : A(0)};
+                cluster_allreduce<A, 2>(v2, wpart, red, 1, cluster, C, rank);
+                eta_new = v2[0];
+                rr = v2[1];
+            }
+            ++iter;
+            if (!finite_(eta_new) || !finite_(pap)) { status = ST_BREAKDOWN; break; }
+            if (relres ? (rr <= thr) : (fabs(eta_new) < tol)) { status = ST_CONVERGED; break; }
+            const T beta = T(eta_new / eta);
+            eta = eta_new;
+            p = fma_rn(beta, p, z);
+            if (act) vp[(lk + 1) * NP + i] = p;
+            for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                if (t < n && has_left) vp[t] = fma_rn(beta, vp[t], zh[t]);
+                if (t >= n && has_right) {
+                    T *h = vp + (nk + 1) * NP + (t - n);
+                    *h = fma_rn(beta, *h, zh[NP + t - n]);
+                }
+            }
+            __syncthreads();
+        }
+
+        // ---- outputs   (include/pcg.cuh:212-217)
+        T *lam_out = static_cast<T *>(d.lambda);
+        if (act) lam_out[(size_t)k * n + i] = lam;
+        if (rank == 0 && tid == 0) {
+            SysResult res;
+            res.iters = iter;
+            res.status = status;
+            res.eta = (double)eta_new;
+            res.rr = relres ? (double)rr : -1.0;
+            res.gg = (double)gg;
+            res.outer = 0;
+            res.pad = 0;
+            lp.results[d.result] = res;
+        }
+
+        // ---- adjoint epilogue: dS = -1/2 (mu lam^T + lam mu^T) on the block pattern
+        if (d.flags & SYS_ADJOINT) {
+            const T *lf = static_cast<const T *>(d.lam_fwd);
+            T *dS = static_cast<T *>(d.dS);
+            group_sync(cluster, C);  // vp / vr free in every CTA
+            T lfi = T(0);
+            if (act) {
+                lfi = lf[(size_t)k * n + i];
+                vr[(lk + 1) * NP + i] = lam;  // mu
+                vp[(lk + 1) * NP + i] = lfi;
+            }
+            if (act && lk == 0 && kb > 0) cluster.map_shared_rank(vr, rank - 1)[(K + 1) * NP + i] = lam;
+            if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(vr, rank + 1)[i] = lam;
+            for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                if (t < n && has_left) vp[t] = lf[(size_t)(kb - 1) * n + t];
+                if (t >= n && has_right) vp[(nk + 1) * NP + (t - n)] = lf[(size_t)ke * n + (t - n)];
+            }
+            group_sync(cluster, C);
+            if (act) {
+                T *row = dS + (size_t)k * blkS + i;
+                for (uint32_t b = 0; b < 3; ++b) {
+                    const bool present = (b != 0 || k > 0) && (b != 2 || k + 1 < N);
+                    const T *lw = vp + (lk + b) * NP;
+                    const T *mw = vr + (lk + b) * NP;
+                    for (uint32_t j = 0; j < n; ++j) {
+                        const T g = present ? T(-0.5) * fma_rn(lam, lw[j], lfi * mw[j]) : T(0);
+                        row[(size_t)(b * n + j) * n] = g;
+                    }
+                }
+            }
+        }
+    }
+}
+
+}  // namespace gbdpcg

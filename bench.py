@@ -1,0 +1,380 @@
+"""Benchmark: batched PCG solves/s at relative residual 1e-6 on GB300.
+
+Workload (one "step"): 4096 independent block-tridiagonal Schur-complement
+systems, n drawn from {6, 12, 14, 24} (m = n/2), N uniform in [16, 128],
+per-system seeds 0..4095 (rank r of a multi-GPU run uses seeds r*4096 + i),
+gamma ~ N(0, 1), lambda0 = 0, FP32, block-Jacobi Phi^-1 (built on the GPU),
+exit on the relative recursive residual ||r|| <= 1e-6 ||gamma||.  All systems
+are solved by one CUDA-graph replay of the persistent cluster launches.
+
+Printed JSON line (rank 0):
+  value      solves/s with inputs resident in HBM (inputs, 1.1 GB, exceed L2)
+  e2e        solves/s through gbdpcg_plan_execute_host from pinned host
+             buffers, host<->device copies inside the timed region
+  roofline   bytes model: sizeof(T)*[(3N-2)n^2 + N n^2 + 6nN] per PCG
+             iteration per system (S and Phi^-1 block rows once, vectors
+             p, r, lambda read and written), summed over the iterations each
+             system took, per step, divided by the step's device time;
+             against the measured HBM copy bandwidth (the matrices stay on
+             chip across iterations, so this streaming-equivalent rate can
+             exceed it).  `compulsory` gives the once-per-solve bytes.
+  cpu_baseline  the oracle's C port of the same PCG on the host cores
+  plain_pcg  one system per launch with the plain (reference-scheme) kernel
+--impl reference: times the reference's CPU path on the host cores — the
+reference ships none, so the oracle's C port of its PCG (all host threads).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gbd-pcg_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "batched solves/s @rel-res 1e-6 (4096 mixed systems)"
+WORKLOAD = "mixed-batch-4096: n in {6,12,14,24}, N~U[16,128], fp32, block-Jacobi, relres 1e-6"
+TOL, MAX_ITER = 1e-6, 500
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--systems", type=int, default=4096)
+    ap.add_argument("--no-extras", action="store_true", help="skip the CPU and plain baselines")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def build_batch(rank, count, workers):
+    from gbdpcg.workload import packed_batch
+    seeds = range(rank * count, rank * count + count)
+    return packed_batch(seeds, np.float32, workers=workers, pinv_layout=1)
+
+
+def algorithmic_bytes(descs, iters, s=4):
+    it = np.asarray(iters, np.float64)
+    n = np.array([d[0] for d in descs], np.float64)
+    N = np.array([d[1] for d in descs], np.float64)
+    per_iter = s * ((3 * N - 2) * n * n + N * n * n + 6 * n * N)
+    compulsory = s * (3 * n * n * N + n * n * N + 2 * n * N)
+    flops = (2 * (3 * N - 2) * n * n + 2 * N * n * n + 10 * n * N)
+    return float((per_iter * it).sum()), float(compulsory.sum()), float((flops * it).sum())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.out.flush()
+        rows = []
+        with open(self.out.name) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        os.unlink(self.out.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({nm for r in rows for nm, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_port_baseline(Sa, Pa, ga, descs, sample, threads):
+    """The oracle's C port of the PCG on `sample` systems with `threads` host threads."""
+    from oracle import oracle as O
+    O.lib()
+    systems = []
+    for (n, N, oS, oP, oV) in descs[:sample]:
+        systems.append({"S": Sa[oS:oS + 3 * n * n * N], "Pinv": Pa[oP:oP + n * n * N],
+                        "gamma": ga[oV:oV + n * N], "lambda": np.zeros(n * N, np.float32), "n": n, "N": N})
+    t0 = time.perf_counter()
+    iters, status, used = O.pcg_batch(systems, flags=O.PINV_BLOCKDIAG | O.EXIT_RELRES, nthreads=threads,
+                                      max_iter=MAX_ITER, tol=TOL)
+    dt = time.perf_counter() - t0
+    return sample / dt, dt, used, iters, status
+
+
+def run_reference(args):
+    """--impl reference: the reference has no CPU implementation of its PCG; the
+    oracle's C port of it runs on all host threads over the same workload."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, ROOT)
+    from oracle import build_oracle
+    build_oracle.build()
+    from oracle import oracle as O
+    descs, Sa, ga, nP = build_batch(0, args.systems, os.cpu_count() or 1)
+    # block-Jacobi Phi^-1 (compact) on the host in FP64, like the GPU builder
+    Pa = np.zeros(nP, np.float32)
+    for (n, N, oS, oP, oV) in descs:
+        lo, di, up = O.unpack_cbtd(Sa[oS:oS + 3 * n * n * N], n, N)
+        Pa[oP:oP + n * n * N] = O.block_jacobi(di, "compact").astype(np.float32)
+    threads = os.cpu_count() or 1
+    # size each step to ~10 s of host work: calibrate on 64 systems
+    rate, _, _, _, _ = cpu_port_baseline(Sa, Pa, ga, descs, min(64, len(descs)), threads)
+    sample = int(min(len(descs), max(64, rate * 10.0)))
+    for _ in range(args.warmup):
+        cpu_port_baseline(Sa, Pa, ga, descs, min(sample, 64), threads)
+    times, used = [], threads
+    for _ in range(args.steps):
+        r, dt, used, _, _ = cpu_port_baseline(Sa, Pa, ga, descs, sample, threads)
+        times.append(dt)
+    total = sum(times)
+    value = sample * args.steps / total
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "systems_per_step": sample, "l2": "host run"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": used, "kind": "port",
+                             "sample": f"first {sample} of the {len(descs)} systems per step (the reference ships "
+                                       f"no CPU path; oracle/pcg_oracle.c restates its PCG)"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import gbdpcg
+    if not os.path.exists(gbdpcg.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    gbdpcg.lib()
+
+    descs, Sa, ga, nP = build_batch(rank, args.systems, max(1, (os.cpu_count() or 1) // max(1, world)))
+    count = len(descs)
+    dS = torch.from_numpy(Sa).to(dev)
+    dg = torch.from_numpy(ga).to(dev)
+    dP = torch.empty(nP, dtype=torch.float32, device=dev)
+    dl = torch.zeros(ga.size, dtype=torch.float32, device=dev)
+    h = gbdpcg.Handle(local)
+    cfg = gbdpcg.config(max_iter=MAX_ITER, exit_tol=TOL, exit_mode=gbdpcg.EXIT_RELRES, zero_guess=1)
+    plan = gbdpcg.Plan(h, layout=gbdpcg.PINV_BLOCKDIAG, cfg=cfg, packed=(descs, dS, dP, dg, dl))
+    plan.build_block_jacobi()
+    torch.cuda.synchronize()
+    launches = plan.launches()
+    stream = torch.cuda.current_stream()
+    for _ in range(max(3, args.warmup)):
+        plan.execute()
+    res = plan.results()
+    iters = [r.iters for r in res]
+    status = [r.status for r in res]
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident timing
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            plan.execute()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    clocks = clk.summary()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = world * count * args.steps / (ms / 1e3)
+
+    # ---- end to end from pinned host buffers through the C ABI
+    hS = torch.from_numpy(Sa).pin_memory()
+    hP = dP.cpu().pin_memory()
+    hg = torch.from_numpy(ga).pin_memory()
+    hl = torch.zeros(ga.size, dtype=torch.float32).pin_memory()
+    plan.execute_host(hS, hP, hg, hl)  # warm
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 4)
+    for _ in range(e2e_steps):
+        plan.execute_host(hS, hP, hg, hl, with_results=True)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = (hS.numel() + hP.numel() + hg.numel()) * 4
+    d2h = hl.numel() * 4 + count * 24
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---- accuracy against FP64 (sample) and the bytes model
+    algo_bytes, compulsory, flops = algorithmic_bytes(descs, iters)
+    lam = dl.cpu().numpy()
+    worst = 0.0
+    for (n, N, oS, oP, oV) in descs[:: max(1, count // 64)]:
+        S = Sa[oS:oS + 3 * n * n * N].astype(np.float64)
+        from gbdpcg.workload import pack_cbtd  # noqa: F401
+        Sd = S.reshape(N, 3 * n, n).transpose(0, 2, 1)
+        x = lam[oV:oV + n * N].astype(np.float64).reshape(N, n)
+        y = np.einsum("kij,kj->ki", Sd[:, :, n:2 * n], x)
+        if N > 1:
+            y[1:] += np.einsum("kij,kj->ki", Sd[1:, :, 0:n], x[:-1])
+            y[:-1] += np.einsum("kij,kj->ki", Sd[:-1, :, 2 * n:], x[1:])
+        g = ga[oV:oV + n * N].astype(np.float64)
+        worst = max(worst, float(np.linalg.norm(g - y.reshape(-1)) / np.linalg.norm(g)))
+
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    achieved = algo_bytes / (ms_step / 1e3) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            tj = json.load(f).get(WORKLOAD)
+        if tj and tj.get("systems") == count:
+            traffic = tj["dram_bytes_per_step"]
+    except (OSError, ValueError):
+        pass
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, see config)",
+        "config": {"workload": WORKLOAD, "systems_per_gpu": count, "global_batch": count * world,
+                   "seeds": f"rank*{count} + [0, {count})", "l2": "inputs (1.1 GB/GPU) larger than L2",
+                   "parallelism": f"replicas{world} (independent systems per GPU)",
+                   "launches_per_step": len(launches)},
+        "iterations": {"mean": float(np.mean(iters)), "max": int(np.max(iters)), "min": int(np.min(iters)),
+                       "all_converged": bool(all(s == 0 for s in status))},
+        "us_per_pcg_iteration": 1e3 * ms_step / float(np.max(iters)),
+        "true_relres_max_sample": worst,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic,
+                     "basis": "streaming-equivalent bytes sizeof(T)[(3N-2)n^2+Nn^2+6nN] per PCG iteration "
+                              "per system, summed over iterations, per step; peak = measured HBM copy",
+                     "compulsory": {"bytes_per_step": compulsory,
+                                    "achieved": compulsory / (ms_step / 1e3) / 1e9,
+                                    "frac": compulsory / (ms_step / 1e3) / 1e9 / hbm},
+                     "fp32_flops_per_step": flops, "fp32_tflops": flops / (ms_step / 1e3) / 1e12},
+        "e2e": {"value": world * count * e2e_steps / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": len(launches) * args.steps,
+        "clocks": clocks,
+    }
+
+    if not args.no_extras and world == 1:
+        # ---- plain PCG: one system per launch (reference scheme, cbtd Phi^-1), on a sample
+        sample = descs[:: max(1, count // 128)][:128]
+        Pc = dP.cpu().numpy()
+        t_plain, t_single, n_ok = 0.0, 0.0, 0
+        for (n, N, oS, oP, oV) in sample:
+            Pt = np.zeros((N, 3 * n, n), np.float32)
+            Pt[:, n:2 * n, :] = Pc[oP:oP + n * n * N].reshape(N, n, n)
+            tPt = torch.from_numpy(Pt.reshape(-1)).to(dev)
+            tS = dS[oS:oS + 3 * n * n * N]
+            tg = dg[oV:oV + n * N]
+            lamt = torch.zeros(n * N, device=dev)
+            cp = gbdpcg.config(max_iter=MAX_ITER, exit_tol=TOL, exit_mode=gbdpcg.EXIT_RELRES,
+                               algorithm=gbdpcg.ALGO_PLAIN, zero_guess=1)
+            cc = gbdpcg.config(max_iter=MAX_ITER, exit_tol=TOL, exit_mode=gbdpcg.EXIT_RELRES, zero_guess=1)
+            h.solve(tS, tPt, tg, lamt, n, N, gbdpcg.PINV_CBTD, cp)  # warm
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            h.solve(tS, tPt, tg, lamt, n, N, gbdpcg.PINV_CBTD, cp, sync=False)
+            b.record(stream)
+            b.synchronize()
+            t_plain += a.elapsed_time(b)
+            a.record(stream)
+            h.solve(tS, dP[oP:oP + n * n * N], tg, lamt, n, N, gbdpcg.PINV_BLOCKDIAG, cc, sync=False)
+            b.record(stream)
+            b.synchronize()
+            t_single += a.elapsed_time(b)
+            n_ok += 1
+        plain_rate = n_ok / (t_plain / 1e3)
+        line["plain_pcg"] = {"value": plain_rate, "unit": "solves/s",
+                             "sample": f"{n_ok} systems of the batch, one cooperative launch each "
+                                       "(plain kernel, cbtd Phi^-1)",
+                             "batched_speedup": value / plain_rate,
+                             "single_cluster_solve_value": n_ok / (t_single / 1e3)}
+        # ---- host-core port of the same PCG (the CPU baseline)
+        threads = os.cpu_count() or 1
+        Pn = dP.cpu().numpy()
+        rate, _, _, _, _ = cpu_port_baseline(Sa, Pn, ga, descs, min(64, count), threads)
+        csample = int(min(count, max(64, rate * 10.0)))
+        rate, dt, used, _, _ = cpu_port_baseline(Sa, Pn, ga, descs, csample, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": "solves/s", "cores": used, "kind": "port",
+                                "sample": f"first {csample} of the {count} systems, oracle/pcg_oracle.c, "
+                                          f"{dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+    plan.close()
+    h.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,943 @@
+// Host runtime and C ABI (include/gbdpcg.h) of the GB300 PCG solver.
+//
+//   * variant registry: the cluster-kernel instantiations, their register
+//     budget (max threads per CTA) and shared-memory plans;
+//   * planner: assigns each system a kernel variant (block-size bound NP,
+//     Phi^-1 storage, precision), a cluster size C and a CTA size, groups
+//     systems with the same launch shape into classes, sorts each class
+//     longest first into a device work list;
+//   * executor: one persistent cluster launch per class (fed by a device work
+//     queue), the classes spread over a few streams, all captured in one CUDA
+//     graph that also resets the queues;
+//   * the single-system entry points (host and device pointers), which pass
+//     the system descriptor by value and need no queue;
+//   * the plain algorithm (one CTA per knot, cooperative launch) for n > 32.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/gbdpcg.h"
+#include "pcg_types.h"
+#include "pcg_variants.h"
+
+namespace gbdpcg {
+cudaError_t launch_block_jacobi(bool f64, bool fp64_compute, const SysDesc *d_descs,
+                                const uint64_t *d_prefix, uint32_t nsys, uint64_t total_knots,
+                                int tri_layout, cudaStream_t stream);
+}
+
+using namespace gbdpcg;
+
+namespace {
+
+thread_local std::string t_last_error;
+
+size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
+
+int fail(int code, const std::string &msg) {
+    t_last_error = msg;
+    return code;
+}
+
+#define GB_CUDA(call)                                                                         \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(GBDPCG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+// ------------------------------------------------------------------ variant registry
+struct VariantInfo {
+    KernelVariant v;
+    int max_threads = 0;  // from the register budget (cudaFuncAttributes)
+    int regs = 0;
+    size_t smem_set = 0;  // max dynamic smem attribute already set
+    bool nonportable = false;
+};
+
+struct Registry {
+    std::vector<VariantInfo> list;
+    int max_smem_optin = 0;
+    int sm_count = 0;
+};
+
+std::mutex g_reg_mu;
+std::map<int, std::unique_ptr<Registry>> g_registries;  // per device
+
+const int kNPs[] = {6, 8, 12, 14, 16, 24, 32};
+
+int np_for(uint32_t n) {
+    for (int np : kNPs)
+        if ((int)n <= np) return np;
+    return 0;
+}
+
+int get_registry(int device, Registry **out) {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    auto it = g_registries.find(device);
+    if (it != g_registries.end()) {
+        *out = it->second.get();
+        return GBDPCG_SUCCESS;
+    }
+    auto reg = std::make_unique<Registry>();
+    KernelVariant buf[16];
+    int (*fns[])(KernelVariant *) = {variants_np6, variants_np8, variants_np12, variants_np14,
+                                     variants_np16, variants_np24, variants_np32};
+    for (auto fn : fns) {
+        const int c = fn(buf);
+        for (int i = 0; i < c; ++i) {
+            VariantInfo vi;
+            vi.v = buf[i];
+            cudaFuncAttributes attr;
+            GB_CUDA(cudaFuncGetAttributes(&attr, vi.v.func));
+            vi.max_threads = attr.maxThreadsPerBlock / 32 * 32;
+            vi.regs = attr.numRegs;
+            reg->list.push_back(vi);
+        }
+    }
+    GB_CUDA(cudaDeviceGetAttribute(&reg->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                   device));
+    GB_CUDA(cudaDeviceGetAttribute(&reg->sm_count, cudaDevAttrMultiProcessorCount, device));
+    *out = reg.get();
+    g_registries[device] = std::move(reg);
+    return GBDPCG_SUCCESS;
+}
+
+VariantInfo *find_variant(Registry *reg, bool f64, bool acc64, int np, bool ptri, bool mreg) {
+    for (auto &vi : reg->list)
+        if (vi.v.f64 == (int)f64 && vi.v.acc64 == (int)(acc64 || f64) && vi.v.np == np &&
+            vi.v.ptri == (int)ptri && vi.v.mreg == (int)mreg)
+            return &vi;
+    return nullptr;
+}
+
+int prepare_variant(VariantInfo *vi, size_t smem, uint32_t C) {
+    if (smem > 48 * 1024 && smem > vi->smem_set) {
+        GB_CUDA(cudaFuncSetAttribute(vi->v.func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+        vi->smem_set = smem;
+    }
+    if (C > 8 && !vi->nonportable) {
+        GB_CUDA(cudaFuncSetAttribute(vi->v.func, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        vi->nonportable = true;
+    }
+    return GBDPCG_SUCCESS;
+}
+
+// ------------------------------------------------------------------ device buffers
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    int ensure(size_t want) {
+        if (want <= bytes) return GBDPCG_SUCCESS;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (cudaMalloc(&p, want) != cudaSuccess)
+            return fail(GBDPCG_ERR_NO_MEMORY, "cudaMalloc of " + std::to_string(want) + " bytes");
+        bytes = want;
+        return GBDPCG_SUCCESS;
+    }
+    template <typename T>
+    T *as(size_t byte_off = 0) const {
+        return reinterpret_cast<T *>(static_cast<char *>(p) + byte_off);
+    }
+};
+
+// ------------------------------------------------------------------ launch shapes
+struct Shape {
+    VariantInfo *vi = nullptr;
+    uint32_t C = 0, threads = 0, K = 0;
+    bool plain = false;
+};
+
+// Threads per CTA the tuner allows for a variant (cap), before the register limit.
+uint32_t default_thread_cap(const VariantInfo *vi) { return (uint32_t)vi->max_threads; }
+
+int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layout,
+                 const gbdpcg_config &cfg, Shape *out) {
+    Shape s;
+    const int np = np_for(n);
+    const bool want_plain = cfg.algorithm == GBDPCG_ALGO_PLAIN || np == 0;
+    if (want_plain) {
+        if (layout != GBDPCG_PINV_CBTD)
+            return fail(GBDPCG_ERR_UNSUPPORTED, "plain algorithm needs a cbtd Phi^-1");
+        s.plain = true;
+        *out = s;
+        return GBDPCG_SUCCESS;
+    }
+    const bool ptri = layout == GBDPCG_PINV_CBTD;
+    const bool acc64 = cfg.dot_precision == GBDPCG_DOT_FP64;
+    std::vector<bool> storages;
+    if (cfg.storage == GBDPCG_STORAGE_REGISTERS) storages = {true};
+    else if (cfg.storage == GBDPCG_STORAGE_SHARED) storages = {false};
+    else storages = {true, false};
+    for (bool mreg : storages) {
+        VariantInfo *vi = find_variant(reg, f64, acc64, np, ptri, mreg);
+        if (!vi) continue;
+        uint32_t cap = cfg.max_threads ? cfg.max_threads : default_thread_cap(vi);
+        cap = std::min<uint32_t>(cap, (uint32_t)vi->max_threads);
+        const uint32_t c_lo = cfg.cluster_size ? cfg.cluster_size : 1;
+        const uint32_t c_hi = cfg.cluster_size ? cfg.cluster_size : 16;
+        for (uint32_t C = c_lo; C <= c_hi; ++C) {
+            if (C > 8 && (C & (C - 1))) continue;  // large clusters: powers of two only
+            const uint32_t K = (N + C - 1) / C;
+            if ((size_t)K * n > cap) continue;
+            if (vi->v.smem_bytes(K) > (size_t)reg->max_smem_optin) continue;
+            s.vi = vi;
+            s.C = C;
+            s.K = K;
+            s.threads = std::max<uint32_t>(32, (K * n + 31) / 32 * 32);
+            *out = s;
+            return GBDPCG_SUCCESS;
+        }
+    }
+    if (cfg.algorithm == GBDPCG_ALGO_AUTO && layout == GBDPCG_PINV_CBTD) {
+        s.plain = true;  // too large for 16 CTAs of rows: one CTA per knot
+        *out = s;
+        return GBDPCG_SUCCESS;
+    }
+    return fail(GBDPCG_ERR_UNSUPPORTED, "no cluster shape holds n=" + std::to_string(n) +
+                                            " N=" + std::to_string(N));
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ handle
+constexpr size_t kWorkspaceBytes = 4096;  // 2 result slots + 256 pad + descriptor + prefix
+
+struct gbdpcg_handle_s {
+    int device = 0;
+    Registry *reg = nullptr;
+    DevBuf ws;          // fixed-size: result slots, one descriptor (never reallocated)
+    DevBuf host_io;     // host-pointer solve: S, Pinv, gamma, lambda
+    DevBuf plain_scratch;  // plain algorithm: r, p, dot partials
+    SysResult *d_last = nullptr;
+    cudaStream_t last_stream = nullptr;
+    bool last_f64 = false;
+};
+
+namespace {
+
+struct HandleScope {  // makes the handle's device current for the duration of a call
+    int prev = -1;
+    explicit HandleScope(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~HandleScope() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+void to_public(const SysResult &r, gbdpcg_result *o) {
+    o->iters = r.iters;
+    o->status = r.status;
+    o->eta = r.eta;
+    o->relres = (r.rr >= 0 && r.gg > 0) ? sqrt(r.rr / r.gg) : (r.rr >= 0 ? 0.0 : -1.0);
+}
+
+SysDesc make_desc(const void *S, const void *P, const void *g, const void *l0, void *l,
+                  uint32_t n, uint32_t N, const gbdpcg_config &cfg, uint32_t layout,
+                  uint32_t result_slot) {
+    SysDesc d;
+    memset(&d, 0, sizeof(d));
+    d.S = S;
+    d.P = P;
+    d.gamma = g;
+    d.lambda0 = l0;
+    d.lambda = l;
+    d.tol = cfg.exit_tol;
+    d.inner_tol = 0;
+    d.n = n;
+    d.N = N;
+    d.max_iter = cfg.max_iter;
+    d.flags = (cfg.exit_mode == GBDPCG_EXIT_RELRES ? SYS_EXIT_RELRES : 0u) |
+              (layout == GBDPCG_PINV_CBTD ? SYS_PINV_TRI : 0u) |
+              (cfg.zero_guess ? SYS_LAMBDA0_ZERO : 0u);
+    d.result = result_slot;
+    return d;
+}
+
+int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
+    if (!cfg) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "config is NULL");
+    if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad pinv_layout");
+    if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FP64 ||
+        cfg->algorithm > GBDPCG_ALGO_PLAIN || cfg->storage > GBDPCG_STORAGE_SHARED ||
+        cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1)
+        return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad config field");
+    if (!(cfg->exit_tol >= 0)) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "exit_tol must be >= 0");
+    return GBDPCG_SUCCESS;
+}
+
+// Launch the plain algorithm for one system (cooperative, N CTAs of 64 threads).
+int launch_plain(gbdpcg_handle_s *h, bool f64, const SysDesc &d, SysResult *d_res,
+                 cudaStream_t stream, DevBuf &scratch) {
+    const size_t s = f64 ? 8 : 4;
+    const size_t vec = (size_t)d.n * d.N * s;
+    const size_t need = 2 * vec + 2 * (size_t)d.N * s + 256;
+    int rc = scratch.ensure(need);
+    if (rc) return rc;
+    char *base = scratch.as<char>();
+    void *d_r = base, *d_p = base + vec, *d_p1 = base + 2 * vec, *d_p2 = base + 2 * vec + d.N * s;
+    const void *func = plain_kernel_ptr(f64);
+    const size_t smem = plain_smem_bytes(f64, d.n, d.N);
+    if (smem > (size_t)h->reg->max_smem_optin)
+        return fail(GBDPCG_ERR_UNSUPPORTED, "plain algorithm: block row exceeds shared memory");
+    if (smem > 48 * 1024)
+        GB_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, 64, smem));
+    if ((int64_t)per_sm * h->reg->sm_count < (int64_t)d.N)
+        return fail(GBDPCG_ERR_UNSUPPORTED, "plain algorithm: knots exceed co-resident CTAs");
+    uint32_t n = d.n, N = d.N, mi = d.max_iter, fl = d.flags;
+    double tol = d.tol;
+    const void *S = d.S, *P = d.P, *g = d.gamma, *l0 = d.lambda0;
+    void *l = d.lambda;
+    void *args[] = {&S, &P, &g, &l0, &l, &d_r, &d_p, &d_p1, &d_p2, &n, &N, &mi, &tol, &fl, &d_res};
+    GB_CUDA(cudaLaunchCooperativeKernel(func, dim3(N), dim3(64), args, smem, stream));
+    return GBDPCG_SUCCESS;
+}
+
+int launch_cluster(const Shape &sh, const LaunchParams &lp, uint32_t grid_clusters,
+                   cudaStream_t stream) {
+    const size_t smem = sh.vi->v.smem_bytes(lp.kmax);
+    int rc = prepare_variant(sh.vi, smem, sh.C);
+    if (rc) return rc;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = sh.C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(grid_clusters * sh.C);
+    cfg.blockDim = dim3(sh.threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void *args[] = {const_cast<LaunchParams *>(&lp)};
+    GB_CUDA(cudaLaunchKernelExC(&cfg, sh.vi->v.func, args));
+    return GBDPCG_SUCCESS;
+}
+
+int max_active_clusters(const Shape &sh, size_t smem, int *out) {
+    int rc = prepare_variant(sh.vi, smem, sh.C);
+    if (rc) return rc;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = sh.C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(sh.C);
+    cfg.blockDim = dim3(sh.threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GB_CUDA(cudaOccupancyMaxActiveClusters(out, sh.vi->v.func, &cfg));
+    return GBDPCG_SUCCESS;
+}
+
+// One system, device pointers; result left in h->d_last.
+int solve_one(gbdpcg_handle_s *h, bool f64, const SysDesc &d0, const gbdpcg_config &cfg,
+              uint32_t layout, cudaStream_t stream) {
+    SysResult *d_res = h->ws.as<SysResult>();
+    int rc;
+    SysDesc d = d0;
+    d.result = 0;
+    Shape sh;
+    rc = choose_shape(h->reg, f64, d.n, d.N, layout, cfg, &sh);
+    if (rc) return rc;
+    h->d_last = d_res;
+    h->last_stream = stream;
+    if (sh.plain) {
+        return launch_plain(h, f64, d, d_res, stream, h->plain_scratch);
+    }
+    LaunchParams lp;
+    memset(&lp, 0, sizeof(lp));
+    lp.descs = nullptr;
+    lp.order = nullptr;
+    lp.count = 1;
+    lp.kmax = sh.K;
+    lp.queue = nullptr;
+    lp.results = d_res;
+    lp.one = d;
+    return launch_cluster(sh, lp, 1, stream);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ plan
+struct PlanClass {
+    Shape sh;
+    uint32_t kmax = 0;
+    std::vector<uint32_t> items;  // indices into descs
+    uint32_t order_off = 0;
+    uint32_t grid_clusters = 0;
+};
+
+struct gbdpcg_plan_s {
+    gbdpcg_handle_s *h = nullptr;
+    bool f64 = false;
+    uint32_t layout = 0;
+    gbdpcg_config cfg;
+    uint32_t count = 0;
+    std::vector<SysDesc> descs;
+    std::vector<PlanClass> classes;
+    std::vector<uint32_t> plain_items;
+    DevBuf d_descs, d_order, d_queues, d_results, d_prefix;
+    DevBuf plain_scratch;
+    uint64_t total_knots = 0;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> events;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    // packed plans: the device arenas and their sizes in bytes
+    bool packed = false;
+    const void *arena_S = nullptr, *arena_P = nullptr, *arena_g = nullptr;
+    void *arena_l = nullptr;
+    size_t bytes_S = 0, bytes_P = 0, bytes_vec = 0;
+    ~gbdpcg_plan_s() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        if (graph) cudaGraphDestroy(graph);
+        for (auto s : streams) cudaStreamDestroy(s);
+        for (auto e : events) cudaEventDestroy(e);
+    }
+};
+
+namespace {
+
+int plan_enqueue(gbdpcg_plan_s *p, cudaStream_t stream) {
+    const uint32_t nc = (uint32_t)p->classes.size();
+    if (nc) GB_CUDA(cudaMemsetAsync(p->d_queues.p, 0, sizeof(uint32_t) * nc, stream));
+    GB_CUDA(cudaEventRecord(p->events[0], stream));
+    const uint32_t ns = (uint32_t)p->streams.size();
+    for (uint32_t c = 0; c < nc; ++c) {
+        cudaStream_t s = p->streams[c % ns];
+        if (c < ns) GB_CUDA(cudaStreamWaitEvent(s, p->events[0], 0));
+        const PlanClass &pc = p->classes[c];
+        LaunchParams lp;
+        memset(&lp, 0, sizeof(lp));
+        lp.descs = p->d_descs.as<SysDesc>();
+        lp.order = p->d_order.as<uint32_t>() + pc.order_off;
+        lp.count = (uint32_t)pc.items.size();
+        lp.kmax = pc.kmax;
+        lp.queue = p->d_queues.as<uint32_t>() + c;
+        lp.results = p->d_results.as<SysResult>();
+        int rc = launch_cluster(pc.sh, lp, pc.grid_clusters, s);
+        if (rc) return rc;
+    }
+    for (uint32_t s = 0; s < std::min(ns, nc); ++s) {
+        GB_CUDA(cudaEventRecord(p->events[1 + s], p->streams[s]));
+        GB_CUDA(cudaStreamWaitEvent(stream, p->events[1 + s], 0));
+    }
+    for (uint32_t idx : p->plain_items) {
+        int rc = launch_plain(p->h, p->f64, p->descs[idx], p->d_results.as<SysResult>() + idx,
+                              stream, p->plain_scratch);
+        if (rc) return rc;
+    }
+    return GBDPCG_SUCCESS;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+int gbdpcg_version(void) { return GBDPCG_VERSION; }
+
+const char *gbdpcg_status_string(int s) {
+    switch (s) {
+        case GBDPCG_SUCCESS: return "success";
+        case GBDPCG_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case GBDPCG_ERR_UNSUPPORTED: return "unsupported size or option";
+        case GBDPCG_ERR_CUDA: return "CUDA error";
+        case GBDPCG_ERR_NO_MEMORY: return "out of device memory";
+        case GBDPCG_ERR_NOT_CONVERGED: return "not converged";
+        default: return "unknown status";
+    }
+}
+
+const char *gbdpcg_last_error(void) { return t_last_error.c_str(); }
+
+void gbdpcg_config_init(gbdpcg_config *cfg) {
+    if (!cfg) return;
+    memset(cfg, 0, sizeof(*cfg));
+    cfg->exit_tol = 1e-6;
+    cfg->max_iter = 25;
+    cfg->exit_mode = GBDPCG_EXIT_REFERENCE;
+    cfg->dot_precision = GBDPCG_DOT_NATIVE;
+    cfg->algorithm = GBDPCG_ALGO_AUTO;
+    cfg->use_graph = 1;
+}
+
+int gbdpcg_create(gbdpcg_handle_t *handle, int device) {
+    if (!handle) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "handle is NULL");
+    int ndev = 0;
+    GB_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad device");
+    HandleScope scope(device);
+    auto h = std::make_unique<gbdpcg_handle_s>();
+    h->device = device;
+    int rc = get_registry(device, &h->reg);
+    if (rc) return rc;
+    rc = h->ws.ensure(kWorkspaceBytes);
+    if (rc) return rc;
+    *handle = h.release();
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_destroy(gbdpcg_handle_t handle) {
+    if (!handle) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "handle is NULL");
+    HandleScope scope(handle->device);
+    delete handle;
+    return GBDPCG_SUCCESS;
+}
+
+static int solve_dev(gbdpcg_handle_t h, bool f64, const void *S, const void *P, uint32_t layout,
+                     const void *g, void *l, uint32_t n, uint32_t N, const gbdpcg_config *cfg,
+                     gbdpcg_result *result, cudaStream_t stream) {
+    if (!h || !S || !P || !g || !l) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (n == 0 || N == 0) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "n and N must be positive");
+    int rc = check_cfg(cfg, layout);
+    if (rc) return rc;
+    HandleScope scope(h->device);
+    SysDesc d = make_desc(S, P, g, l, l, n, N, *cfg, layout, 0);
+    rc = solve_one(h, f64, d, *cfg, layout, stream);
+    if (rc) return rc;
+    h->last_f64 = f64;
+    if (result) return gbdpcg_last_result(h, result);
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_solve_dev_f32(gbdpcg_handle_t h, const float *d_S, const float *d_Pinv,
+                         uint32_t pinv_layout, const float *d_gamma, float *d_lambda, uint32_t n,
+                         uint32_t N, const gbdpcg_config *cfg, gbdpcg_result *result,
+                         gbdpcg_stream_t stream) {
+    return solve_dev(h, false, d_S, d_Pinv, pinv_layout, d_gamma, d_lambda, n, N, cfg, result,
+                     (cudaStream_t)stream);
+}
+
+int gbdpcg_solve_dev_f64(gbdpcg_handle_t h, const double *d_S, const double *d_Pinv,
+                         uint32_t pinv_layout, const double *d_gamma, double *d_lambda,
+                         uint32_t n, uint32_t N, const gbdpcg_config *cfg,
+                         gbdpcg_result *result, gbdpcg_stream_t stream) {
+    return solve_dev(h, true, d_S, d_Pinv, pinv_layout, d_gamma, d_lambda, n, N, cfg, result,
+                     (cudaStream_t)stream);
+}
+
+int gbdpcg_last_result(gbdpcg_handle_t h, gbdpcg_result *result) {
+    if (!h || !result || !h->d_last) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "no result");
+    HandleScope scope(h->device);
+    SysResult r;
+    GB_CUDA(cudaMemcpyAsync(&r, h->d_last, sizeof(r), cudaMemcpyDeviceToHost, h->last_stream));
+    GB_CUDA(cudaStreamSynchronize(h->last_stream));
+    to_public(r, result);
+    return GBDPCG_SUCCESS;
+}
+
+static int block_jacobi(gbdpcg_handle_t h, bool f64, const void *S, void *P, uint32_t layout,
+                        uint32_t n, uint32_t N, cudaStream_t stream) {
+    if (!h || !S || !P) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (n == 0 || N == 0 || n > 32) return fail(GBDPCG_ERR_UNSUPPORTED, "block-Jacobi needs 1 <= n <= 32");
+    if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad layout");
+    HandleScope scope(h->device);
+    // descriptor + prefix live in the handle workspace, after the result slots
+    SysDesc d;
+    memset(&d, 0, sizeof(d));
+    d.S = S;
+    d.P = P;
+    d.n = n;
+    d.N = N;
+    char *base = h->ws.as<char>(sizeof(SysResult) * 2 + 256);
+    uint64_t prefix = 0;
+    GB_CUDA(cudaMemcpyAsync(base, &d, sizeof(d), cudaMemcpyHostToDevice, stream));
+    GB_CUDA(cudaMemcpyAsync(base + sizeof(SysDesc), &prefix, sizeof(prefix),
+                            cudaMemcpyHostToDevice, stream));
+    GB_CUDA(launch_block_jacobi(f64, false, reinterpret_cast<SysDesc *>(base),
+                                reinterpret_cast<uint64_t *>(base + sizeof(SysDesc)), 1, N,
+                                layout == GBDPCG_PINV_CBTD, stream));
+    // the host-side sources above must outlive the copies
+    GB_CUDA(cudaStreamSynchronize(stream));
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_block_jacobi_f32(gbdpcg_handle_t h, const float *d_S, float *d_Pinv,
+                            uint32_t pinv_layout, uint32_t n, uint32_t N,
+                            gbdpcg_stream_t stream) {
+    return block_jacobi(h, false, d_S, d_Pinv, pinv_layout, n, N, (cudaStream_t)stream);
+}
+
+int gbdpcg_block_jacobi_f64(gbdpcg_handle_t h, const double *d_S, double *d_Pinv,
+                            uint32_t pinv_layout, uint32_t n, uint32_t N,
+                            gbdpcg_stream_t stream) {
+    return block_jacobi(h, true, d_S, d_Pinv, pinv_layout, n, N, (cudaStream_t)stream);
+}
+
+// ---- host-pointer solves (per-thread handle on the current device)
+static int thread_handle(gbdpcg_handle_t *out) {
+    static thread_local std::map<int, gbdpcg_handle_t> handles;
+    int dev = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    auto it = handles.find(dev);
+    if (it != handles.end()) {
+        *out = it->second;
+        return GBDPCG_SUCCESS;
+    }
+    gbdpcg_handle_t h = nullptr;
+    int rc = gbdpcg_create(&h, dev);
+    if (rc) return rc;
+    handles[dev] = h;
+    *out = h;
+    return GBDPCG_SUCCESS;
+}
+
+static int solve_host(bool f64, const void *S, const void *P, const void *g, void *l, uint32_t n,
+                      uint32_t N, const gbdpcg_config *cfg, gbdpcg_result *result) {
+    if (!S || !g || !l) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (n == 0 || N == 0) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "n and N must be positive");
+    gbdpcg_config c;
+    if (cfg) c = *cfg;
+    else gbdpcg_config_init(&c);
+    const uint32_t layout = P ? GBDPCG_PINV_CBTD : GBDPCG_PINV_BLOCKDIAG;
+    int rc = check_cfg(&c, layout);
+    if (rc) return rc;
+    gbdpcg_handle_t h = nullptr;
+    rc = thread_handle(&h);
+    if (rc) return rc;
+    const size_t s = f64 ? 8 : 4;
+    const size_t mat = (size_t)3 * n * n * N * s, vec = (size_t)n * N * s;
+    // when Phi^-1 is built here, the plain algorithm still needs the cbtd layout
+    const uint32_t build_layout =
+        (!P && (c.algorithm == GBDPCG_ALGO_PLAIN || n > 32)) ? GBDPCG_PINV_CBTD : layout;
+    const size_t pmat = P || build_layout == GBDPCG_PINV_CBTD ? mat : (size_t)n * n * N * s;
+    rc = h->host_io.ensure(mat + pmat + 2 * vec + 1024);
+    if (rc) return rc;
+    char *dS = h->host_io.as<char>(), *dP = dS + round_up(mat, 256),
+         *dg = dP + round_up(pmat, 256), *dl = dg + round_up(vec, 256);
+    cudaStream_t st = nullptr;
+    GB_CUDA(cudaMemcpyAsync(dS, S, mat, cudaMemcpyHostToDevice, st));
+    if (P) GB_CUDA(cudaMemcpyAsync(dP, P, mat, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(dg, g, vec, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(dl, l, vec, cudaMemcpyHostToDevice, st));
+    if (!P) {
+        if (n > 32) return fail(GBDPCG_ERR_UNSUPPORTED, "block-Jacobi builder needs n <= 32");
+        rc = block_jacobi(h, f64, dS, dP, build_layout, n, N, st);
+        if (rc) return rc;
+    }
+    rc = solve_dev(h, f64, dS, dP, build_layout, dg, dl, n, N, &c, nullptr, st);
+    if (rc) return rc;
+    GB_CUDA(cudaMemcpyAsync(l, dl, vec, cudaMemcpyDeviceToHost, st));
+    gbdpcg_result r;
+    rc = gbdpcg_last_result(h, &r);
+    if (rc) return rc;
+    if (result) *result = r;
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_solve_f32(const float *S, const float *Pinv, const float *gamma, float *lambda,
+                     uint32_t n, uint32_t N, const gbdpcg_config *cfg, gbdpcg_result *result) {
+    return solve_host(false, S, Pinv, gamma, lambda, n, N, cfg, result);
+}
+
+int gbdpcg_solve_f64(const double *S, const double *Pinv, const double *gamma, double *lambda,
+                     uint32_t n, uint32_t N, const gbdpcg_config *cfg, gbdpcg_result *result) {
+    return solve_host(true, S, Pinv, gamma, lambda, n, N, cfg, result);
+}
+
+int gbdpcg_adjoint_dev_f32(gbdpcg_handle_t h, const float *d_S, const float *d_Pinv,
+                           uint32_t pinv_layout, const float *d_lambda, const float *d_grad_lambda,
+                           float *d_grad_gamma, float *d_grad_S, uint32_t n, uint32_t N,
+                           const gbdpcg_config *cfg, gbdpcg_result *result,
+                           gbdpcg_stream_t stream) {
+    if (!h || !d_S || !d_Pinv || !d_lambda || !d_grad_lambda || !d_grad_gamma || !d_grad_S)
+        return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (n == 0 || N == 0) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "n and N must be positive");
+    int rc = check_cfg(cfg, pinv_layout);
+    if (rc) return rc;
+    if (cfg->algorithm == GBDPCG_ALGO_PLAIN || n > 32)
+        return fail(GBDPCG_ERR_UNSUPPORTED, "adjoint runs on the cluster solver (n <= 32)");
+    HandleScope scope(h->device);
+    SysDesc d = make_desc(d_S, d_Pinv, d_grad_lambda, nullptr, d_grad_gamma, n, N, *cfg,
+                          pinv_layout, 0);
+    d.flags |= SYS_ADJOINT | SYS_LAMBDA0_ZERO;
+    d.lam_fwd = d_lambda;
+    d.dS = d_grad_S;
+    rc = solve_one(h, false, d, *cfg, pinv_layout, (cudaStream_t)stream);
+    if (rc) return rc;
+    h->last_f64 = false;
+    if (result) return gbdpcg_last_result(h, result);
+    return GBDPCG_SUCCESS;
+}
+
+// ---- plans
+int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *systems, uint32_t count,
+                       uint32_t pinv_layout, const gbdpcg_config *cfg, gbdpcg_plan_t *plan) {
+    if (!h || !systems || !plan || count == 0)
+        return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer or empty batch");
+    if (dtype != 0 && dtype != 1) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "dtype must be 0 or 1");
+    int rc = check_cfg(cfg, pinv_layout);
+    if (rc) return rc;
+    HandleScope scope(h->device);
+    auto p = std::make_unique<gbdpcg_plan_s>();
+    p->h = h;
+    p->f64 = dtype == 1;
+    p->layout = pinv_layout;
+    p->cfg = *cfg;
+    p->count = count;
+    const bool adjoint = systems[0].lambda_fwd != nullptr;
+    std::map<std::tuple<const void *, uint32_t, uint32_t>, uint32_t> class_of;
+    std::vector<uint64_t> prefix(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const gbdpcg_system &s = systems[i];
+        if (!s.S || !s.Pinv || !s.gamma || !s.lambda || s.n == 0 || s.N == 0)
+            return fail(GBDPCG_ERR_INVALID_ARGUMENT, "system " + std::to_string(i) + " is incomplete");
+        if ((s.lambda_fwd != nullptr) != adjoint || (adjoint && !s.dS))
+            return fail(GBDPCG_ERR_INVALID_ARGUMENT, "mixed forward and adjoint systems");
+        SysDesc d = make_desc(s.S, s.Pinv, s.gamma, s.lambda, s.lambda, s.n, s.N, *cfg,
+                              pinv_layout, i);
+        if (adjoint) {
+            d.flags |= SYS_ADJOINT | SYS_LAMBDA0_ZERO;
+            d.lam_fwd = s.lambda_fwd;
+            d.dS = s.dS;
+        }
+        prefix[i] = p->total_knots;
+        p->total_knots += s.N;
+        p->descs.push_back(d);
+        Shape sh;
+        rc = choose_shape(h->reg, p->f64, s.n, s.N, pinv_layout, *cfg, &sh);
+        if (rc) return rc;
+        if (sh.plain) {
+            if (adjoint) return fail(GBDPCG_ERR_UNSUPPORTED, "adjoint needs n <= 32");
+            p->plain_items.push_back(i);
+            continue;
+        }
+        auto key = std::make_tuple((const void *)sh.vi, sh.C, sh.threads);
+        auto it = class_of.find(key);
+        if (it == class_of.end()) {
+            PlanClass pc;
+            pc.sh = sh;
+            it = class_of.emplace(key, (uint32_t)p->classes.size()).first;
+            p->classes.push_back(pc);
+        }
+        PlanClass &pc = p->classes[it->second];
+        pc.items.push_back(i);
+        pc.kmax = std::max(pc.kmax, sh.K);
+    }
+    // longest first within a class; classes with the most work first
+    auto cost = [&](uint32_t i) { return (double)p->descs[i].n * p->descs[i].n * p->descs[i].N; };
+    for (auto &pc : p->classes)
+        std::stable_sort(pc.items.begin(), pc.items.end(),
+                         [&](uint32_t a, uint32_t b) { return cost(a) > cost(b); });
+    std::stable_sort(p->classes.begin(), p->classes.end(),
+                     [&](const PlanClass &a, const PlanClass &b) {
+                         return cost(a.items[0]) > cost(b.items[0]);
+                     });
+    std::vector<uint32_t> order;
+    for (auto &pc : p->classes) {
+        pc.order_off = (uint32_t)order.size();
+        order.insert(order.end(), pc.items.begin(), pc.items.end());
+        int active = 0;
+        rc = max_active_clusters(pc.sh, pc.sh.vi->v.smem_bytes(pc.kmax), &active);
+        if (rc) return rc;
+        if (active <= 0)
+            return fail(GBDPCG_ERR_UNSUPPORTED, "cluster shape cannot be scheduled (C=" +
+                                                    std::to_string(pc.sh.C) + ")");
+        pc.grid_clusters = std::min<uint32_t>((uint32_t)pc.items.size(), (uint32_t)active);
+    }
+    const size_t nc = p->classes.size();
+    if ((rc = p->d_descs.ensure(sizeof(SysDesc) * count))) return rc;
+    if ((rc = p->d_order.ensure(sizeof(uint32_t) * std::max<size_t>(1, order.size())))) return rc;
+    if ((rc = p->d_queues.ensure(sizeof(uint32_t) * std::max<size_t>(1, nc)))) return rc;
+    if ((rc = p->d_results.ensure(sizeof(SysResult) * count))) return rc;
+    if ((rc = p->d_prefix.ensure(sizeof(uint64_t) * count))) return rc;
+    GB_CUDA(cudaMemcpy(p->d_descs.p, p->descs.data(), sizeof(SysDesc) * count, cudaMemcpyHostToDevice));
+    if (!order.empty())
+        GB_CUDA(cudaMemcpy(p->d_order.p, order.data(), sizeof(uint32_t) * order.size(),
+                           cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(p->d_prefix.p, prefix.data(), sizeof(uint64_t) * count, cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemset(p->d_results.p, 0, sizeof(SysResult) * count));
+    const uint32_t ns = (uint32_t)std::min<size_t>(4, std::max<size_t>(1, nc));
+    for (uint32_t s = 0; s < ns; ++s) {
+        cudaStream_t st;
+        GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        p->streams.push_back(st);
+    }
+    for (uint32_t e = 0; e < ns + 1; ++e) {
+        cudaEvent_t ev;
+        GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        p->events.push_back(ev);
+    }
+    *plan = p.release();
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_execute(gbdpcg_plan_t p, gbdpcg_stream_t stream_) {
+    if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    HandleScope scope(p->h->device);
+    cudaStream_t stream = (cudaStream_t)stream_;
+    const bool graph = p->cfg.use_graph && p->plain_items.empty();
+    if (!graph) return plan_enqueue(p, stream);
+    if (!p->gexec) {
+        cudaStream_t cap;
+        GB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) {
+            cudaStreamDestroy(cap);
+            GB_CUDA(e);
+        }
+        int rc = plan_enqueue(p, cap);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(cap, &g);
+        cudaStreamDestroy(cap);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        GB_CUDA(e);
+        p->graph = g;
+        GB_CUDA(cudaGraphInstantiate(&p->gexec, g, 0));
+    }
+    GB_CUDA(cudaGraphLaunch(p->gexec, stream));
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_create_packed(gbdpcg_handle_t h, int dtype, const gbdpcg_packed_system *systems,
+                              uint32_t count, const void *d_S, const void *d_Pinv,
+                              const void *d_gamma, void *d_lambda, uint32_t pinv_layout,
+                              const gbdpcg_config *cfg, gbdpcg_plan_t *plan) {
+    if (!systems || !d_S || !d_Pinv || !d_gamma || !d_lambda || !plan || count == 0)
+        return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer or empty batch");
+    if (dtype != 0 && dtype != 1) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "dtype must be 0 or 1");
+    const size_t s = dtype ? 8 : 4;
+    std::vector<gbdpcg_system> sys(count);
+    size_t eS = 0, eP = 0, eV = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const gbdpcg_packed_system &q = systems[i];
+        const size_t n = q.n, N = q.N;
+        const size_t pm = pinv_layout == GBDPCG_PINV_CBTD ? 3 * n * n * N : n * n * N;
+        sys[i].S = static_cast<const char *>(d_S) + q.S_off * s;
+        sys[i].Pinv = static_cast<const char *>(d_Pinv) + q.Pinv_off * s;
+        sys[i].gamma = static_cast<const char *>(d_gamma) + q.vec_off * s;
+        sys[i].lambda = static_cast<char *>(d_lambda) + q.vec_off * s;
+        sys[i].lambda_fwd = nullptr;
+        sys[i].dS = nullptr;
+        sys[i].n = q.n;
+        sys[i].N = q.N;
+        eS = std::max(eS, (size_t)q.S_off + 3 * n * n * N);
+        eP = std::max(eP, (size_t)q.Pinv_off + pm);
+        eV = std::max(eV, (size_t)q.vec_off + n * N);
+    }
+    int rc = gbdpcg_plan_create(h, dtype, sys.data(), count, pinv_layout, cfg, plan);
+    if (rc) return rc;
+    gbdpcg_plan_s *p = *plan;
+    p->packed = true;
+    p->arena_S = d_S;
+    p->arena_P = d_Pinv;
+    p->arena_g = d_gamma;
+    p->arena_l = d_lambda;
+    p->bytes_S = eS * s;
+    p->bytes_P = eP * s;
+    p->bytes_vec = eV * s;
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_execute_host(gbdpcg_plan_t p, const void *h_S, const void *h_Pinv,
+                             const void *h_gamma, void *h_lambda, gbdpcg_result *h_results,
+                             gbdpcg_stream_t stream_) {
+    if (!p || !h_lambda) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (!p->packed) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan was not created packed");
+    HandleScope scope(p->h->device);
+    cudaStream_t st = (cudaStream_t)stream_;
+    if (h_S) GB_CUDA(cudaMemcpyAsync(const_cast<void *>(p->arena_S), h_S, p->bytes_S,
+                                     cudaMemcpyHostToDevice, st));
+    if (h_Pinv) GB_CUDA(cudaMemcpyAsync(const_cast<void *>(p->arena_P), h_Pinv, p->bytes_P,
+                                        cudaMemcpyHostToDevice, st));
+    if (h_gamma) GB_CUDA(cudaMemcpyAsync(const_cast<void *>(p->arena_g), h_gamma, p->bytes_vec,
+                                         cudaMemcpyHostToDevice, st));
+    if (!p->cfg.zero_guess)
+        GB_CUDA(cudaMemcpyAsync(p->arena_l, h_lambda, p->bytes_vec, cudaMemcpyHostToDevice, st));
+    int rc = gbdpcg_plan_execute(p, stream_);
+    if (rc) return rc;
+    GB_CUDA(cudaMemcpyAsync(h_lambda, p->arena_l, p->bytes_vec, cudaMemcpyDeviceToHost, st));
+    if (h_results) return gbdpcg_plan_results(p, h_results, stream_);
+    GB_CUDA(cudaStreamSynchronize(st));
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_build_block_jacobi(gbdpcg_plan_t p, gbdpcg_stream_t stream) {
+    if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    for (auto &d : p->descs)
+        if (d.n > 32) return fail(GBDPCG_ERR_UNSUPPORTED, "block-Jacobi builder needs n <= 32");
+    HandleScope scope(p->h->device);
+    GB_CUDA(launch_block_jacobi(p->f64, false, p->d_descs.as<SysDesc>(), p->d_prefix.as<uint64_t>(),
+                                p->count, p->total_knots, p->layout == GBDPCG_PINV_CBTD,
+                                (cudaStream_t)stream));
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_results(gbdpcg_plan_t p, gbdpcg_result *results, gbdpcg_stream_t stream) {
+    if (!p || !results) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    HandleScope scope(p->h->device);
+    std::vector<SysResult> r(p->count);
+    GB_CUDA(cudaMemcpyAsync(r.data(), p->d_results.p, sizeof(SysResult) * p->count,
+                            cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    GB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    for (uint32_t i = 0; i < p->count; ++i) to_public(r[i], &results[i]);
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_launch_count(gbdpcg_plan_t p, uint32_t *launches) {
+    if (!p || !launches) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    *launches = (uint32_t)(p->classes.size() + p->plain_items.size());
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_launch_info(gbdpcg_plan_t p, uint32_t i, uint32_t *cluster, uint32_t *threads,
+                            uint32_t *kmax, uint32_t *systems, uint32_t *ctas) {
+    if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (i < p->classes.size()) {
+        const PlanClass &pc = p->classes[i];
+        if (cluster) *cluster = pc.sh.C;
+        if (threads) *threads = pc.sh.threads;
+        if (kmax) *kmax = pc.kmax;
+        if (systems) *systems = (uint32_t)pc.items.size();
+        if (ctas) *ctas = pc.grid_clusters * pc.sh.C;
+        return GBDPCG_SUCCESS;
+    }
+    i -= (uint32_t)p->classes.size();
+    if (i >= p->plain_items.size()) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "launch index");
+    const SysDesc &d = p->descs[p->plain_items[i]];
+    if (cluster) *cluster = 0;
+    if (threads) *threads = 64;
+    if (kmax) *kmax = 1;
+    if (systems) *systems = 1;
+    if (ctas) *ctas = d.N;
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_destroy(gbdpcg_plan_t p) {
+    if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    HandleScope scope(p->h->device);
+    delete p;
+    return GBDPCG_SUCCESS;
+}
+
+}  // extern "C"

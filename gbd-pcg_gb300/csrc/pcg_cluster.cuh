@@ -206,8 +206,23 @@ __device__ __forceinline__ bool finite_(T x) {
 // A: accumulation type of the dot products (T, or double for mixed precision);
 // NP: compile-time block size bound (n <= NP); PTRI: Phi^-1 is block-
 // tridiagonal; MREG: matrix rows held in registers (else in shared memory).
+// Register budget of one thread: the matrix rows it holds plus a fixed base.
+// The launch bound caps the compiler at that budget, so a CTA of up to
+// max_threads() rows always fits one SM's 64K registers.
 template <typename T, typename A, int NP, bool PTRI, bool MREG>
-__global__ void pcg_cluster_kernel(const LaunchParams lp) {
+struct RegBudget {
+    static constexpr int words = (int)(sizeof(T) / 4);
+    static constexpr int matrix = MREG ? (3 + (PTRI ? 3 : 1)) * NP * words : 0;
+    static constexpr int base = (sizeof(T) == 8 || sizeof(A) == 8) ? 80 : 64;
+    static constexpr int regs = matrix + base > 255 ? 255 : matrix + base;
+    // warps are spread over 4 sub-partitions of 16K registers each: whole groups of 4 warps
+    static constexpr int max_threads_raw = 65536 / regs / 128 * 128;
+    static constexpr int max_threads = max_threads_raw > 1024 ? 1024 : max_threads_raw;
+};
+
+template <typename T, typename A, int NP, bool PTRI, bool MREG>
+__global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads), 1)
+    pcg_cluster_kernel(const LaunchParams lp) {
     using Plan = SmemPlan<T, A, NP, PTRI, MREG>;
     constexpr int NBP = PTRI ? 3 : 1;
     const cg::cluster_group cluster = cg::this_cluster();
@@ -228,16 +243,23 @@ __global__ void pcg_cluster_kernel(const LaunchParams lp) {
     T *mp = reinterpret_cast<T *>(sp);
     const size_t zero_elems = (2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T);
 
-    for (;;) {
+    const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
+    for (uint32_t pass = 0;; ++pass) {
         // ---- pull the next system (cluster leader pops, broadcasts by DSMEM)
-        if (rank == 0 && tid == 0) {
-            const uint32_t it = atomicAdd(lp.queue, 1u);
-            for (uint32_t c = 0; c < C; ++c) *cluster.map_shared_rank(s_item, c) = it;
+        uint32_t item;
+        if (lp.queue) {
+            if (rank == 0 && tid == 0) {
+                const uint32_t it = atomicAdd(lp.queue, 1u);
+                for (uint32_t c = 0; c < C; ++c) *cluster.map_shared_rank(s_item, c) = it;
+            }
+            group_sync(cluster, C);
+            item = *reinterpret_cast<volatile uint32_t *>(s_item);
+        } else {
+            item = cluster_id + pass * nclusters;
+            __syncthreads();  // the previous system's epilogue has finished with shared memory
         }
-        group_sync(cluster, C);
-        const uint32_t item = *reinterpret_cast<volatile uint32_t *>(s_item);
         if (item >= lp.count) break;
-        const SysDesc d = lp.descs[lp.order[item]];
+        const SysDesc d = lp.descs ? lp.descs[lp.order ? lp.order[item] : item] : lp.one;
         const uint32_t n = d.n, N = d.N;
         const uint32_t K = (N + C - 1) / C;
         if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (size_t)K * n > nthr) {

@@ -1,0 +1,12 @@
+// Cluster-kernel variants for blocks of size n <= 16.
+#include "pcg_variants.cuh"
+
+namespace gbdpcg {
+int variants_np16(KernelVariant *out) {
+    int c = 0;
+    GBDPCG_VARIANTS_F32(16)
+    GBDPCG_VARIANTS_F64_SMEM(16)
+    out[c++] = GBDPCG_VARIANT(double, double, 16, false, true);
+    return c;
+}
+}  // namespace gbdpcg

@@ -1,0 +1,12 @@
+// Cluster-kernel variants for blocks of size n <= 24.
+#include "pcg_variants.cuh"
+
+namespace gbdpcg {
+int variants_np24(KernelVariant *out) {
+    int c = 0;
+    GBDPCG_VARIANTS_F32(24)
+    GBDPCG_VARIANTS_F64_SMEM(24)
+
+    return c;
+}
+}  // namespace gbdpcg

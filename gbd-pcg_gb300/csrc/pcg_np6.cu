@@ -1,0 +1,13 @@
+// Cluster-kernel variants for blocks of size n <= 6.
+#include "pcg_variants.cuh"
+
+namespace gbdpcg {
+int variants_np6(KernelVariant *out) {
+    int c = 0;
+    GBDPCG_VARIANTS_F32(6)
+    GBDPCG_VARIANTS_F64_SMEM(6)
+    out[c++] = GBDPCG_VARIANT(double, double, 6, false, true);
+    out[c++] = GBDPCG_VARIANT(double, double, 6, true, true);
+    return c;
+}
+}  // namespace gbdpcg

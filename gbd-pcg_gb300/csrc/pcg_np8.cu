@@ -1,0 +1,13 @@
+// Cluster-kernel variants for blocks of size n <= 8.
+#include "pcg_variants.cuh"
+
+namespace gbdpcg {
+int variants_np8(KernelVariant *out) {
+    int c = 0;
+    GBDPCG_VARIANTS_F32(8)
+    GBDPCG_VARIANTS_F64_SMEM(8)
+    out[c++] = GBDPCG_VARIANT(double, double, 8, false, true);
+    out[c++] = GBDPCG_VARIANT(double, double, 8, true, true);
+    return c;
+}
+}  // namespace gbdpcg

@@ -57,12 +57,14 @@ struct SysResult {
 
 // Launch-wide parameters of the persistent cluster kernel.
 struct LaunchParams {
-    const SysDesc *descs;
+    const SysDesc *descs;    // null: the single system `one` (passed by value)
     const uint32_t *order;   // work list: indices into descs, longest first
     uint32_t count;
     uint32_t kmax;           // knots per CTA the shared memory is sized for
-    uint32_t *queue;         // work-queue head (zeroed before the launch)
+    uint32_t *queue;         // work-queue head (zeroed before the launch); null: static
+                             // round-robin of items over clusters
     SysResult *results;
+    SysDesc one;
 };
 
 }  // namespace gbdpcg

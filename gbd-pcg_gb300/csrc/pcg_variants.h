@@ -1,0 +1,30 @@
+// Registry of the instantiated cluster-kernel variants (host side).
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+namespace gbdpcg {
+
+struct KernelVariant {
+    int f64;     // matrices and vectors in double
+    int acc64;   // dot products accumulated in double
+    int np;      // compile-time block-size bound (n <= np)
+    int ptri;    // Phi^-1 block-tridiagonal (cbtd) instead of block-diagonal
+    int mreg;    // matrix rows in registers (else staged in shared memory)
+    const void *func;
+    size_t (*smem_bytes)(uint32_t kmax);
+};
+
+// Each returns the number of variants written to `out` (at most 16).
+int variants_np6(KernelVariant *out);
+int variants_np8(KernelVariant *out);
+int variants_np12(KernelVariant *out);
+int variants_np14(KernelVariant *out);
+int variants_np16(KernelVariant *out);
+int variants_np24(KernelVariant *out);
+int variants_np32(KernelVariant *out);
+
+const void *plain_kernel_ptr(bool f64);
+size_t plain_smem_bytes(bool f64, uint32_t n, uint32_t N);
+
+}  // namespace gbdpcg

@@ -1,0 +1,363 @@
+"""Python binding of the GB300 PCG solver's C ABI (include/gbdpcg.h).
+
+The compute runs in libgbdpcg.so (hand-written sm_103a CUDA); this module only
+marshals arguments.  There is no fallback: if the library is missing, every
+call raises.
+
+Mirrors the reference's interface (Sdevaud/GBD-PCG include/interface.cuh,
+include/types.cuh): `pcg_config` defaults (tol 1e-6, 25 iterations),
+`solvePCG(S, Pinv, gamma, lambda, stateSize, knotPoints, config)` with lambda
+in/out, `pcg_solve(S, gamma, lambda, ...)` with the preconditioner built on the
+GPU.  Unlike the reference, the host form returns the iteration count (the
+reference returns 1, include/interface.cuh:90) and reports errors by raising
+instead of exiting the process.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "_build", "libgbdpcg.so")
+
+SUCCESS, ERR_INVALID_ARGUMENT, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_MEMORY = 0, 1, 2, 3, 4
+CONVERGED, MAX_ITER, BREAKDOWN, REJECTED = 0, 1, 2, -1
+EXIT_REFERENCE, EXIT_RELRES = 0, 1
+PINV_CBTD, PINV_BLOCKDIAG = 0, 1
+ALGO_AUTO, ALGO_CLUSTER, ALGO_PLAIN = 0, 1, 2
+DOT_NATIVE, DOT_FP64 = 0, 1
+STORAGE_AUTO, STORAGE_REGISTERS, STORAGE_SHARED = 0, 1, 2
+
+
+class GbdpcgError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what}: {status_string(code)} ({code}): {last_error()}")
+        self.code = code
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("exit_tol", ctypes.c_double), ("max_iter", ctypes.c_uint32),
+                ("exit_mode", ctypes.c_uint32), ("dot_precision", ctypes.c_uint32),
+                ("algorithm", ctypes.c_uint32), ("cluster_size", ctypes.c_uint32),
+                ("max_threads", ctypes.c_uint32), ("storage", ctypes.c_uint32),
+                ("use_graph", ctypes.c_uint32), ("zero_guess", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 3)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("iters", ctypes.c_uint32), ("status", ctypes.c_int32), ("eta", ctypes.c_double),
+                ("relres", ctypes.c_double)]
+
+    def __repr__(self):
+        return f"Result(iters={self.iters}, status={self.status}, eta={self.eta:.3g}, relres={self.relres:.3g})"
+
+
+class PackedSystem(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_uint32), ("N", ctypes.c_uint32), ("S_off", ctypes.c_uint64),
+                ("Pinv_off", ctypes.c_uint64), ("vec_off", ctypes.c_uint64)]
+
+
+class System(ctypes.Structure):
+    _fields_ = [("S", ctypes.c_void_p), ("Pinv", ctypes.c_void_p), ("gamma", ctypes.c_void_p),
+                ("lambda_", ctypes.c_void_p), ("lambda_fwd", ctypes.c_void_p), ("dS", ctypes.c_void_p),
+                ("n", ctypes.c_uint32), ("N", ctypes.c_uint32)]
+
+
+# Every symbol of include/gbdpcg.h with its ctypes signature.
+_P, _U, _I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int
+_SIGS = {
+    "gbdpcg_version": ([], _I),
+    "gbdpcg_status_string": ([_I], ctypes.c_char_p),
+    "gbdpcg_last_error": ([], ctypes.c_char_p),
+    "gbdpcg_config_init": ([_P], None),
+    "gbdpcg_create": ([_P, _I], _I),
+    "gbdpcg_destroy": ([_P], _I),
+    "gbdpcg_solve_f32": ([_P, _P, _P, _P, _U, _U, _P, _P], _I),
+    "gbdpcg_solve_f64": ([_P, _P, _P, _P, _U, _U, _P, _P], _I),
+    "gbdpcg_solve_dev_f32": ([_P, _P, _P, _U, _P, _P, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_solve_dev_f64": ([_P, _P, _P, _U, _P, _P, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_last_result": ([_P, _P], _I),
+    "gbdpcg_block_jacobi_f32": ([_P, _P, _P, _U, _U, _U, _P], _I),
+    "gbdpcg_block_jacobi_f64": ([_P, _P, _P, _U, _U, _U, _P], _I),
+    "gbdpcg_adjoint_dev_f32": ([_P, _P, _P, _U, _P, _P, _P, _P, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_plan_create": ([_P, _I, _P, _U, _U, _P, _P], _I),
+    "gbdpcg_plan_execute": ([_P, _P], _I),
+    "gbdpcg_plan_create_packed": ([_P, _I, _P, _U, _P, _P, _P, _P, _U, _P, _P], _I),
+    "gbdpcg_plan_execute_host": ([_P, _P, _P, _P, _P, _P, _P], _I),
+    "gbdpcg_plan_build_block_jacobi": ([_P, _P], _I),
+    "gbdpcg_plan_results": ([_P, _P, _P], _I),
+    "gbdpcg_plan_launch_count": ([_P, _P], _I),
+    "gbdpcg_plan_launch_info": ([_P, _U, _P, _P, _P, _P, _P], _I),
+    "gbdpcg_plan_destroy": ([_P], _I),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libgbdpcg.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libgbdpcg.so not built ({LIB_PATH}); run gbd-pcg_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def status_string(code: int) -> str:
+    return lib().gbdpcg_status_string(code).decode()
+
+
+def last_error() -> str:
+    return lib().gbdpcg_last_error().decode()
+
+
+def _check(code: int, what: str):
+    if code != SUCCESS:
+        raise GbdpcgError(code, what)
+
+
+def config(**kw) -> Config:
+    """pcg_config defaults (include/types.cuh:18-34) with overrides."""
+    c = Config()
+    lib().gbdpcg_config_init(ctypes.byref(c))
+    for k, v in kw.items():
+        if not hasattr(c, k):
+            raise AttributeError(k)
+        setattr(c, k, v)
+    return c
+
+
+def _np_ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+# ------------------------------------------------------------------- host pointers
+def solve(S: np.ndarray, Pinv: Optional[np.ndarray], gamma: np.ndarray, lam: np.ndarray,
+          n: int, N: int, cfg: Optional[Config] = None) -> Result:
+    """Host-array solve (solvePCG host overload; Pinv None = pcg_solve with the
+    block-Jacobi preconditioner built on the GPU).  `lam` is updated in place."""
+    dt = lam.dtype
+    if dt not in (np.float32, np.float64):
+        raise TypeError("float32 or float64 arrays")
+    for a in (S, gamma, lam) + ((Pinv,) if Pinv is not None else ()):
+        if a.dtype != dt or not a.flags.c_contiguous:
+            raise TypeError("all arrays must be C-contiguous and of one dtype")
+    if S.size != 3 * n * n * N or gamma.size != n * N or lam.size != n * N:
+        raise ValueError("array sizes do not match n, N")
+    if Pinv is not None and Pinv.size != 3 * n * n * N:
+        raise ValueError("Pinv must be cbtd (3 n^2 N)")
+    r = Result()
+    fn = lib().gbdpcg_solve_f64 if dt == np.float64 else lib().gbdpcg_solve_f32
+    _check(fn(_np_ptr(S), _np_ptr(Pinv) if Pinv is not None else None, _np_ptr(gamma), _np_ptr(lam),
+              n, N, ctypes.byref(cfg) if cfg is not None else None, ctypes.byref(r)), "gbdpcg_solve")
+    return r
+
+
+def solvePCG(h_S, h_Pinv, h_gamma, h_lambda, stateSize, knotPoints, config_=None) -> int:
+    """The reference's host solvePCG (include/interface.cuh:24-32); returns the
+    iteration count."""
+    return solve(h_S, h_Pinv, h_gamma, h_lambda, stateSize, knotPoints, config_).iters
+
+
+def pcg_solve(h_S, h_gamma, h_lambda, stateSize, knotPoints, config_=None) -> int:
+    """The reference's documented pcg_solve (README.md:42): block-Jacobi Phi^-1
+    built on the GPU; returns the iteration count."""
+    return solve(h_S, None, h_gamma, h_lambda, stateSize, knotPoints, config_).iters
+
+
+# ------------------------------------------------------------------- device pointers (torch)
+def _tp(t) -> Optional[int]:
+    return None if t is None else t.data_ptr()
+
+
+def _stream(stream) -> Optional[int]:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return stream if isinstance(stream, int) else stream.cuda_stream
+
+
+class Handle:
+    def __init__(self, device: int = 0):
+        self.h = ctypes.c_void_p()
+        _check(lib().gbdpcg_create(ctypes.byref(self.h), device), "gbdpcg_create")
+
+    def close(self):
+        if self.h:
+            lib().gbdpcg_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, S, Pinv, gamma, lam, n, N, layout=PINV_CBTD, cfg=None, stream=None, sync=True):
+        """Device solve; torch CUDA tensors; `lam` in/out.  Returns Result if sync."""
+        cfg = cfg or config()
+        fn = lib().gbdpcg_solve_dev_f64 if lam.dtype.itemsize == 8 else lib().gbdpcg_solve_dev_f32
+        r = Result()
+        _check(fn(self.h, _tp(S), _tp(Pinv), layout, _tp(gamma), _tp(lam), n, N, ctypes.byref(cfg),
+                  ctypes.byref(r) if sync else None, _stream(stream)), "gbdpcg_solve_dev")
+        return r if sync else None
+
+    def last_result(self) -> Result:
+        r = Result()
+        _check(lib().gbdpcg_last_result(self.h, ctypes.byref(r)), "gbdpcg_last_result")
+        return r
+
+    def block_jacobi(self, S, Pinv_out, n, N, layout=PINV_BLOCKDIAG, stream=None):
+        fn = lib().gbdpcg_block_jacobi_f64 if S.dtype.itemsize == 8 else lib().gbdpcg_block_jacobi_f32
+        _check(fn(self.h, _tp(S), _tp(Pinv_out), layout, n, N, _stream(stream)), "gbdpcg_block_jacobi")
+
+    def adjoint(self, S, Pinv, lam, grad_lam, grad_gamma, grad_S, n, N, layout=PINV_CBTD, cfg=None,
+                stream=None, sync=True):
+        cfg = cfg or config()
+        r = Result()
+        _check(lib().gbdpcg_adjoint_dev_f32(self.h, _tp(S), _tp(Pinv), layout, _tp(lam), _tp(grad_lam),
+                                            _tp(grad_gamma), _tp(grad_S), n, N, ctypes.byref(cfg),
+                                            ctypes.byref(r) if sync else None, _stream(stream)),
+               "gbdpcg_adjoint_dev_f32")
+        return r if sync else None
+
+
+class Plan:
+    """Batched solve of many systems (device tensors).  `systems` is a list of
+    dicts with keys S, Pinv, gamma, lambda (and lambda_fwd, dS for an adjoint
+    plan), n, N.  The tensors must stay alive as long as the plan."""
+
+    def __init__(self, handle: Handle, systems=None, layout=PINV_BLOCKDIAG, cfg=None, dtype=None,
+                 packed=None):
+        cfg = cfg or config()
+        self.handle = handle
+        self.p = ctypes.c_void_p()
+        if packed is not None:
+            # packed = (list of (n, N, S_off, Pinv_off, vec_off), S, Pinv, gamma, lambda) tensors
+            descs, S, P, g, l = packed
+            arr = (PackedSystem * len(descs))(*[PackedSystem(*d) for d in descs])
+            self.count = len(descs)
+            dt = 1 if S.dtype.itemsize == 8 else 0
+            _check(lib().gbdpcg_plan_create_packed(handle.h, dt, ctypes.cast(arr, ctypes.c_void_p), len(descs),
+                                                   _tp(S), _tp(P), _tp(g), _tp(l), layout, ctypes.byref(cfg),
+                                                   ctypes.byref(self.p)), "gbdpcg_plan_create_packed")
+            return
+        if dtype is None:
+            dtype = 1 if systems[0]["S"].dtype.itemsize == 8 else 0
+        arr = (System * len(systems))()
+        for i, s in enumerate(systems):
+            arr[i] = System(_tp(s["S"]), _tp(s["Pinv"]), _tp(s["gamma"]), _tp(s["lambda"]),
+                            _tp(s.get("lambda_fwd")), _tp(s.get("dS")), s["n"], s["N"])
+        self.count = len(systems)
+        self.handle = handle
+        self.p = ctypes.c_void_p()
+        _check(lib().gbdpcg_plan_create(handle.h, dtype, ctypes.cast(arr, ctypes.c_void_p), len(systems),
+                                        layout, ctypes.byref(cfg), ctypes.byref(self.p)), "gbdpcg_plan_create")
+
+    def execute(self, stream=None):
+        _check(lib().gbdpcg_plan_execute(self.p, _stream(stream)), "gbdpcg_plan_execute")
+
+    def execute_host(self, h_S, h_P, h_g, h_l, with_results=False, stream=None):
+        """End-to-end from host arrays (numpy or pinned CPU tensors)."""
+        def ptr(a):
+            if a is None:
+                return None
+            return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data_as(ctypes.c_void_p)
+        res = (Result * self.count)() if with_results else None
+        _check(lib().gbdpcg_plan_execute_host(self.p, ptr(h_S), ptr(h_P), ptr(h_g), ptr(h_l),
+                                              ctypes.cast(res, ctypes.c_void_p) if res is not None else None,
+                                              _stream(stream)), "gbdpcg_plan_execute_host")
+        return list(res) if res is not None else None
+
+    def build_block_jacobi(self, stream=None):
+        _check(lib().gbdpcg_plan_build_block_jacobi(self.p, _stream(stream)), "gbdpcg_plan_build_block_jacobi")
+
+    def results(self, stream=None):
+        arr = (Result * self.count)()
+        _check(lib().gbdpcg_plan_results(self.p, ctypes.cast(arr, ctypes.c_void_p), _stream(stream)),
+               "gbdpcg_plan_results")
+        return list(arr)
+
+    def launches(self):
+        c = ctypes.c_uint32()
+        _check(lib().gbdpcg_plan_launch_count(self.p, ctypes.byref(c)), "gbdpcg_plan_launch_count")
+        out = []
+        for i in range(c.value):
+            v = [ctypes.c_uint32() for _ in range(5)]
+            _check(lib().gbdpcg_plan_launch_info(self.p, i, *[ctypes.byref(x) for x in v]),
+                   "gbdpcg_plan_launch_info")
+            out.append(dict(zip(("cluster", "threads", "kmax", "systems", "ctas"), [x.value for x in v])))
+        return out
+
+    def close(self):
+        if self.p:
+            lib().gbdpcg_plan_destroy(self.p)
+            self.p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------- autograd
+_default_handles = {}
+
+
+def default_handle(device: int = 0) -> Handle:
+    h = _default_handles.get(device)
+    if h is None:
+        h = _default_handles[device] = Handle(device)
+    return h
+
+
+def _make_fn():
+    import torch
+
+    class PCGSolve(torch.autograd.Function):
+        """lambda = S^-1 gamma by PCG; backward by the adjoint PCG solve
+        (S symmetric): dgamma = mu with S mu = dL/dlambda, and dS on the
+        block-tridiagonal pattern = -1/2 (mu lambda^T + lambda mu^T)."""
+
+        @staticmethod
+        def forward(ctx, S, Pinv, gamma, n, N, layout, cfg_kw):
+            h = default_handle(S.device.index or 0)
+            lam = torch.zeros_like(gamma)
+            r = h.solve(S, Pinv, gamma, lam, n, N, layout, config(**cfg_kw))
+            ctx.save_for_backward(S, Pinv, lam)
+            ctx.meta = (n, N, layout, cfg_kw)
+            ctx.result = r
+            return lam
+
+        @staticmethod
+        def backward(ctx, grad_lam):
+            S, Pinv, lam = ctx.saved_tensors
+            n, N, layout, cfg_kw = ctx.meta
+            h = default_handle(S.device.index or 0)
+            g_gamma = torch.empty_like(lam)
+            g_S = torch.empty_like(S)
+            h.adjoint(S, Pinv, lam, grad_lam.contiguous(), g_gamma, g_S, n, N, layout, config(**cfg_kw))
+            return g_S, None, g_gamma, None, None, None, None
+
+    return PCGSolve
+
+
+_fn = None
+
+
+def pcg_solve_autograd(S, Pinv, gamma, n, N, layout=PINV_BLOCKDIAG, **cfg_kw):
+    """Differentiable solve of one float32 system (torch CUDA tensors)."""
+    global _fn
+    if _fn is None:
+        _fn = _make_fn()
+    return _fn.apply(S, Pinv, gamma, n, N, layout, cfg_kw)

@@ -1,0 +1,230 @@
+/*
+ * gbdpcg — C ABI of the GB300 (sm_103a) PCG solver for the block-tridiagonal
+ * Schur-complement systems  Phi^-1 S lambda = Phi^-1 gamma  of optimal control.
+ *
+ * It is the drop-in boundary for the reference's PCG path (Sdevaud/GBD-PCG):
+ * the C++ templates of the reference's interface (solvePCG, pcg_solve,
+ * pcg_config — see gpu_pcg.cuh in this directory) are inline wrappers over
+ * these entry points.  Plain pointers and sizes only; every call returns a
+ * status code (the reference exits the process instead,
+ * include/gpuassert.cuh:5-14).
+ *
+ * Data layout (the reference's, include/pcg.cuh:104-110 and
+ * include/utils.cuh:62,71,80): S and a block-tridiagonal Phi^-1 are
+ * "compressed block-tridiagonal" (cbtd) arrays of N block rows, each an n x 3n
+ * column-major matrix [S_{k,k-1} | S_{k,k} | S_{k,k+1}], element (r, c) of
+ * block row k at k*3n^2 + c*n + r.  The blocks S_{0,-1} and S_{N-1,N} are
+ * present as padding and never read.  A block-diagonal Phi^-1 may instead be
+ * given compactly: n^2 per knot, column-major.  Vectors are n*N, knot-major.
+ *
+ * Supported sizes: 1 <= n <= 32 on the cluster solver (any N up to what 16
+ * CTAs hold); larger n runs the plain algorithm (one CTA per knot).
+ */
+#ifndef GBDPCG_H
+#define GBDPCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBDPCG_VERSION 1000
+
+#if defined(__GNUC__)
+#define GBDPCG_API __attribute__((visibility("default")))
+#else
+#define GBDPCG_API
+#endif
+
+/* ---- return codes of the API calls ---- */
+typedef enum {
+    GBDPCG_SUCCESS = 0,
+    GBDPCG_ERR_INVALID_ARGUMENT = 1, /* null pointer, zero size, bad enum */
+    GBDPCG_ERR_UNSUPPORTED = 2,      /* size or option combination not supported */
+    GBDPCG_ERR_CUDA = 3,             /* a CUDA call failed; see gbdpcg_last_error() */
+    GBDPCG_ERR_NO_MEMORY = 4,
+    GBDPCG_ERR_NOT_CONVERGED = 5     /* returned by nothing but gbdpcg_status_string() knows it */
+} gbdpcg_status;
+
+/* ---- per-system outcome (gbdpcg_result.status) ---- */
+enum {
+    GBDPCG_CONVERGED = 0,   /* exit test met */
+    GBDPCG_MAX_ITER = 1,    /* pcg_max_iter passes without meeting it (the reference's
+                               d_max_iter_exit, include/pcg.cuh:101,212) */
+    GBDPCG_BREAKDOWN = 2,   /* p^T S p or r^T Phi^-1 r not finite */
+    GBDPCG_REJECTED = -1    /* the system did not fit the launch it was planned into */
+};
+
+/* exit criterion */
+enum {
+    GBDPCG_EXIT_REFERENCE = 0, /* |r^T Phi^-1 r| < exit_tol   (include/pcg.cuh:195) */
+    GBDPCG_EXIT_RELRES = 1     /* ||r||_2 <= exit_tol ||gamma||_2 (recursive residual) */
+};
+/* Phi^-1 storage */
+enum { GBDPCG_PINV_CBTD = 0, GBDPCG_PINV_BLOCKDIAG = 1 };
+/* algorithm */
+enum {
+    GBDPCG_ALGO_AUTO = 0,    /* cluster solver when n <= 32, else plain */
+    GBDPCG_ALGO_CLUSTER = 1, /* one thread-block cluster per system, DSMEM halos */
+    GBDPCG_ALGO_PLAIN = 2    /* one CTA per knot, grid-wide barriers (the reference's scheme) */
+};
+/* dot-product accumulation for float systems */
+enum { GBDPCG_DOT_NATIVE = 0, GBDPCG_DOT_FP64 = 1 };
+/* where the cluster solver keeps the matrix rows */
+enum { GBDPCG_STORAGE_AUTO = 0, GBDPCG_STORAGE_REGISTERS = 1, GBDPCG_STORAGE_SHARED = 2 };
+
+typedef struct {
+    double exit_tol;         /* pcg_exit_tol, default 1e-6 (include/constants.cuh:17) */
+    uint32_t max_iter;       /* pcg_max_iter, default 25  (include/constants.cuh:15) */
+    uint32_t exit_mode;      /* GBDPCG_EXIT_*, default REFERENCE */
+    uint32_t dot_precision;  /* GBDPCG_DOT_*, default NATIVE */
+    uint32_t algorithm;      /* GBDPCG_ALGO_*, default AUTO */
+    uint32_t cluster_size;   /* 0 = chosen by the tuner, else 1..16 CTAs per system */
+    uint32_t max_threads;    /* 0 = chosen by the tuner, else a cap on threads per CTA */
+    uint32_t storage;        /* GBDPCG_STORAGE_* */
+    uint32_t use_graph;      /* plans: capture the launches in a CUDA graph (default 1) */
+    uint32_t zero_guess;     /* 1: start from lambda = 0 and do not read lambda (default 0) */
+    uint32_t reserved[3];
+} gbdpcg_config;
+
+typedef struct {
+    uint32_t iters;        /* PCG passes, the converging one included (include/pcg.cuh:195) */
+    int32_t status;        /* GBDPCG_CONVERGED / _MAX_ITER / _BREAKDOWN / _REJECTED */
+    double eta;            /* last r^T Phi^-1 r */
+    double relres;         /* ||r||/||gamma|| of the recursive residual (-1 if not tracked) */
+} gbdpcg_result;
+
+/* One system of a batch.  Device pointers, element type of the batch.
+ * Forward solve: lambda is in/out (initial guess, solution).
+ * Adjoint solve: gamma = dL/dlambda, lambda = dL/dgamma (out), lambda_fwd = the
+ * forward solution, dS = dL/dS (out, cbtd).  lambda_fwd and dS are NULL for a
+ * forward solve. */
+typedef struct {
+    const void *S;
+    const void *Pinv;
+    const void *gamma;
+    void *lambda;
+    const void *lambda_fwd;
+    void *dS;
+    uint32_t n;
+    uint32_t N;
+} gbdpcg_system;
+
+typedef struct gbdpcg_handle_s *gbdpcg_handle_t;
+typedef struct gbdpcg_plan_s *gbdpcg_plan_t;
+typedef void *gbdpcg_stream_t; /* a cudaStream_t; NULL is the legacy default stream */
+
+GBDPCG_API int gbdpcg_version(void);
+GBDPCG_API const char *gbdpcg_status_string(int status);
+/* Message of the last failed call on this thread. */
+GBDPCG_API const char *gbdpcg_last_error(void);
+/* Defaults of pcg_config (include/types.cuh:18-34, include/constants.cuh:14-20). */
+GBDPCG_API void gbdpcg_config_init(gbdpcg_config *cfg);
+
+/* Handle: device, workspace, tuning table, launch cache.  One per thread of use. */
+GBDPCG_API int gbdpcg_create(gbdpcg_handle_t *handle, int device);
+GBDPCG_API int gbdpcg_destroy(gbdpcg_handle_t handle);
+
+/* Host-pointer solve of one system; synchronous.  Replaces the host overload
+ * solvePCG(h_S, h_Pinv, h_gamma, h_lambda, stateSize, knotPoints, config)
+ * (include/interface.cuh:24-91).  Pinv is a cbtd array, or NULL to build the
+ * block-Jacobi preconditioner on the GPU (the reference's documented
+ * pcg_solve(S, gamma, lambda, ...) without Pinv, README.md:42).  S, Pinv and
+ * gamma are not written (the reference copies them back, interface.cuh:77,79).
+ * lambda is the initial guess on entry and the solution on return.  Uses a
+ * per-thread handle on the current device. */
+GBDPCG_API int gbdpcg_solve_f32(const float *S, const float *Pinv, const float *gamma, float *lambda,
+                     uint32_t n, uint32_t N, const gbdpcg_config *cfg, gbdpcg_result *result);
+GBDPCG_API int gbdpcg_solve_f64(const double *S, const double *Pinv, const double *gamma, double *lambda,
+                     uint32_t n, uint32_t N, const gbdpcg_config *cfg, gbdpcg_result *result);
+
+/* Device-pointer solve of one system, stream-ordered.  Replaces the device
+ * overload solvePCG(state_size, knot_points, d_S, d_Pinv, d_gamma, d_lambda,
+ * d_r, d_p, d_v_temp, d_eta_new_temp, config) (include/interface.cuh:94-146);
+ * the cluster solver keeps r and p on chip, so no scratch is passed.  If
+ * `result` is non-NULL the call waits for the stream and fills it; else the
+ * result stays on the device (gbdpcg_last_result). */
+GBDPCG_API int gbdpcg_solve_dev_f32(gbdpcg_handle_t h, const float *d_S, const float *d_Pinv,
+                         uint32_t pinv_layout, const float *d_gamma, float *d_lambda, uint32_t n,
+                         uint32_t N, const gbdpcg_config *cfg, gbdpcg_result *result,
+                         gbdpcg_stream_t stream);
+GBDPCG_API int gbdpcg_solve_dev_f64(gbdpcg_handle_t h, const double *d_S, const double *d_Pinv,
+                         uint32_t pinv_layout, const double *d_gamma, double *d_lambda,
+                         uint32_t n, uint32_t N, const gbdpcg_config *cfg,
+                         gbdpcg_result *result, gbdpcg_stream_t stream);
+/* Waits for the last device-pointer solve of this handle and returns its result. */
+GBDPCG_API int gbdpcg_last_result(gbdpcg_handle_t h, gbdpcg_result *result);
+
+/* Block-Jacobi preconditioner Phi^-1 = blockdiag(S_kk^-1) of a cbtd S, on the
+ * GPU, in cbtd or compact layout.  No reference counterpart: the reference
+ * takes Phi^-1 from its caller. */
+GBDPCG_API int gbdpcg_block_jacobi_f32(gbdpcg_handle_t h, const float *d_S, float *d_Pinv,
+                            uint32_t pinv_layout, uint32_t n, uint32_t N,
+                            gbdpcg_stream_t stream);
+GBDPCG_API int gbdpcg_block_jacobi_f64(gbdpcg_handle_t h, const double *d_S, double *d_Pinv,
+                            uint32_t pinv_layout, uint32_t n, uint32_t N,
+                            gbdpcg_stream_t stream);
+
+/* Adjoint of one solve S lambda = gamma (S symmetric): solves S mu = dL/dlambda
+ * with the same PCG and writes dL/dgamma = mu and the block-tridiagonal
+ * dL/dS = -1/2 (mu_i lambda_j^T + lambda_i mu_j^T) in cbtd layout (padding
+ * blocks zero).  No reference counterpart. */
+GBDPCG_API int gbdpcg_adjoint_dev_f32(gbdpcg_handle_t h, const float *d_S, const float *d_Pinv,
+                           uint32_t pinv_layout, const float *d_lambda, const float *d_grad_lambda,
+                           float *d_grad_gamma, float *d_grad_S, uint32_t n, uint32_t N,
+                           const gbdpcg_config *cfg, gbdpcg_result *result,
+                           gbdpcg_stream_t stream);
+
+/* Batched solve of many independent systems of mixed n and N in persistent
+ * cluster launches fed by device work queues (longest first), captured in one
+ * CUDA graph.  No reference counterpart: the reference solves one system per
+ * call.  `dtype` is 0 for float, 1 for double.  `systems` is a host array of
+ * device pointers; all systems of a plan share pinv_layout and whether they
+ * are adjoint solves (lambda_fwd != NULL).  The plan keeps the pointers: re-
+ * executing it re-solves whatever the buffers hold. */
+GBDPCG_API int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *systems, uint32_t count,
+                       uint32_t pinv_layout, const gbdpcg_config *cfg, gbdpcg_plan_t *plan);
+GBDPCG_API int gbdpcg_plan_execute(gbdpcg_plan_t plan, gbdpcg_stream_t stream);
+
+/* A system of a packed batch: element offsets into four device arenas
+ * (S, Pinv, gamma, lambda; gamma and lambda share vec_off). */
+typedef struct {
+    uint32_t n;
+    uint32_t N;
+    uint64_t S_off;
+    uint64_t Pinv_off;
+    uint64_t vec_off;
+} gbdpcg_packed_system;
+
+/* Plan over packed device arenas (what a caller that keeps the batch in a few
+ * large buffers uses).  The arena sizes are those the offsets reach. */
+GBDPCG_API int gbdpcg_plan_create_packed(gbdpcg_handle_t h, int dtype,
+                                         const gbdpcg_packed_system *systems, uint32_t count,
+                                         const void *d_S, const void *d_Pinv, const void *d_gamma,
+                                         void *d_lambda, uint32_t pinv_layout,
+                                         const gbdpcg_config *cfg, gbdpcg_plan_t *plan);
+/* End-to-end solve of a packed plan from host arenas: copies S, Pinv, gamma
+ * (each skipped when NULL) host to device, executes, copies lambda (and, if
+ * non-NULL, the per-system results) back, and waits.  Pinned host memory
+ * makes the copies asynchronous DMA. */
+GBDPCG_API int gbdpcg_plan_execute_host(gbdpcg_plan_t plan, const void *h_S, const void *h_Pinv,
+                                        const void *h_gamma, void *h_lambda,
+                                        gbdpcg_result *h_results, gbdpcg_stream_t stream);
+/* Builds every system's block-Jacobi Phi^-1 into its Pinv pointer (stream-ordered). */
+GBDPCG_API int gbdpcg_plan_build_block_jacobi(gbdpcg_plan_t plan, gbdpcg_stream_t stream);
+/* Waits for the stream and copies `count` results out. */
+GBDPCG_API int gbdpcg_plan_results(gbdpcg_plan_t plan, gbdpcg_result *results, gbdpcg_stream_t stream);
+/* Number of launches (cluster classes + plain systems) the plan makes per execution. */
+GBDPCG_API int gbdpcg_plan_launch_count(gbdpcg_plan_t plan, uint32_t *launches);
+/* Describes launch i: cluster size, threads per CTA, knots per CTA, systems, CTAs in the grid. */
+GBDPCG_API int gbdpcg_plan_launch_info(gbdpcg_plan_t plan, uint32_t i, uint32_t *cluster, uint32_t *threads,
+                            uint32_t *kmax, uint32_t *systems, uint32_t *ctas);
+GBDPCG_API int gbdpcg_plan_destroy(gbdpcg_plan_t plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBDPCG_H */

@@ -23,7 +23,6 @@ from __future__ import annotations
 
 import ctypes
 import os
-from dataclasses import dataclass
 
 import numpy as np
 
@@ -42,69 +41,36 @@ REF_SIZES = {
 
 
 # --------------------------------------------------------------------------- generator
-@dataclass
-class System:
-    n: int
-    N: int
-    D: np.ndarray      # (N, n, n) diagonal blocks S_kk, FP64
-    O: np.ndarray      # (N-1, n, n) super-diagonal blocks S_{k,k+1}, FP64
-    gamma: np.ndarray  # (n*N,) FP64
-    seed: int = 0
-
-    def cbtd(self, dtype=np.float64) -> np.ndarray:
-        return pack_cbtd(self.D, self.O).astype(dtype)
+# The synthetic systems come from the package's workload module (pure numpy).
+import sys as _sys
+_PKG = os.path.join(os.path.dirname(HERE), "gbd-pcg_gb300")
+if _PKG not in _sys.path:
+    _sys.path.insert(0, _PKG)
+from gbdpcg.workload import System, generate, generate_mixed, pack_cbtd  # noqa: E402,F401
 
 
-def generate(n: int, N: int, seed: int, ill: bool = False, rng=None) -> System:
-    """Synthetic optimal-control Schur complement.
-
-    A_k ~ N(0, 1/n) rescaled to spectral radius 0.98, B_k ~ N(0, 1) (n x m,
-    m = n/2), Q_k = diag U[1, 10] (k = 0..N), R_k = diag U[0.1, 1]; or, when
-    `ill`, Q_k log-uniform in [1e-2, 1e4] and R_k log-uniform in [1e-3, 1].
-      S_kk     = A_k Q_k^-1 A_k^T + B_k R_k^-1 B_k^T + Q_{k+1}^-1
-      S_{k,k+1} = -Q_{k+1}^-1 A_{k+1}^T
-    gamma ~ N(0, 1).  Draw order: A, B, Q, R, gamma from default_rng(seed).
-    """
-    if rng is None:
-        rng = np.random.default_rng(seed)
-    m = max(1, n // 2)
-    A = rng.standard_normal((N, n, n)) / np.sqrt(n)
-    rho = np.max(np.abs(np.linalg.eigvals(A)), axis=1)
-    A *= (0.98 / rho)[:, None, None]
-    B = rng.standard_normal((N, n, m))
-    if ill:
-        Q = np.exp(rng.uniform(np.log(1e-2), np.log(1e4), (N + 1, n)))
-        R = np.exp(rng.uniform(np.log(1e-3), 0.0, (N, m)))
-    else:
-        Q = rng.uniform(1.0, 10.0, (N + 1, n))
-        R = rng.uniform(0.1, 1.0, (N, m))
-    gamma = rng.standard_normal(n * N)
-    Qi, Ri = 1.0 / Q, 1.0 / R
-    D = np.einsum("kij,kj,klj->kil", A, Qi[:N], A) + np.einsum("kij,kj,klj->kil", B, Ri, B)
-    D[:, np.arange(n), np.arange(n)] += Qi[1:]
-    D = 0.5 * (D + D.transpose(0, 2, 1))
-    O = -(Qi[1:N][:, :, None] * A[1:].transpose(0, 2, 1))
-    return System(n, N, D, O, gamma, seed)
+def quantize(a: np.ndarray, bits: int = 20) -> np.ndarray:
+    """Round to the grid 2^-bits.  LAPACK/BLAS differ between platforms in the
+    last bits; rounding the generated inputs to a coarse grid makes the golden
+    cases bit-identical on every machine (values below 2^3 then fit FP32)."""
+    return np.round(np.asarray(a, np.float64) * 2.0 ** bits) / 2.0 ** bits
 
 
-def generate_mixed(seed: int, sizes=(6, 12, 14, 24), nmin=16, nmax=128) -> System:
-    """One system of the mixed batch: n from `sizes`, N uniform in [nmin, nmax],
-    then the generator above, all from default_rng(seed)."""
-    rng = np.random.default_rng(seed)
-    n = int(rng.choice(np.asarray(sizes)))
-    N = int(rng.integers(nmin, nmax + 1))
-    return generate(n, N, seed, rng=rng)
+def golden_case(n: int, N: int, seed: int, dtype):
+    """Platform-independent inputs of a golden case: (S, Pinv cbtd, gamma)."""
+    sy = generate(n, N, seed)
+    S = quantize(sy.cbtd()).astype(dtype)
+    P = quantize(block_jacobi(sy.D)).astype(dtype)
+    g = quantize(sy.gamma).astype(dtype)
+    return S, P, g
 
 
-def pack_cbtd(D: np.ndarray, O: np.ndarray) -> np.ndarray:
-    """(N, n, n) diagonal + (N-1, n, n) super-diagonal blocks -> flat cbtd array."""
-    N, n, _ = D.shape
-    Sc = np.zeros((N, 3 * n, n), dtype=np.float64)   # Sc[k, c, r] = block row k, (r, c)
-    Sc[:, n:2 * n, :] = D.transpose(0, 2, 1)
-    if N > 1:
-        Sc[1:, 0:n, :] = O                            # S_{k,k-1} = O_{k-1}^T
-        Sc[:-1, 2 * n:3 * n, :] = O.transpose(0, 2, 1)  # S_{k,k+1} = O_k
-    return Sc.reshape(-1)
+def digest(*arrays) -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()[:16]
 
 
 def unpack_cbtd(S: np.ndarray, n: int, N: int):

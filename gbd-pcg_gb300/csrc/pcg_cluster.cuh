@@ -59,10 +59,10 @@ struct SmemPlan {
     __host__ __device__ static size_t mat_p(uint32_t kmax) {
         return MREG ? 0 : round_up((size_t)kmax * NB_P * NP * NP * sizeof(T), 32);
     }
-    static constexpr size_t kWpart = 2 * 32 * 2 * sizeof(A);  // 2 buffers x 32 warps x 2 values
-    static constexpr size_t kRed = 2 * 16 * 2 * sizeof(A);    // 2 buffers x 16 ranks x 2 values
+    // reduction slots: 2 buffers x 2 values x (16 ranks x 32 warps)
+    static constexpr size_t kSlots = 2 * 2 * 16 * 32 * sizeof(A);
     __host__ __device__ static size_t bytes(uint32_t kmax) {
-        return 2 * vec(kmax) + 2 * halo() + kWpart + kRed + 32 + mat_s(kmax) + mat_p(kmax);
+        return 2 * vec(kmax) + 2 * halo() + kSlots + 32 + mat_s(kmax) + mat_p(kmax);
     }
 };
 
@@ -143,50 +143,52 @@ __device__ __forceinline__ A warp_sum(A v) {
     return v;
 }
 
-// Cluster-wide sum of NQ values.  Identical result in every thread of the
-// cluster.  `buf` alternates between call sites so that a buffer is rewritten
-// only after a barrier that every reader has passed.  Remote pushes made by
-// the caller before this call are visible to their targets afterwards.
+// Cluster-wide sum of NQ values, identical in every thread of the cluster.
+//   1. warp butterfly: every lane holds its warp's sum;
+//   2. lane 0 of warp w stores it into slot [rank*32 + w] of every CTA of the
+//      cluster (DSMEM stores; a local store when C == 1);
+//   3. one barrier (barrier.cluster, or __syncthreads when C == 1), whose
+//      release/acquire makes the stores — and any halo pushes the caller made
+//      before this call — visible;
+//   4. every warp reduces the slots: lane l adds warp l's partials of ranks
+//      0..C-1 in rank order, then a butterfly over the lanes.
+// Every warp of every CTA reads the same slots in the same order, so all hold
+// the same bits; a warp's slot depends only on its index (rows map to threads
+// from thread 0), so the result does not depend on the CTA size either.
+// `buf` alternates between call sites so that a slot array is rewritten only
+// after a barrier that every reader has passed.
+constexpr int kMaxSlots = 16 * 32;  // ranks x warps
+
 template <typename A, int NQ>
-__device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *wpart, A *red, int buf,
+__device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
                                                   const cg::cluster_group &cluster, uint32_t C,
                                                   uint32_t rank) {
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nwarps = blockDim.x >> 5;
-    A *wp = wpart + buf * 64;
+    A *sl = slots + (size_t)buf * kMaxSlots * 2;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) v[q] = warp_sum(v[q]);
-    if (lane == 0) {
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) wp[warp * 2 + q] = v[q];
-    }
-    __syncthreads();
+    const uint32_t my = rank * 32 + warp;
     if (C == 1) {
+        if (lane == 0) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            A s = A(0);
-            for (uint32_t w = 0; w < nwarps; ++w) s += wp[w * 2 + q];
-            v[q] = s;
+            for (int q = 0; q < NQ; ++q) sl[q * kMaxSlots + my] = v[q];
         }
-        return;
-    }
-    A *rd = red + buf * 32;
-    if (warp == 0) {
-        A s[NQ];
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) s[q] = warp_sum(lane < nwarps ? wp[lane * 2 + q] : A(0));
+        __syncthreads();
+    } else {
         if (lane < C) {
-            A *dst = cluster.map_shared_rank(rd, lane);
+            A *dst = cluster.map_shared_rank(sl, lane);
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) dst[rank * 2 + q] = s[q];
+            for (int q = 0; q < NQ; ++q) dst[q * kMaxSlots + my] = v[q];
         }
+        cluster.sync();
     }
-    cluster.sync();
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
         A s = A(0);
-        for (uint32_t c = 0; c < C; ++c) s += rd[c * 2 + q];
-        v[q] = s;
+        if (lane < nwarps)
+            for (uint32_t c = 0; c < C; ++c) s += sl[q * kMaxSlots + c * 32 + lane];
+        v[q] = warp_sum(s);
     }
 }
 
@@ -236,8 +238,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
     T *vr = reinterpret_cast<T *>(sp); sp += Plan::vec(lp.kmax);
     T *uh = reinterpret_cast<T *>(sp); sp += Plan::halo();
     T *zh = reinterpret_cast<T *>(sp); sp += Plan::halo();
-    A *wpart = reinterpret_cast<A *>(sp); sp += Plan::kWpart;
-    A *red = reinterpret_cast<A *>(sp); sp += Plan::kRed;
+    A *slots = reinterpret_cast<A *>(sp); sp += Plan::kSlots;
     uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp);
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
         A eta, gg;
         {
             A v2[2] = {act ? A(r) * A(z) : A(0), act ? A(gam) * A(gam) : A(0)};
-            cluster_allreduce<A, 2>(v2, wpart, red, 1, cluster, C, rank);
+            cluster_allreduce<A, 2>(v2, slots, 1, cluster, C, rank);
             eta = v2[0];
             gg = v2[1];
         }
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
             A pap;
             {
                 A v1[1] = {act ? A(p) * A(y) : A(0)};
-                cluster_allreduce<A, 1>(v1, wpart, red, 0, cluster, C, rank);
+                cluster_allreduce<A, 1>(v1, slots, 0, cluster, C, rank);
                 pap = v1[0];
             }
             const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
@@ -407,7 +408,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
             if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(zh, rank + 1)[i] = z;
             {
                 A v2[2] = {act ? A(r) * A(z) : A(0), (act && relres) ? A(r) * A(r) : A(0)};
-                cluster_allreduce<A, 2>(v2, wpart, red, 1, cluster, C, rank);
+                cluster_allreduce<A, 2>(v2, slots, 1, cluster, C, rank);
                 eta_new = v2[0];
                 rr = v2[1];
             }

@@ -112,10 +112,10 @@ int get_registry(int device, Registry **out) {
     return GBDPCG_SUCCESS;
 }
 
-VariantInfo *find_variant(Registry *reg, bool f64, bool acc64, int np, bool ptri, bool mreg) {
+VariantInfo *find_variant(Registry *reg, bool f64, bool acc64, int np, bool ptri, int st, int rpt) {
     for (auto &vi : reg->list)
         if (vi.v.f64 == (int)f64 && vi.v.acc64 == (int)(acc64 || f64) && vi.v.np == np &&
-            vi.v.ptri == (int)ptri && vi.v.mreg == (int)mreg)
+            vi.v.ptri == (int)ptri && vi.v.st == st && vi.v.rpt == rpt)
             return &vi;
     return nullptr;
 }
@@ -163,8 +163,22 @@ struct Shape {
     bool plain = false;
 };
 
-// Threads per CTA the tuner allows for a variant (cap), before the register limit.
-uint32_t default_thread_cap(const VariantInfo *vi) { return (uint32_t)vi->max_threads; }
+// Storage / rows-per-thread candidates in order of preference: the first that
+// holds the system wins.  Rows held in registers are the fastest; S in
+// registers with Phi^-1 in shared memory holds 2 rows per thread (about 1.5x
+// the rows per SM); rows in shared memory hold the most but read every matrix
+// element from shared memory each iteration.
+struct Pref {
+    int st, rpt;
+};
+
+std::vector<Pref> storage_prefs(bool f64, bool ptri, uint32_t storage) {
+    if (storage == GBDPCG_STORAGE_REGISTERS) return {{0, 1}, {0, 2}};
+    if (storage == GBDPCG_STORAGE_SHARED) return {{2, 1}};
+    if (storage == GBDPCG_STORAGE_SPLIT) return ptri ? std::vector<Pref>{} : std::vector<Pref>{{1, 2}, {1, 1}};
+    if (f64) return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{0, 1}, {1, 1}, {2, 1}};
+    return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{1, 2}, {0, 1}, {1, 1}, {2, 1}};
+}
 
 int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layout,
                  const gbdpcg_config &cfg, Shape *out) {
@@ -180,26 +194,27 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
     }
     const bool ptri = layout == GBDPCG_PINV_CBTD;
     const bool acc64 = cfg.dot_precision == GBDPCG_DOT_FP64;
-    std::vector<bool> storages;
-    if (cfg.storage == GBDPCG_STORAGE_REGISTERS) storages = {true};
-    else if (cfg.storage == GBDPCG_STORAGE_SHARED) storages = {false};
-    else storages = {true, false};
-    for (bool mreg : storages) {
-        VariantInfo *vi = find_variant(reg, f64, acc64, np, ptri, mreg);
+    for (const Pref &pf : storage_prefs(f64, ptri, cfg.storage)) {
+        if (pf.rpt > 1 && (n % pf.rpt) != 0) continue;
+        VariantInfo *vi = find_variant(reg, f64, acc64, np, ptri, pf.st, pf.rpt);
         if (!vi) continue;
-        uint32_t cap = cfg.max_threads ? cfg.max_threads : default_thread_cap(vi);
+        uint32_t cap = cfg.max_threads ? cfg.max_threads : (uint32_t)vi->max_threads;
         cap = std::min<uint32_t>(cap, (uint32_t)vi->max_threads);
         const uint32_t c_lo = cfg.cluster_size ? cfg.cluster_size : 1;
         const uint32_t c_hi = cfg.cluster_size ? cfg.cluster_size : 16;
         for (uint32_t C = c_lo; C <= c_hi; ++C) {
             if (C > 8 && (C & (C - 1))) continue;  // large clusters: powers of two only
             const uint32_t K = (N + C - 1) / C;
-            if ((size_t)K * n > cap) continue;
+            const uint32_t thr = (K * n + pf.rpt - 1) / pf.rpt;
+            if (thr > cap) continue;
             if (vi->v.smem_bytes(K) > (size_t)reg->max_smem_optin) continue;
             s.vi = vi;
             s.C = C;
             s.K = K;
-            s.threads = std::max<uint32_t>(32, (K * n + 31) / 32 * 32);
+            // CTA sizes are rounded to 64 threads so that systems of similar
+            // size share a launch
+            s.threads = std::min<uint32_t>(cap, std::max<uint32_t>(64, (thr + 63) / 64 * 64));
+            if (s.threads < thr) s.threads = (thr + 31) / 32 * 32;
             *out = s;
             return GBDPCG_SUCCESS;
         }
@@ -277,7 +292,7 @@ int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
     if (!cfg) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "config is NULL");
     if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad pinv_layout");
     if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FP64 ||
-        cfg->algorithm > GBDPCG_ALGO_PLAIN || cfg->storage > GBDPCG_STORAGE_SHARED ||
+        cfg->algorithm > GBDPCG_ALGO_PLAIN || cfg->storage > GBDPCG_STORAGE_SPLIT ||
         cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad config field");
     if (!(cfg->exit_tol >= 0)) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "exit_tol must be >= 0");

@@ -7,24 +7,24 @@
 //     system from a device work queue (an atomic counter over a host-sorted,
 //     longest-first list).  C comes from the launch's cluster dimension.
 //   * CTA `rank` owns the contiguous knots [kb, ke), kb = rank*K, K = ceil(N/C).
-//   * Thread t of a CTA owns one matrix row: local knot t / n, row t % n.  Its
-//     row of S (3 blocks) and of Phi^-1 (1 or 3 blocks) is either held in
-//     registers for the whole solve (MREG) — the matvec is then a register tile
-//     fed by vectorised shared-memory loads of the p / r window — or staged in
-//     shared memory (for FP64 and large blocks, where registers do not fit).
+//   * Thread t of a CTA owns RPT consecutive matrix rows (RPT = 2 only for even
+//     n, so both rows lie in one knot and share every vector load).  The rows
+//     of S (3 blocks) and of Phi^-1 (1 or 3 blocks) are held for the whole
+//     solve either in registers (register-tile matvec fed by vectorised
+//     shared-memory loads of the p / r window) or in shared memory (staged
+//     once per system); ST selects: 0 both in registers, 1 S in registers and
+//     Phi^-1 in shared memory, 2 both in shared memory.
 //   * Vectors p and r live in shared memory with one halo knot on each side.
 //     Neighbour CTAs exchange boundary vectors through distributed shared
 //     memory (DSMEM): instead of re-publishing p and r after every update (as
-//     the reference does through global memory, include/pcg.cuh:175,205 and 4
-//     grid.sync per iteration), each CTA pushes its boundary upsilon = S p and
+//     the reference does through global memory, include/pcg.cuh:175,205, with
+//     4 grid.sync per iteration), each CTA pushes its boundary upsilon = S p and
 //     z = Phi^-1 r together with its dot-product partial, and the receiver
 //     applies the same fused multiply-add to its halo copy that the owner
 //     applies to the original (r_h -= alpha upsilon_h; p_h = z_h + beta p_h),
 //     so the halos stay bit-identical with two cluster barriers per iteration.
-//   * Dot products: warp shuffle butterfly -> per-warp partials in shared memory
-//     -> one CTA partial pushed to every CTA of the cluster -> barrier.cluster ->
-//     every thread sums the C partials in rank order.  All threads of the
-//     cluster therefore hold identical alpha, beta and exit decisions.
+//   * Dot products: see cluster_allreduce.  All threads of the cluster hold
+//     identical alpha, beta and exit decisions.
 // Arithmetic follows the reference: alpha = eta / p.Sp, lambda += alpha p,
 // r -= alpha Sp, beta = eta'/eta, p = z + beta p as fused multiply-adds; exit
 // on |r.z| < tol (include/pcg.cuh:195) or, optionally, on the relative
@@ -45,8 +45,13 @@ __device__ __forceinline__ double fma_rn(double a, double b, double c) { return 
 
 __host__ __device__ constexpr size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
-// Shared-memory plan of one CTA (element counts; every buffer 32-byte aligned).
-template <typename T, typename A, int NP, bool PTRI, bool MREG>
+enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2 };
+
+// Reduction slots: [2 buffers][2 values][16 ranks x 32 warps]
+constexpr int kMaxSlots = 16 * 32;
+
+// Shared-memory plan of one CTA (every buffer 32-byte aligned).
+template <typename T, typename A, int NP, bool PTRI, int ST>
 struct SmemPlan {
     static constexpr int NB_P = PTRI ? 3 : 1;
     __host__ __device__ static size_t vec(uint32_t kmax) {
@@ -54,20 +59,34 @@ struct SmemPlan {
     }
     __host__ __device__ static size_t halo() { return round_up((size_t)2 * NP * sizeof(T), 32); }
     __host__ __device__ static size_t mat_s(uint32_t kmax) {
-        return MREG ? 0 : round_up((size_t)kmax * 3 * NP * NP * sizeof(T), 32);
+        return ST == ST_SMEM ? round_up((size_t)kmax * 3 * NP * NP * sizeof(T), 32) : 0;
     }
     __host__ __device__ static size_t mat_p(uint32_t kmax) {
-        return MREG ? 0 : round_up((size_t)kmax * NB_P * NP * NP * sizeof(T), 32);
+        return ST >= ST_REG_S ? round_up((size_t)kmax * NB_P * NP * NP * sizeof(T), 32) : 0;
     }
-    // reduction slots: 2 buffers x 2 values x (16 ranks x 32 warps)
-    static constexpr size_t kSlots = 2 * 2 * 16 * 32 * sizeof(A);
+    static constexpr size_t kSlots = 2 * 2 * kMaxSlots * sizeof(A);
     __host__ __device__ static size_t bytes(uint32_t kmax) {
         return 2 * vec(kmax) + 2 * halo() + kSlots + 32 + mat_s(kmax) + mat_p(kmax);
     }
 };
 
-// Load NP consecutive shared-memory elements into registers with the widest
-// aligned vector loads (base is NP-element aligned).
+// Register budget of one thread: the matrix rows it holds plus a fixed base.
+// The launch bound caps the compiler at that budget, so a CTA of up to
+// max_threads rows always fits one SM's 64K registers (warps are spread over 4
+// sub-partitions of 16K registers: whole groups of 4 warps).
+template <typename T, typename A, int NP, bool PTRI, int ST, int RPT>
+struct RegBudget {
+    static constexpr int words = (int)(sizeof(T) / 4);
+    static constexpr int matrix =
+        RPT * ((ST <= ST_REG_S ? 3 * NP : 0) + (ST == ST_REG ? (PTRI ? 3 : 1) * NP : 0)) * words;
+    static constexpr int base = ((sizeof(T) == 8 || sizeof(A) == 8) ? 72 : 56) + 8 * (RPT - 1) * words;
+    static constexpr int regs = matrix + base > 255 ? 255 : matrix + base;
+    static constexpr int max_threads_raw = 65536 / regs / 128 * 128;
+    static constexpr int max_threads = max_threads_raw > 1024 ? 1024 : max_threads_raw;
+};
+
+// Load NP consecutive shared-memory elements (NP-element aligned) into
+// registers with the widest aligned vector loads.
 template <typename T, int NP>
 __device__ __forceinline__ void lds_row(T (&x)[NP], const T *p) {
     if constexpr (sizeof(T) == 4 && NP % 4 == 0) {
@@ -94,46 +113,71 @@ __device__ __forceinline__ void lds_row(T (&x)[NP], const T *p) {
     }
 }
 
-// Register-tile block-row matvec: y = sum_b sum_j M[b][j] * x[b*NP + j].
-// One accumulator chain per block, summed in block order.
-template <typename T, int NP, int NB>
-__device__ __forceinline__ T reg_matvec(const T (&M)[NB * NP], const T *x) {
-    T acc[NB];
+// Register-tile block-row matvec of RPT rows sharing one window:
+// y[q] = sum_b sum_j M[q][b*NP + j] * x[b*NP + j]; one accumulator chain per
+// block, summed in block order.
+template <typename T, int NP, int NB, int RPT>
+__device__ __forceinline__ void reg_matvec(const T (&M)[RPT][NB * NP], const T *x, T (&y)[RPT]) {
+    T acc[RPT][NB];
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         T xv[NP];
         lds_row<T, NP>(xv, x + b * NP);
-        acc[b] = T(0);
 #pragma unroll
-        for (int j = 0; j < NP; ++j) acc[b] = fma_rn(M[b * NP + j], xv[j], acc[b]);
+        for (int q = 0; q < RPT; ++q) {
+            acc[q][b] = T(0);
+#pragma unroll
+            for (int j = 0; j < NP; ++j) acc[q][b] = fma_rn(M[q][b * NP + j], xv[j], acc[q][b]);
+        }
     }
-    T y = acc[0];
 #pragma unroll
-    for (int b = 1; b < NB; ++b) y += acc[b];
-    return y;
+    for (int q = 0; q < RPT; ++q) {
+        T s = acc[q][0];
+#pragma unroll
+        for (int b = 1; b < NB; ++b) s += acc[q][b];
+        y[q] = s;
+    }
 }
 
-// Shared-memory block-row matvec over the present blocks [b0, b1) of a
-// column-major n x (NB n) block row staged in shared memory; x points at the
-// window of block 0 (windows are NP apart).
-template <typename T, int NP, int NB>
-__device__ __forceinline__ T smem_matvec(const T *Mrow, int b0, int b1, const T *x, uint32_t n,
-                                         uint32_t i) {
-    T acc[NB];
+// Shared-memory block-row matvec of RPT adjacent rows i..i+RPT-1 over the
+// present blocks [b0, b1) of a column-major n x (NB n) block row; x points at
+// the window of block 0 (windows are NP apart).  Same summation order as
+// reg_matvec (padding there contributes exact zeros).
+template <typename T, int NP, int NB, int RPT>
+__device__ __forceinline__ void smem_matvec(const T *Mrow, int b0, int b1, const T *x, uint32_t n,
+                                            uint32_t i, T (&y)[RPT]) {
+    T acc[RPT][NB];
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
-        acc[b] = T(0);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) acc[q][b] = T(0);
         if (b >= b0 && b < b1) {
             const T *col = Mrow + (size_t)b * n * n + i;
             const T *xb = x + b * NP;
 #pragma unroll 4
-            for (uint32_t j = 0; j < n; ++j) acc[b] = fma_rn(col[(size_t)j * n], xb[j], acc[b]);
+            for (uint32_t j = 0; j < n; ++j) {
+                const T xj = xb[j];
+                if constexpr (RPT == 2 && sizeof(T) == 4) {
+                    const float2 m = *reinterpret_cast<const float2 *>(col + (size_t)j * n);
+                    acc[0][b] = fma_rn(m.x, xj, acc[0][b]);
+                    acc[1][b] = fma_rn(m.y, xj, acc[1][b]);
+                } else if constexpr (RPT == 2) {
+                    const double2 m = *reinterpret_cast<const double2 *>(col + (size_t)j * n);
+                    acc[0][b] = fma_rn(m.x, xj, acc[0][b]);
+                    acc[1][b] = fma_rn(m.y, xj, acc[1][b]);
+                } else {
+                    acc[0][b] = fma_rn(col[(size_t)j * n], xj, acc[0][b]);
+                }
+            }
         }
     }
-    T y = acc[0];
 #pragma unroll
-    for (int b = 1; b < NB; ++b) y += acc[b];
-    return y;
+    for (int q = 0; q < RPT; ++q) {
+        T s = acc[q][0];
+#pragma unroll
+        for (int b = 1; b < NB; ++b) s += acc[q][b];
+        y[q] = s;
+    }
 }
 
 template <typename A>
@@ -157,8 +201,6 @@ __device__ __forceinline__ A warp_sum(A v) {
 // from thread 0), so the result does not depend on the CTA size either.
 // `buf` alternates between call sites so that a slot array is rewritten only
 // after a barrier that every reader has passed.
-constexpr int kMaxSlots = 16 * 32;  // ranks x warps
-
 template <typename A, int NQ>
 __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
                                                   const cg::cluster_group &cluster, uint32_t C,
@@ -199,34 +241,16 @@ __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uin
         __syncthreads();
 }
 
-template <typename T>
-__device__ __forceinline__ bool finite_(T x) {
-    return isfinite(x);
-}
-
 // The solver.  T: storage and arithmetic type of matrices and vectors;
 // A: accumulation type of the dot products (T, or double for mixed precision);
-// NP: compile-time block size bound (n <= NP); PTRI: Phi^-1 is block-
-// tridiagonal; MREG: matrix rows held in registers (else in shared memory).
-// Register budget of one thread: the matrix rows it holds plus a fixed base.
-// The launch bound caps the compiler at that budget, so a CTA of up to
-// max_threads() rows always fits one SM's 64K registers.
-template <typename T, typename A, int NP, bool PTRI, bool MREG>
-struct RegBudget {
-    static constexpr int words = (int)(sizeof(T) / 4);
-    static constexpr int matrix = MREG ? (3 + (PTRI ? 3 : 1)) * NP * words : 0;
-    static constexpr int base = (sizeof(T) == 8 || sizeof(A) == 8) ? 80 : 64;
-    static constexpr int regs = matrix + base > 255 ? 255 : matrix + base;
-    // warps are spread over 4 sub-partitions of 16K registers each: whole groups of 4 warps
-    static constexpr int max_threads_raw = 65536 / regs / 128 * 128;
-    static constexpr int max_threads = max_threads_raw > 1024 ? 1024 : max_threads_raw;
-};
-
-template <typename T, typename A, int NP, bool PTRI, bool MREG>
-__global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads), 1)
+// NP: compile-time block-size bound (n <= NP); PTRI: Phi^-1 is block-
+// tridiagonal; ST: storage of the matrix rows; RPT: rows per thread.
+template <typename T, typename A, int NP, bool PTRI, int ST, int RPT>
+__global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threads), 1)
     pcg_cluster_kernel(const LaunchParams lp) {
-    using Plan = SmemPlan<T, A, NP, PTRI, MREG>;
+    using Plan = SmemPlan<T, A, NP, PTRI, ST>;
     constexpr int NBP = PTRI ? 3 : 1;
+    constexpr bool S_REG = ST <= ST_REG_S, P_REG = ST == ST_REG;
     const cg::cluster_group cluster = cg::this_cluster();
     const uint32_t C = cluster.num_blocks();
     const uint32_t rank = cluster.block_rank();
@@ -242,7 +266,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
     uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp);
-    const size_t zero_elems = (2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T);
+    const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
 
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     for (uint32_t pass = 0;; ++pass) {
@@ -263,7 +287,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
         const SysDesc d = lp.descs ? lp.descs[lp.order ? lp.order[item] : item] : lp.one;
         const uint32_t n = d.n, N = d.N;
         const uint32_t K = (N + C - 1) / C;
-        if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (size_t)K * n > nthr) {
+        if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (size_t)K * n > (size_t)nthr * RPT ||
+            (RPT > 1 && (n % RPT) != 0)) {
             if (rank == 0 && tid == 0) {
                 SysResult res = {};
                 res.status = -1;
@@ -273,7 +298,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
             continue;                // uniform: every CTA of the cluster sees the same descriptor
         }
         const uint32_t kb = min(rank * K, N), ke = min(kb + K, N), nk = ke - kb;
-        const uint32_t lk = tid / n, i = tid - lk * n;
+        const uint32_t row0 = tid * RPT;
+        const uint32_t lk = row0 / n, i = row0 - lk * n;  // rows i .. i+RPT-1 of local knot lk
         const bool act = lk < nk;
         const uint32_t k = kb + lk;
         const bool relres = (d.flags & SYS_EXIT_RELRES) != 0;
@@ -282,62 +308,75 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
         const T *__restrict__ gamma = static_cast<const T *>(d.gamma);
         const T *__restrict__ lam0 =
             (d.flags & SYS_LAMBDA0_ZERO) ? nullptr : static_cast<const T *>(d.lambda0);
-        const size_t blkS = (size_t)3 * n * n, blkP = (size_t)NBP * n * n;
+        const uint32_t blkS = 3 * n * n, blkP = NBP * n * n;
         const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
+        const bool first_knot = act && lk == 0 && kb > 0, last_knot = act && lk + 1 == nk && ke < N;
 
-        for (size_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
+        for (uint32_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
 
         // ---- matrices: registers or shared memory
-        T Sr[MREG ? 3 * NP : 1];
-        T Pr[MREG ? NBP * NP : 1];
-        if constexpr (MREG) {
+        T Sr[S_REG ? RPT : 1][S_REG ? 3 * NP : 1];
+        T Pr[P_REG ? RPT : 1][P_REG ? NBP * NP : 1];
+        if constexpr (S_REG) {
             const T *Sk = S + (size_t)k * blkS;
-            const T *Pk = P + (size_t)k * blkP;
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
                 const bool present = act && (b != 0 || k > 0) && (b != 2 || k + 1 < N);
 #pragma unroll
                 for (int j = 0; j < NP; ++j)
-                    Sr[b * NP + j] =
-                        (present && (uint32_t)j < n) ? __ldg(Sk + (size_t)(b * n + j) * n + i) : T(0);
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q)
+                        Sr[q][b * NP + j] = (present && (uint32_t)j < n)
+                                                ? __ldg(Sk + (b * n + j) * n + i + q)
+                                                : T(0);
             }
+        } else {
+            const T *Sg = S + (size_t)kb * blkS;
+            for (uint32_t e = tid; e < nk * blkS; e += nthr) ms[e] = __ldg(Sg + e);
+        }
+        if constexpr (P_REG) {
+            const T *Pk = P + (size_t)k * blkP;
 #pragma unroll
             for (int b = 0; b < NBP; ++b) {
                 const bool present =
                     act && (!PTRI || ((b != 0 || k > 0) && (b != 2 || k + 1 < N)));
 #pragma unroll
                 for (int j = 0; j < NP; ++j)
-                    Pr[b * NP + j] =
-                        (present && (uint32_t)j < n) ? __ldg(Pk + (size_t)(b * n + j) * n + i) : T(0);
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q)
+                        Pr[q][b * NP + j] = (present && (uint32_t)j < n)
+                                                ? __ldg(Pk + (b * n + j) * n + i + q)
+                                                : T(0);
             }
         } else {
-            const T *Sg = S + (size_t)kb * blkS;
             const T *Pg = P + (size_t)kb * blkP;
-            for (size_t e = tid; e < nk * blkS; e += nthr) ms[e] = __ldg(Sg + e);
-            for (size_t e = tid; e < nk * blkP; e += nthr) mp[e] = __ldg(Pg + e);
+            for (uint32_t e = tid; e < nk * blkP; e += nthr) mp[e] = __ldg(Pg + e);
         }
         const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
-        auto matS = [&](const T *x) -> T {
-            if constexpr (MREG) return reg_matvec<T, NP, 3>(Sr, x);
-            else return smem_matvec<T, NP, 3>(ms + lk * blkS, sb0, sb1, x, n, i);
+        auto matS = [&](const T *x, T(&y)[RPT]) {
+            if constexpr (S_REG) reg_matvec<T, NP, 3, RPT>(Sr, x, y);
+            else smem_matvec<T, NP, 3, RPT>(ms + lk * blkS, sb0, sb1, x, n, i, y);
         };
-        auto matP = [&](const T *x) -> T {
-            if constexpr (MREG) {
-                if constexpr (PTRI) return reg_matvec<T, NP, 3>(Pr, x);
-                else return reg_matvec<T, NP, 1>(Pr, x + NP);
+        auto matP = [&](const T *x, T(&y)[RPT]) {
+            if constexpr (P_REG) {
+                if constexpr (PTRI) reg_matvec<T, NP, 3, RPT>(Pr, x, y);
+                else reg_matvec<T, NP, 1, RPT>(Pr, x + NP, y);
             } else {
-                if constexpr (PTRI) return smem_matvec<T, NP, 3>(mp + lk * blkP, sb0, sb1, x, n, i);
-                else return smem_matvec<T, NP, 1>(mp + lk * blkP, 0, 1, x + NP, n, i);
+                if constexpr (PTRI) smem_matvec<T, NP, 3, RPT>(mp + lk * blkP, sb0, sb1, x, n, i, y);
+                else smem_matvec<T, NP, 1, RPT>(mp + lk * blkP, 0, 1, x + NP, n, i, y);
             }
         };
+        T *my_p = vp + (lk + 1) * NP + i;  // this thread's rows in the windows
+        T *my_r = vr + (lk + 1) * NP + i;
         __syncthreads();
 
         // ---- r = gamma - S lambda0   (include/pcg.cuh:119-126)
-        T gam = T(0), lam = T(0);
-        if (act) {
-            gam = gamma[(size_t)k * n + i];
-            lam = lam0 ? lam0[(size_t)k * n + i] : T(0);
-            vp[(lk + 1) * NP + i] = lam;
+        T gam[RPT], lam[RPT], r[RPT], p[RPT], z[RPT], y[RPT];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            gam[q] = act ? gamma[(size_t)k * n + i + q] : T(0);
+            lam[q] = (act && lam0) ? lam0[(size_t)k * n + i + q] : T(0);
+            if (act) my_p[q] = lam[q];
         }
         if (lam0) {
             for (uint32_t t = tid; t < 2 * n; t += nthr) {
@@ -346,26 +385,56 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
             }
         }
         __syncthreads();
-        T r = act ? gam - matS(vp + lk * NP) : T(0);
+        if (act) matS(vp + lk * NP, y);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) r[q] = act ? gam[q] - y[q] : T(0);
         group_sync(cluster, C);  // all windows read before any neighbour writes into them
 
         // ---- z = Phi^-1 r; p = z; eta = r.z   (include/pcg.cuh:131-149)
-        if (act) vr[(lk + 1) * NP + i] = r;
+        if (act) {
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) my_r[q] = r[q];
+        }
         if constexpr (PTRI) {
-            if (act && lk == 0 && kb > 0) cluster.map_shared_rank(vr, rank - 1)[(K + 1) * NP + i] = r;
-            if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(vr, rank + 1)[i] = r;
+            if (first_knot) {
+                T *dst = cluster.map_shared_rank(vr, rank - 1) + (K + 1) * NP + i;
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) dst[q] = r[q];
+            }
+            if (last_knot) {
+                T *dst = cluster.map_shared_rank(vr, rank + 1) + i;
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) dst[q] = r[q];
+            }
             group_sync(cluster, C);
         } else {
             __syncthreads();
         }
-        T z = act ? matP(vr + lk * NP) : T(0);
-        T p = z;
-        if (act) vp[(lk + 1) * NP + i] = p;
-        if (act && lk == 0 && kb > 0) cluster.map_shared_rank(vp, rank - 1)[(K + 1) * NP + i] = z;
-        if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(vp, rank + 1)[i] = z;
+        if (act) matP(vr + lk * NP, z);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            if (!act) z[q] = T(0);
+            p[q] = z[q];
+            if (act) my_p[q] = p[q];
+        }
+        if (first_knot) {
+            T *dst = cluster.map_shared_rank(vp, rank - 1) + (K + 1) * NP + i;
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) dst[q] = z[q];
+        }
+        if (last_knot) {
+            T *dst = cluster.map_shared_rank(vp, rank + 1) + i;
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) dst[q] = z[q];
+        }
         A eta, gg;
         {
-            A v2[2] = {act ? A(r) * A(z) : A(0), act ? A(gam) * A(gam) : A(0)};
+            A v2[2] = {A(0), A(0)};
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) {
+                v2[0] += A(r[q]) * A(z[q]);
+                v2[1] += A(gam[q]) * A(gam[q]);
+            }
             cluster_allreduce<A, 2>(v2, slots, 1, cluster, C, rank);
             eta = v2[0];
             gg = v2[1];
@@ -377,22 +446,40 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
         uint32_t iter = 0;
         int32_t status = ST_MAX_ITER;
         A eta_new = A(0), rr = A(0);
-        for (; iter < d.max_iter;) {
-            const T y = act ? matS(vp + lk * NP) : T(0);
+        const uint32_t max_iter = d.max_iter;
+        for (; iter < max_iter;) {
+            if (act) matS(vp + lk * NP, y);
+            else {
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) y[q] = T(0);
+            }
             if constexpr (PTRI) {  // neighbours need this CTA's boundary upsilon for their r halo
-                if (act && lk == 0 && kb > 0) cluster.map_shared_rank(uh, rank - 1)[NP + i] = y;
-                if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(uh, rank + 1)[i] = y;
+                if (first_knot) {
+                    T *dst = cluster.map_shared_rank(uh, rank - 1) + NP + i;
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) dst[q] = y[q];
+                }
+                if (last_knot) {
+                    T *dst = cluster.map_shared_rank(uh, rank + 1) + i;
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) dst[q] = y[q];
+                }
             }
             A pap;
             {
-                A v1[1] = {act ? A(p) * A(y) : A(0)};
+                A v1[1] = {A(0)};
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) v1[0] += A(p[q]) * A(y[q]);
                 cluster_allreduce<A, 1>(v1, slots, 0, cluster, C, rank);
                 pap = v1[0];
             }
             const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
-            lam = fma_rn(alpha, p, lam);
-            r = fma_rn(-alpha, y, r);
-            if (act) vr[(lk + 1) * NP + i] = r;
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) {
+                lam[q] = fma_rn(alpha, p[q], lam[q]);
+                r[q] = fma_rn(-alpha, y[q], r[q]);
+                if (act) my_r[q] = r[q];
+            }
             if constexpr (PTRI) {
                 for (uint32_t t = tid; t < 2 * n; t += nthr) {
                     if (t < n && has_left) vr[t] = fma_rn(-alpha, uh[t], vr[t]);
@@ -403,22 +490,42 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
                 }
             }
             __syncthreads();
-            z = act ? matP(vr + lk * NP) : T(0);
-            if (act && lk == 0 && kb > 0) cluster.map_shared_rank(zh, rank - 1)[NP + i] = z;
-            if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(zh, rank + 1)[i] = z;
+            if (act) matP(vr + lk * NP, z);
+            else {
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) z[q] = T(0);
+            }
+            if (first_knot) {
+                T *dst = cluster.map_shared_rank(zh, rank - 1) + NP + i;
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) dst[q] = z[q];
+            }
+            if (last_knot) {
+                T *dst = cluster.map_shared_rank(zh, rank + 1) + i;
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) dst[q] = z[q];
+            }
             {
-                A v2[2] = {act ? A(r) * A(z) : A(0), (act && relres) ? A(r) * A(r) : A(0)};
+                A v2[2] = {A(0), A(0)};
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) {
+                    v2[0] += A(r[q]) * A(z[q]);
+                    if (relres) v2[1] += A(r[q]) * A(r[q]);
+                }
                 cluster_allreduce<A, 2>(v2, slots, 1, cluster, C, rank);
                 eta_new = v2[0];
                 rr = v2[1];
             }
             ++iter;
-            if (!finite_(eta_new) || !finite_(pap)) { status = ST_BREAKDOWN; break; }
+            if (!isfinite(eta_new) || !isfinite(pap)) { status = ST_BREAKDOWN; break; }
             if (relres ? (rr <= thr) : (fabs(eta_new) < tol)) { status = ST_CONVERGED; break; }
             const T beta = T(eta_new / eta);
             eta = eta_new;
-            p = fma_rn(beta, p, z);
-            if (act) vp[(lk + 1) * NP + i] = p;
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) {
+                p[q] = fma_rn(beta, p[q], z[q]);
+                if (act) my_p[q] = p[q];
+            }
             for (uint32_t t = tid; t < 2 * n; t += nthr) {
                 if (t < n && has_left) vp[t] = fma_rn(beta, vp[t], zh[t]);
                 if (t >= n && has_right) {
@@ -431,7 +538,10 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
 
         // ---- outputs   (include/pcg.cuh:212-217)
         T *lam_out = static_cast<T *>(d.lambda);
-        if (act) lam_out[(size_t)k * n + i] = lam;
+        if (act) {
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) lam_out[(size_t)k * n + i + q] = lam[q];
+        }
         if (rank == 0 && tid == 0) {
             SysResult res;
             res.iters = iter;
@@ -449,28 +559,41 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, MREG>::max_threads)
             const T *lf = static_cast<const T *>(d.lam_fwd);
             T *dS = static_cast<T *>(d.dS);
             group_sync(cluster, C);  // vp / vr free in every CTA
-            T lfi = T(0);
-            if (act) {
-                lfi = lf[(size_t)k * n + i];
-                vr[(lk + 1) * NP + i] = lam;  // mu
-                vp[(lk + 1) * NP + i] = lfi;
+            T lfi[RPT];
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) {
+                lfi[q] = act ? lf[(size_t)k * n + i + q] : T(0);
+                if (act) {
+                    my_r[q] = lam[q];  // mu
+                    my_p[q] = lfi[q];
+                }
             }
-            if (act && lk == 0 && kb > 0) cluster.map_shared_rank(vr, rank - 1)[(K + 1) * NP + i] = lam;
-            if (act && lk + 1 == nk && ke < N) cluster.map_shared_rank(vr, rank + 1)[i] = lam;
+            if (first_knot) {
+                T *dst = cluster.map_shared_rank(vr, rank - 1) + (K + 1) * NP + i;
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) dst[q] = lam[q];
+            }
+            if (last_knot) {
+                T *dst = cluster.map_shared_rank(vr, rank + 1) + i;
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) dst[q] = lam[q];
+            }
             for (uint32_t t = tid; t < 2 * n; t += nthr) {
                 if (t < n && has_left) vp[t] = lf[(size_t)(kb - 1) * n + t];
                 if (t >= n && has_right) vp[(nk + 1) * NP + (t - n)] = lf[(size_t)ke * n + (t - n)];
             }
             group_sync(cluster, C);
             if (act) {
-                T *row = dS + (size_t)k * blkS + i;
                 for (uint32_t b = 0; b < 3; ++b) {
                     const bool present = (b != 0 || k > 0) && (b != 2 || k + 1 < N);
                     const T *lw = vp + (lk + b) * NP;
                     const T *mw = vr + (lk + b) * NP;
                     for (uint32_t j = 0; j < n; ++j) {
-                        const T g = present ? T(-0.5) * fma_rn(lam, lw[j], lfi * mw[j]) : T(0);
-                        row[(size_t)(b * n + j) * n] = g;
+#pragma unroll
+                        for (int q = 0; q < RPT; ++q) {
+                            const T g = present ? T(-0.5) * fma_rn(lam[q], lw[j], lfi[q] * mw[j]) : T(0);
+                            dS[(size_t)k * blkS + (b * n + j) * n + i + q] = g;
+                        }
                     }
                 }
             }

@@ -5,8 +5,9 @@ namespace gbdpcg {
 int variants_np24(KernelVariant *out) {
     int c = 0;
     GBDPCG_VARIANTS_F32(24)
+    GBDPCG_VARIANTS_F32_RPT2(24)
     GBDPCG_VARIANTS_F64_SMEM(24)
-
+    out[c++] = GBDPCG_VARIANT(double, double, 24, false, ST_REG_S, 1);
     return c;
 }
 }  // namespace gbdpcg

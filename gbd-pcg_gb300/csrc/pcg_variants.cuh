@@ -4,22 +4,28 @@
 #include "pcg_cluster.cuh"
 #include "pcg_variants.h"
 
-#define GBDPCG_VARIANT(T, A, NP, PTRI, MREG)                                                  \
+#define GBDPCG_VARIANT(T, A, NP, PTRI, ST, RPT)                                               \
     ::gbdpcg::KernelVariant {                                                                 \
-        sizeof(T) == 8, sizeof(A) == 8, NP, PTRI, MREG,                                       \
-            (const void *)&::gbdpcg::pcg_cluster_kernel<T, A, NP, PTRI, MREG>,                \
-            &::gbdpcg::SmemPlan<T, A, NP, PTRI, MREG>::bytes                                  \
+        sizeof(T) == 8, sizeof(A) == 8, NP, PTRI, ST, RPT,                                    \
+            (const void *)&::gbdpcg::pcg_cluster_kernel<T, A, NP, PTRI, ST, RPT>,             \
+            &::gbdpcg::SmemPlan<T, A, NP, PTRI, ST>::bytes                                    \
     }
 
-// fp32 in registers (native and FP64 dot accumulation) and in shared memory;
-// fp64 in shared memory, and in registers where the rows fit.
+// FP32: rows in registers (RPT 1; RPT 2 for even bounds), S in registers with
+// Phi^-1 in shared memory, both in shared memory; FP64 dot accumulation with
+// rows in registers.
 #define GBDPCG_VARIANTS_F32(NP)                                                               \
-    out[c++] = GBDPCG_VARIANT(float, float, NP, false, true);                                 \
-    out[c++] = GBDPCG_VARIANT(float, float, NP, true, true);                                  \
-    out[c++] = GBDPCG_VARIANT(float, double, NP, false, true);                                \
-    out[c++] = GBDPCG_VARIANT(float, double, NP, true, true);                                 \
-    out[c++] = GBDPCG_VARIANT(float, float, NP, false, false);                                \
-    out[c++] = GBDPCG_VARIANT(float, float, NP, true, false);
+    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_REG, 1);                            \
+    out[c++] = GBDPCG_VARIANT(float, float, NP, true, ST_REG, 1);                             \
+    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_REG_S, 1);                          \
+    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_SMEM, 1);                           \
+    out[c++] = GBDPCG_VARIANT(float, float, NP, true, ST_SMEM, 1);                            \
+    out[c++] = GBDPCG_VARIANT(float, double, NP, false, ST_REG, 1);                           \
+    out[c++] = GBDPCG_VARIANT(float, double, NP, true, ST_REG, 1);
+#define GBDPCG_VARIANTS_F32_RPT2(NP)                                                          \
+    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_REG, 2);                            \
+    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_REG_S, 2);
+// FP64: rows in shared memory, and in registers where they fit.
 #define GBDPCG_VARIANTS_F64_SMEM(NP)                                                          \
-    out[c++] = GBDPCG_VARIANT(double, double, NP, false, false);                              \
-    out[c++] = GBDPCG_VARIANT(double, double, NP, true, false);
+    out[c++] = GBDPCG_VARIANT(double, double, NP, false, ST_SMEM, 1);                         \
+    out[c++] = GBDPCG_VARIANT(double, double, NP, true, ST_SMEM, 1);

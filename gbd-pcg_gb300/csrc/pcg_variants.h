@@ -10,12 +10,14 @@ struct KernelVariant {
     int acc64;   // dot products accumulated in double
     int np;      // compile-time block-size bound (n <= np)
     int ptri;    // Phi^-1 block-tridiagonal (cbtd) instead of block-diagonal
-    int mreg;    // matrix rows in registers (else staged in shared memory)
+    int st;      // storage: 0 S and Phi^-1 in registers, 1 S in registers and Phi^-1 in
+                 // shared memory, 2 both in shared memory
+    int rpt;     // matrix rows per thread (2 needs an even n)
     const void *func;
     size_t (*smem_bytes)(uint32_t kmax);
 };
 
-// Each returns the number of variants written to `out` (at most 16).
+// Each returns the number of variants written to `out` (at most 24).
 int variants_np6(KernelVariant *out);
 int variants_np8(KernelVariant *out);
 int variants_np12(KernelVariant *out);

@@ -29,7 +29,7 @@ EXIT_REFERENCE, EXIT_RELRES = 0, 1
 PINV_CBTD, PINV_BLOCKDIAG = 0, 1
 ALGO_AUTO, ALGO_CLUSTER, ALGO_PLAIN = 0, 1, 2
 DOT_NATIVE, DOT_FP64 = 0, 1
-STORAGE_AUTO, STORAGE_REGISTERS, STORAGE_SHARED = 0, 1, 2
+STORAGE_AUTO, STORAGE_REGISTERS, STORAGE_SHARED, STORAGE_SPLIT = 0, 1, 2, 3
 
 
 class GbdpcgError(RuntimeError):

@@ -72,8 +72,15 @@ enum {
 };
 /* dot-product accumulation for float systems */
 enum { GBDPCG_DOT_NATIVE = 0, GBDPCG_DOT_FP64 = 1 };
-/* where the cluster solver keeps the matrix rows */
-enum { GBDPCG_STORAGE_AUTO = 0, GBDPCG_STORAGE_REGISTERS = 1, GBDPCG_STORAGE_SHARED = 2 };
+/* where the cluster solver keeps the matrix rows: AUTO picks; REGISTERS: S and
+ * Phi^-1 rows in registers; SHARED: both staged in shared memory; SPLIT: S rows
+ * in registers (two per thread for even n), Phi^-1 in shared memory */
+enum {
+    GBDPCG_STORAGE_AUTO = 0,
+    GBDPCG_STORAGE_REGISTERS = 1,
+    GBDPCG_STORAGE_SHARED = 2,
+    GBDPCG_STORAGE_SPLIT = 3
+};
 
 typedef struct {
     double exit_tol;         /* pcg_exit_tol, default 1e-6 (include/constants.cuh:17) */

@@ -218,3 +218,31 @@ def test_batched_plan_matches_single(gb, oracle_mod, handle):
             assert r.status == gb.CONVERGED and r.iters == it1
             assert s["lambda"].cpu().numpy().tobytes() == lam1.tobytes()
     plan.close()
+
+
+@pytest.mark.parametrize("dts", ["f32", "f64"])
+@pytest.mark.parametrize("storage", ["registers", "shared", "split"])
+@pytest.mark.parametrize("n,N", [(6, 70), (14, 128), (24, 100), (7, 33)])
+def test_every_storage_variant(gb, oracle_mod, handle, dts, storage, n, N):
+    """Each way of holding the rows (registers; shared memory; S in registers
+    with Phi^-1 in shared memory, two rows per thread for even n) converges
+    like the oracle on the block-diagonal preconditioner."""
+    import torch
+    O = oracle_mod
+    dt = _dt(dts)
+    sy, S, P, g = system(O, n, N, 21, dt, "compact")
+    tol = 1e-6 if dts == "f32" else 1e-12
+    lam_o, it_o, st_o, _, _ = O.pcg(S, P, g, np.zeros(n * N, dt), n, N, 500, tol,
+                                    flags=O.PINV_BLOCKDIAG | O.EXIT_RELRES)
+    d = torch.device("cuda:0")
+    lam = torch.zeros(n * N, dtype=torch.float64 if dts == "f64" else torch.float32, device=d)
+    st = {"registers": gb.STORAGE_REGISTERS, "shared": gb.STORAGE_SHARED, "split": gb.STORAGE_SPLIT}[storage]
+    try:
+        r = handle.solve(*(torch.from_numpy(a).to(d) for a in (S, P, g)), lam, n, N, gb.PINV_BLOCKDIAG,
+                         gb.config(max_iter=500, exit_tol=tol, exit_mode=gb.EXIT_RELRES, storage=st))
+    except gb.GbdpcgError as e:
+        assert e.code == gb.ERR_UNSUPPORTED
+        pytest.skip(f"no {storage} shape at n={n} N={N}: {e}")
+    assert r.status == gb.CONVERGED and abs(int(r.iters) - it_o) <= 1, (r, it_o)
+    x = O.block_cholesky_solve(S.astype(np.float64), n, N, g.astype(np.float64))
+    assert relerr(lam.cpu().numpy(), x) <= 1.5 * relerr(lam_o, x) + (1e-6 if dts == "f32" else 1e-13)

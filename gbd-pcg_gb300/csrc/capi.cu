@@ -89,7 +89,7 @@ int get_registry(int device, Registry **out) {
         return GBDPCG_SUCCESS;
     }
     auto reg = std::make_unique<Registry>();
-    KernelVariant buf[16];
+    KernelVariant buf[kMaxVariantsPerNP];
     int (*fns[])(KernelVariant *) = {variants_np6, variants_np8, variants_np12, variants_np14,
                                      variants_np16, variants_np24, variants_np32};
     for (auto fn : fns) {
@@ -112,10 +112,11 @@ int get_registry(int device, Registry **out) {
     return GBDPCG_SUCCESS;
 }
 
-VariantInfo *find_variant(Registry *reg, bool f64, bool acc64, int np, bool ptri, int st, int rpt) {
+VariantInfo *find_variant(Registry *reg, bool f64, bool acc64, int np, bool ptri, int st, int rpt,
+                          int alg) {
     for (auto &vi : reg->list)
         if (vi.v.f64 == (int)f64 && vi.v.acc64 == (int)(acc64 || f64) && vi.v.np == np &&
-            vi.v.ptri == (int)ptri && vi.v.st == st && vi.v.rpt == rpt)
+            vi.v.ptri == (int)ptri && vi.v.st == st && vi.v.rpt == rpt && vi.v.alg == alg)
             return &vi;
     return nullptr;
 }
@@ -194,9 +195,12 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
     }
     const bool ptri = layout == GBDPCG_PINV_CBTD;
     const bool acc64 = cfg.dot_precision == GBDPCG_DOT_FP64;
+    const int alg = cfg.algorithm == GBDPCG_ALGO_SINGLE_REDUCTION ? 1 : 0;
+    if (alg == 1 && ptri)
+        return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm needs a block-diagonal Phi^-1");
     for (const Pref &pf : storage_prefs(f64, ptri, cfg.storage)) {
         if (pf.rpt > 1 && (n % pf.rpt) != 0) continue;
-        VariantInfo *vi = find_variant(reg, f64, acc64, np, ptri, pf.st, pf.rpt);
+        VariantInfo *vi = find_variant(reg, f64, acc64, np, ptri, pf.st, pf.rpt, alg);
         if (!vi) continue;
         uint32_t cap = cfg.max_threads ? cfg.max_threads : (uint32_t)vi->max_threads;
         cap = std::min<uint32_t>(cap, (uint32_t)vi->max_threads);
@@ -207,7 +211,7 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
             const uint32_t K = (N + C - 1) / C;
             const uint32_t thr = (K * n + pf.rpt - 1) / pf.rpt;
             if (thr > cap) continue;
-            if (vi->v.smem_bytes(K) > (size_t)reg->max_smem_optin) continue;
+            if (vi->v.smem_bytes(K, C) > (size_t)reg->max_smem_optin) continue;
             s.vi = vi;
             s.C = C;
             s.K = K;
@@ -292,7 +296,7 @@ int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
     if (!cfg) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "config is NULL");
     if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad pinv_layout");
     if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FP64 ||
-        cfg->algorithm > GBDPCG_ALGO_PLAIN || cfg->storage > GBDPCG_STORAGE_SPLIT ||
+        cfg->algorithm > GBDPCG_ALGO_SINGLE_REDUCTION || cfg->storage > GBDPCG_STORAGE_SPLIT ||
         cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad config field");
     if (!(cfg->exit_tol >= 0)) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "exit_tol must be >= 0");
@@ -330,7 +334,7 @@ int launch_plain(gbdpcg_handle_s *h, bool f64, const SysDesc &d, SysResult *d_re
 
 int launch_cluster(const Shape &sh, const LaunchParams &lp, uint32_t grid_clusters,
                    cudaStream_t stream) {
-    const size_t smem = sh.vi->v.smem_bytes(lp.kmax);
+    const size_t smem = sh.vi->v.smem_bytes(lp.kmax, sh.C);
     int rc = prepare_variant(sh.vi, smem, sh.C);
     if (rc) return rc;
     cudaLaunchConfig_t cfg;
@@ -770,7 +774,7 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
         pc.order_off = (uint32_t)order.size();
         order.insert(order.end(), pc.items.begin(), pc.items.end());
         int active = 0;
-        rc = max_active_clusters(pc.sh, pc.sh.vi->v.smem_bytes(pc.kmax), &active);
+        rc = max_active_clusters(pc.sh, pc.sh.vi->v.smem_bytes(pc.kmax, pc.sh.C), &active);
         if (rc) return rc;
         if (active <= 0)
             return fail(GBDPCG_ERR_UNSUPPORTED, "cluster shape cannot be scheduled (C=" +

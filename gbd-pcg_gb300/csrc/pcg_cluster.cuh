@@ -47,8 +47,9 @@ __host__ __device__ constexpr size_t round_up(size_t x, size_t m) { return (x + 
 
 enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2 };
 
-// Reduction slots: [2 buffers][2 values][16 ranks x 32 warps]
-constexpr int kMaxSlots = 16 * 32;
+// Reduction slots: [2 buffers][3 values][C ranks x 32 warps]
+constexpr int kMaxValues = 3;
+__host__ __device__ constexpr size_t slot_stride(uint32_t C) { return (size_t)32 * C; }
 
 // Shared-memory plan of one CTA (every buffer 32-byte aligned).
 template <typename T, typename A, int NP, bool PTRI, int ST>
@@ -64,9 +65,11 @@ struct SmemPlan {
     __host__ __device__ static size_t mat_p(uint32_t kmax) {
         return ST >= ST_REG_S ? round_up((size_t)kmax * NB_P * NP * NP * sizeof(T), 32) : 0;
     }
-    static constexpr size_t kSlots = 2 * 2 * kMaxSlots * sizeof(A);
-    __host__ __device__ static size_t bytes(uint32_t kmax) {
-        return 2 * vec(kmax) + 2 * halo() + kSlots + 32 + mat_s(kmax) + mat_p(kmax);
+    __host__ __device__ static size_t slots(uint32_t C) {
+        return round_up(2 * kMaxValues * slot_stride(C) * sizeof(A), 32);
+    }
+    __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C) {
+        return 2 * vec(kmax) + 2 * halo() + slots(C) + 32 + mat_s(kmax) + mat_p(kmax);
     }
 };
 
@@ -200,14 +203,16 @@ __device__ __forceinline__ A warp_sum(A v) {
 // the same bits; a warp's slot depends only on its index (rows map to threads
 // from thread 0), so the result does not depend on the CTA size either.
 // `buf` alternates between call sites so that a slot array is rewritten only
-// after a barrier that every reader has passed.
+// after a barrier that every reader has passed.  Slots: [buf][q][C*32].
 template <typename A, int NQ>
 __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
                                                   const cg::cluster_group &cluster, uint32_t C,
                                                   uint32_t rank) {
+    static_assert(NQ <= kMaxValues, "slot array holds kMaxValues values");
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nwarps = blockDim.x >> 5;
-    A *sl = slots + (size_t)buf * kMaxSlots * 2;
+    const uint32_t kMaxSlots = (uint32_t)slot_stride(C);
+    A *sl = slots + (size_t)buf * kMaxSlots * kMaxValues;
 #pragma unroll
     for (int q = 0; q < NQ; ++q) v[q] = warp_sum(v[q]);
     const uint32_t my = rank * 32 + warp;
@@ -262,7 +267,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     T *vr = reinterpret_cast<T *>(sp); sp += Plan::vec(lp.kmax);
     T *uh = reinterpret_cast<T *>(sp); sp += Plan::halo();
     T *zh = reinterpret_cast<T *>(sp); sp += Plan::halo();
-    A *slots = reinterpret_cast<A *>(sp); sp += Plan::kSlots;
+    A *slots = reinterpret_cast<A *>(sp); sp += Plan::slots(C);
     uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp);
@@ -597,6 +602,351 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                     }
                 }
             }
+        }
+    }
+}
+
+}  // namespace gbdpcg
+
+namespace gbdpcg {
+
+// Shared-memory plan of the single-reduction kernel: the standard plan plus
+// the Phi^-1 blocks of the two halo knots and a second w-halo buffer.
+template <typename T, typename A, int NP, int ST>
+struct SmemPlanSR {
+    using Base = SmemPlan<T, A, NP, false, ST>;
+    __host__ __device__ static size_t mhalo() { return round_up((size_t)2 * NP * NP * sizeof(T), 32); }
+    __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C) {
+        return Base::bytes(kmax, C) + mhalo() + 2 * Base::halo();
+    }
+};
+
+// Single-reduction (Chronopoulos-Gear) PCG with a block-diagonal Phi^-1: the
+// vectors s = S p and u = Phi^-1 r are carried by recurrences so that
+// gamma = r.u, delta = (S u).u (and r.r) are reduced together: one cluster
+// barrier per iteration instead of two.
+//   r0 = gamma - S x0, u0 = M r0, w0 = S u0, g0 = r0.u0, d0 = w0.u0,
+//   alpha0 = g0/d0, beta0 = 0; per pass
+//   p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = M r;
+//   w = S u; g' = r.u; d' = w.u; beta = g'/g; alpha = g'/(d' - beta g'/alpha).
+// Halos: a CTA needs u of its two halo knots for w = S u.  It receives the
+// neighbours' boundary w with the reduction and repeats, on its copies, the
+// owner's s_h = w_h + beta s_h, r_h -= alpha s_h and u_h = M_h r_h (the halo
+// knots' Phi^-1 blocks are loaded once per system), with the same operations
+// in the same order, so the halos equal the owner's values bit for bit.
+// Iterates differ from the two-reduction kernel at roundoff level; the exit
+// test (|g'| < tol, or ||r|| <= tol ||gamma||) and the pass count are the
+// standard iteration's.
+template <typename T, typename A, int NP, int ST, int RPT>
+__global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_threads), 1)
+    pcg_sr_kernel(const LaunchParams lp) {
+    using Plan = SmemPlan<T, A, NP, false, ST>;
+    using PlanSR = SmemPlanSR<T, A, NP, ST>;
+    constexpr bool S_REG = ST <= ST_REG_S, P_REG = ST == ST_REG;
+    const cg::cluster_group cluster = cg::this_cluster();
+    const uint32_t C = cluster.num_blocks();
+    const uint32_t rank = cluster.block_rank();
+    const uint32_t tid = threadIdx.x, nthr = blockDim.x;
+
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char *sp = smem_raw;
+    T *vu = reinterpret_cast<T *>(sp); sp += Plan::vec(lp.kmax);   // u window (own + halos)
+    T *vr = reinterpret_cast<T *>(sp); sp += Plan::vec(lp.kmax);   // r window (own + halos)
+    T *sh = reinterpret_cast<T *>(sp); sp += Plan::halo();          // s of the halo knots
+    T *wh0 = reinterpret_cast<T *>(sp); sp += Plan::halo();         // received w halos, buffer 0
+    A *slots = reinterpret_cast<A *>(sp); sp += Plan::slots(C);
+    uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
+    T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
+    T *mp = reinterpret_cast<T *>(sp); sp += Plan::mat_p(lp.kmax);
+    T *mh = reinterpret_cast<T *>(sp); sp += PlanSR::mhalo();       // Phi^-1 of the halo knots
+    T *wh1 = reinterpret_cast<T *>(sp);                              // received w halos, buffer 1
+    const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
+
+    const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
+    for (uint32_t pass = 0;; ++pass) {
+        uint32_t item;
+        if (lp.queue) {
+            if (rank == 0 && tid == 0) {
+                const uint32_t it = atomicAdd(lp.queue, 1u);
+                for (uint32_t c = 0; c < C; ++c) *cluster.map_shared_rank(s_item, c) = it;
+            }
+            group_sync(cluster, C);
+            item = *reinterpret_cast<volatile uint32_t *>(s_item);
+        } else {
+            item = cluster_id + pass * nclusters;
+            __syncthreads();
+        }
+        if (item >= lp.count) break;
+        const SysDesc d = lp.descs ? lp.descs[lp.order ? lp.order[item] : item] : lp.one;
+        const uint32_t n = d.n, N = d.N;
+        const uint32_t K = (N + C - 1) / C;
+        if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (size_t)K * n > (size_t)nthr * RPT ||
+            (RPT > 1 && (n % RPT) != 0) || (d.flags & (SYS_PINV_TRI | SYS_ADJOINT))) {
+            if (rank == 0 && tid == 0) {
+                SysResult res = {};
+                res.status = -1;
+                lp.results[d.result] = res;
+            }
+            group_sync(cluster, C);
+            continue;
+        }
+        const uint32_t kb = min(rank * K, N), ke = min(kb + K, N), nk = ke - kb;
+        const uint32_t row0 = tid * RPT;
+        const uint32_t lk = row0 / n, i = row0 - lk * n;
+        const bool act = lk < nk;
+        const uint32_t k = kb + lk;
+        const bool relres = (d.flags & SYS_EXIT_RELRES) != 0;
+        const T *__restrict__ S = static_cast<const T *>(d.S);
+        const T *__restrict__ P = static_cast<const T *>(d.P);
+        const T *__restrict__ gamma = static_cast<const T *>(d.gamma);
+        const T *__restrict__ lam0 =
+            (d.flags & SYS_LAMBDA0_ZERO) ? nullptr : static_cast<const T *>(d.lambda0);
+        const uint32_t blkS = 3 * n * n, blkP = n * n;
+        const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
+        const bool first_knot = act && lk == 0 && kb > 0, last_knot = act && lk + 1 == nk && ke < N;
+
+        for (uint32_t e = tid; e < zero_elems; e += nthr) vu[e] = T(0);
+        // Phi^-1 blocks of the halo knots (column-major n x n)
+        for (uint32_t e = tid; e < 2 * n * n; e += nthr) {
+            const uint32_t side = e / (n * n), w = e - side * n * n;
+            if (side == 0 && has_left) mh[w] = __ldg(P + (size_t)(kb - 1) * blkP + w);
+            if (side == 1 && has_right) mh[NP * NP + w] = __ldg(P + (size_t)ke * blkP + w);
+        }
+
+        T Sr[S_REG ? RPT : 1][S_REG ? 3 * NP : 1];
+        T Pr[P_REG ? RPT : 1][P_REG ? NP : 1];
+        if constexpr (S_REG) {
+            const T *Sk = S + (size_t)k * blkS;
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                const bool present = act && (b != 0 || k > 0) && (b != 2 || k + 1 < N);
+#pragma unroll
+                for (int j = 0; j < NP; ++j)
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q)
+                        Sr[q][b * NP + j] = (present && (uint32_t)j < n)
+                                                ? __ldg(Sk + (b * n + j) * n + i + q)
+                                                : T(0);
+            }
+        } else {
+            const T *Sg = S + (size_t)kb * blkS;
+            for (uint32_t e = tid; e < nk * blkS; e += nthr) ms[e] = __ldg(Sg + e);
+        }
+        if constexpr (P_REG) {
+            const T *Pk = P + (size_t)k * blkP;
+#pragma unroll
+            for (int j = 0; j < NP; ++j)
+#pragma unroll
+                for (int q = 0; q < RPT; ++q)
+                    Pr[q][j] = (act && (uint32_t)j < n) ? __ldg(Pk + j * n + i + q) : T(0);
+        } else {
+            const T *Pg = P + (size_t)kb * blkP;
+            for (uint32_t e = tid; e < nk * blkP; e += nthr) mp[e] = __ldg(Pg + e);
+        }
+        const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
+        auto matS = [&](const T *x, T(&y)[RPT]) {
+            if constexpr (S_REG) reg_matvec<T, NP, 3, RPT>(Sr, x, y);
+            else smem_matvec<T, NP, 3, RPT>(ms + lk * blkS, sb0, sb1, x, n, i, y);
+        };
+        auto matP = [&](const T *x, T(&y)[RPT]) {
+            if constexpr (P_REG) reg_matvec<T, NP, 1, RPT>(Pr, x + NP, y);
+            else smem_matvec<T, NP, 1, RPT>(mp + lk * blkP, 0, 1, x + NP, n, i, y);
+        };
+        // u of halo row t (0..n-1 left knot, n..2n-1 right knot) from the r halo,
+        // in the order of the owner's Phi^-1 matvec (j ascending from 0)
+        auto halo_u = [&](uint32_t t) {
+            const uint32_t side = t < n ? 0 : 1, row = t - side * n;
+            const T *M = mh + side * NP * NP + row;
+            const T *rw = vr + (side ? (nk + 1) * NP : 0);
+            T acc = T(0);
+            for (uint32_t j = 0; j < n; ++j) acc = fma_rn(M[j * n], rw[j], acc);
+            return acc;
+        };
+        T *my_u = vu + (lk + 1) * NP + i;
+        T *my_r = vr + (lk + 1) * NP + i;
+        __syncthreads();
+
+        // ---- r0 = gamma - S x0 (the u window holds x0 for this product)
+        T gam[RPT], lam[RPT], r[RPT], u[RPT], w[RPT], p[RPT], s[RPT];
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            gam[q] = act ? gamma[(size_t)k * n + i + q] : T(0);
+            lam[q] = (act && lam0) ? lam0[(size_t)k * n + i + q] : T(0);
+            if (act) my_u[q] = lam[q];
+            p[q] = T(0);
+            s[q] = T(0);
+        }
+        if (lam0) {
+            for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                if (t < n && has_left) vu[t] = lam0[(size_t)(kb - 1) * n + t];
+                if (t >= n && has_right) vu[(nk + 1) * NP + (t - n)] = lam0[(size_t)ke * n + (t - n)];
+            }
+        }
+        __syncthreads();
+        if (act) matS(vu + lk * NP, w);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) r[q] = act ? gam[q] - w[q] : T(0);
+        group_sync(cluster, C);  // windows read before any neighbour writes into them
+        if (act) {
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) my_r[q] = r[q];
+        }
+        if (first_knot) {
+            T *dst = cluster.map_shared_rank(vr, rank - 1) + (K + 1) * NP + i;
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) dst[q] = r[q];
+        }
+        if (last_knot) {
+            T *dst = cluster.map_shared_rank(vr, rank + 1) + i;
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) dst[q] = r[q];
+        }
+        group_sync(cluster, C);
+        // ---- u0 = M r0 (own rows and halo rows), w0 = S u0
+        if (act) matP(vr + lk * NP, u);
+        else {
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) u[q] = T(0);
+        }
+        for (uint32_t t = tid; t < 2 * n; t += nthr) {
+            if (t < n && has_left) vu[t] = halo_u(t);
+            if (t >= n && has_right) vu[(nk + 1) * NP + (t - n)] = halo_u(t);
+        }
+        if (act) {
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) my_u[q] = u[q];
+        }
+        __syncthreads();
+        if (act) matS(vu + lk * NP, w);
+        else {
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) w[q] = T(0);
+        }
+        if (first_knot) {
+            T *dst = cluster.map_shared_rank(wh0, rank - 1) + NP + i;
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) dst[q] = w[q];
+        }
+        if (last_knot) {
+            T *dst = cluster.map_shared_rank(wh0, rank + 1) + i;
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) dst[q] = w[q];
+        }
+        A g, dlt, gg;
+        {
+            A v3[3] = {A(0), A(0), A(0)};
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) {
+                v3[0] += A(r[q]) * A(u[q]);
+                v3[1] += A(w[q]) * A(u[q]);
+                v3[2] += A(gam[q]) * A(gam[q]);
+            }
+            cluster_allreduce<A, 3>(v3, slots, 0, cluster, C, rank);
+            g = v3[0];
+            dlt = v3[1];
+            gg = v3[2];
+        }
+        const A thr = A(d.tol * d.tol * (double)gg);
+        const A tol = A(d.tol);
+        T alpha = (dlt == A(0)) ? T(0) : T(g / dlt);
+        T beta = T(0);
+
+        uint32_t iter = 0;
+        int32_t status = ST_MAX_ITER;
+        A g_new = A(0), rr = A(0);
+        const uint32_t max_iter = d.max_iter;
+        for (; iter < max_iter;) {
+            const T *wh = (iter & 1) ? wh1 : wh0;   // w halos received with the last reduction
+            T *wh_next = (iter & 1) ? wh0 : wh1;
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) {
+                p[q] = fma_rn(beta, p[q], u[q]);
+                s[q] = fma_rn(beta, s[q], w[q]);
+                lam[q] = fma_rn(alpha, p[q], lam[q]);
+                r[q] = fma_rn(-alpha, s[q], r[q]);
+                if (act) my_r[q] = r[q];
+            }
+            for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                if (t < n && has_left) {
+                    sh[t] = fma_rn(beta, sh[t], wh[t]);
+                    vr[t] = fma_rn(-alpha, sh[t], vr[t]);
+                }
+                if (t >= n && has_right) {
+                    const uint32_t j = t - n;
+                    sh[NP + j] = fma_rn(beta, sh[NP + j], wh[NP + j]);
+                    T *h = vr + (nk + 1) * NP + j;
+                    *h = fma_rn(-alpha, sh[NP + j], *h);
+                }
+            }
+            __syncthreads();
+            if (act) matP(vr + lk * NP, u);
+            else {
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) u[q] = T(0);
+            }
+            for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                if (t < n && has_left) vu[t] = halo_u(t);
+                if (t >= n && has_right) vu[(nk + 1) * NP + (t - n)] = halo_u(t);
+            }
+            if (act) {
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) my_u[q] = u[q];
+            }
+            __syncthreads();
+            if (act) matS(vu + lk * NP, w);
+            else {
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) w[q] = T(0);
+            }
+            if (first_knot) {
+                T *dst = cluster.map_shared_rank(wh_next, rank - 1) + NP + i;
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) dst[q] = w[q];
+            }
+            if (last_knot) {
+                T *dst = cluster.map_shared_rank(wh_next, rank + 1) + i;
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) dst[q] = w[q];
+            }
+            A dn;
+            {
+                A v3[3] = {A(0), A(0), A(0)};
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) {
+                    v3[0] += A(r[q]) * A(u[q]);
+                    v3[1] += A(w[q]) * A(u[q]);
+                    if (relres) v3[2] += A(r[q]) * A(r[q]);
+                }
+                cluster_allreduce<A, 3>(v3, slots, (iter + 1) & 1, cluster, C, rank);
+                g_new = v3[0];
+                dn = v3[1];
+                rr = v3[2];
+            }
+            ++iter;
+            if (!isfinite(g_new) || !isfinite(dn)) { status = ST_BREAKDOWN; break; }
+            if (relres ? (rr <= thr) : (fabs(g_new) < tol)) { status = ST_CONVERGED; break; }
+            const A b = g_new / g;
+            const A den = dn - b * g_new / A(alpha);
+            beta = T(b);
+            alpha = (den == A(0)) ? T(0) : T(g_new / den);
+            g = g_new;
+        }
+
+        T *lam_out = static_cast<T *>(d.lambda);
+        if (act) {
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) lam_out[(size_t)k * n + i + q] = lam[q];
+        }
+        if (rank == 0 && tid == 0) {
+            SysResult res;
+            res.iters = iter;
+            res.status = status;
+            res.eta = (double)g_new;
+            res.rr = relres ? (double)rr : -1.0;
+            res.gg = (double)gg;
+            res.outer = 0;
+            res.pad = 0;
+            lp.results[d.result] = res;
         }
     }
 }

@@ -8,8 +8,10 @@ int variants_np8(KernelVariant *out) {
     GBDPCG_VARIANTS_F32_RPT2(8)
     GBDPCG_VARIANTS_F64_SMEM(8)
     out[c++] = GBDPCG_VARIANT(double, double, 8, false, ST_REG, 1);
+    out[c++] = GBDPCG_VARIANT_SR(double, double, 8, ST_REG, 1);
     out[c++] = GBDPCG_VARIANT(double, double, 8, true, ST_REG, 1);
     out[c++] = GBDPCG_VARIANT(double, double, 8, false, ST_REG_S, 1);
+    out[c++] = GBDPCG_VARIANT_SR(double, double, 8, ST_REG_S, 1);
     return c;
 }
 }  // namespace gbdpcg

@@ -6,9 +6,15 @@
 
 #define GBDPCG_VARIANT(T, A, NP, PTRI, ST, RPT)                                               \
     ::gbdpcg::KernelVariant {                                                                 \
-        sizeof(T) == 8, sizeof(A) == 8, NP, PTRI, ST, RPT,                                    \
+        sizeof(T) == 8, sizeof(A) == 8, NP, PTRI, ST, RPT, 0,                                 \
             (const void *)&::gbdpcg::pcg_cluster_kernel<T, A, NP, PTRI, ST, RPT>,             \
             &::gbdpcg::SmemPlan<T, A, NP, PTRI, ST>::bytes                                    \
+    }
+#define GBDPCG_VARIANT_SR(T, A, NP, ST, RPT)                                                  \
+    ::gbdpcg::KernelVariant {                                                                 \
+        sizeof(T) == 8, sizeof(A) == 8, NP, false, ST, RPT, 1,                                \
+            (const void *)&::gbdpcg::pcg_sr_kernel<T, A, NP, ST, RPT>,                        \
+            &::gbdpcg::SmemPlanSR<T, A, NP, ST>::bytes                                        \
     }
 
 // FP32: rows in registers (RPT 1; RPT 2 for even bounds), S in registers with
@@ -21,11 +27,17 @@
     out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_SMEM, 1);                           \
     out[c++] = GBDPCG_VARIANT(float, float, NP, true, ST_SMEM, 1);                            \
     out[c++] = GBDPCG_VARIANT(float, double, NP, false, ST_REG, 1);                           \
-    out[c++] = GBDPCG_VARIANT(float, double, NP, true, ST_REG, 1);
+    out[c++] = GBDPCG_VARIANT(float, double, NP, true, ST_REG, 1);                            \
+    out[c++] = GBDPCG_VARIANT_SR(float, float, NP, ST_REG, 1);                                \
+    out[c++] = GBDPCG_VARIANT_SR(float, float, NP, ST_REG_S, 1);                              \
+    out[c++] = GBDPCG_VARIANT_SR(float, float, NP, ST_SMEM, 1);                               \
+    out[c++] = GBDPCG_VARIANT_SR(float, double, NP, ST_REG, 1);
 #define GBDPCG_VARIANTS_F32_RPT2(NP)                                                          \
     out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_REG, 2);                            \
-    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_REG_S, 2);
+    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_REG_S, 2);                          \
+    out[c++] = GBDPCG_VARIANT_SR(float, float, NP, ST_REG_S, 2);
 // FP64: rows in shared memory, and in registers where they fit.
 #define GBDPCG_VARIANTS_F64_SMEM(NP)                                                          \
     out[c++] = GBDPCG_VARIANT(double, double, NP, false, ST_SMEM, 1);                         \
-    out[c++] = GBDPCG_VARIANT(double, double, NP, true, ST_SMEM, 1);
+    out[c++] = GBDPCG_VARIANT(double, double, NP, true, ST_SMEM, 1);                          \
+    out[c++] = GBDPCG_VARIANT_SR(double, double, NP, ST_SMEM, 1);

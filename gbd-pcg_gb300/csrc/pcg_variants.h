@@ -13,11 +13,13 @@ struct KernelVariant {
     int st;      // storage: 0 S and Phi^-1 in registers, 1 S in registers and Phi^-1 in
                  // shared memory, 2 both in shared memory
     int rpt;     // matrix rows per thread (2 needs an even n)
+    int alg;     // 0 two reductions per iteration, 1 single reduction (block-diagonal Phi^-1)
     const void *func;
-    size_t (*smem_bytes)(uint32_t kmax);
+    size_t (*smem_bytes)(uint32_t kmax, uint32_t C);
 };
 
-// Each returns the number of variants written to `out` (at most 24).
+// Each returns the number of variants written to `out` (at most kMaxVariantsPerNP).
+constexpr int kMaxVariantsPerNP = 32;
 int variants_np6(KernelVariant *out);
 int variants_np8(KernelVariant *out);
 int variants_np12(KernelVariant *out);

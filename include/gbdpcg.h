@@ -68,7 +68,10 @@ enum { GBDPCG_PINV_CBTD = 0, GBDPCG_PINV_BLOCKDIAG = 1 };
 enum {
     GBDPCG_ALGO_AUTO = 0,    /* cluster solver when n <= 32, else plain */
     GBDPCG_ALGO_CLUSTER = 1, /* one thread-block cluster per system, DSMEM halos */
-    GBDPCG_ALGO_PLAIN = 2    /* one CTA per knot, grid-wide barriers (the reference's scheme) */
+    GBDPCG_ALGO_PLAIN = 2,   /* one CTA per knot, grid-wide barriers (the reference's scheme) */
+    GBDPCG_ALGO_SINGLE_REDUCTION = 3 /* cluster solver, Chronopoulos-Gear recurrences: one
+                                        cluster-wide reduction per iteration; block-diagonal
+                                        Phi^-1 only; iterates differ at roundoff level */
 };
 /* dot-product accumulation for float systems */
 enum { GBDPCG_DOT_NATIVE = 0, GBDPCG_DOT_FP64 = 1 };

@@ -175,7 +175,7 @@ def lib():
         L.oracle_ref_pcg_f32.restype = u32
         L.oracle_ref_pcg_f64.argtypes = [P, P, P, P, u32, u32, u32, f64, ip]
         L.oracle_ref_pcg_f64.restype = u32
-        for nm in ("oracle_pcg_f32", "oracle_pcg_f64"):
+        for nm in ("oracle_pcg_f32", "oracle_pcg_f64", "oracle_pcg_cg1_f32", "oracle_pcg_cg1_f64"):
             getattr(L, nm).argtypes = [P, P, P, P, u32, u32, u32, f64, u32, ip, ip, ip]
             getattr(L, nm).restype = ctypes.c_int
         for nm in ("oracle_matvec_f32", "oracle_matvec_f64"):
@@ -214,6 +214,19 @@ def pcg(S, Pinv, gamma, lambda0, n, N, max_iter=200, tol=1e-6, flags=0):
     lam = np.array(lambda0, dtype=dt, copy=True)
     it, eta, rr = ctypes.c_uint32(0), ctypes.c_double(0), ctypes.c_double(0)
     fn = lib().oracle_pcg_f64 if dt == np.float64 else lib().oracle_pcg_f32
+    st = fn(_ptr(S), _ptr(Pinv), _ptr(gamma), _ptr(lam), n, N, max_iter, tol, flags,
+            ctypes.byref(it), ctypes.byref(eta), ctypes.byref(rr))
+    return lam, int(it.value), int(st), float(eta.value), float(rr.value)
+
+
+def pcg_single_reduction(S, Pinv, gamma, lambda0, n, N, max_iter=200, tol=1e-6, flags=0):
+    """Single-reduction (Chronopoulos-Gear) PCG with compact block-diagonal Phi^-1.
+    Returns (lambda, iters, status, eta, rr)."""
+    dt = _dt(S)
+    S, Pinv, gamma = (np.ascontiguousarray(a, dtype=dt) for a in (S, Pinv, gamma))
+    lam = np.array(lambda0, dtype=dt, copy=True)
+    it, eta, rr = ctypes.c_uint32(0), ctypes.c_double(0), ctypes.c_double(0)
+    fn = lib().oracle_pcg_cg1_f64 if dt == np.float64 else lib().oracle_pcg_cg1_f32
     st = fn(_ptr(S), _ptr(Pinv), _ptr(gamma), _ptr(lam), n, N, max_iter, tol, flags,
             ctypes.byref(it), ctypes.byref(eta), ctypes.byref(rr))
     return lam, int(it.value), int(st), float(eta.value), float(rr.value)

@@ -272,3 +272,71 @@ int oracle_pcg_batch(oracle_system *sys, uint32_t count, int is_f64, uint32_t fl
     free(th);
     return started;
 }
+
+/* ------------- single-reduction (Chronopoulos-Gear) PCG, block-diagonal Phi^-1 -------------
+ * The product's opt-in single-reduction variant: s = S p and u = Phi^-1 r are
+ * carried by recurrences so that gamma = r.u, delta = (S u).u (and r.r) are
+ * reduced together, once per iteration:
+ *   r0 = gamma - S x0, u0 = M r0, w0 = S u0, g0 = r0.u0, d0 = w0.u0,
+ *   alpha0 = g0/d0, beta0 = 0, p_-1 = s_-1 = 0; then per pass
+ *   p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = M r;
+ *   w = S u; g' = r.u; d' = w.u; beta = g'/g; alpha = g'/(d' - beta g'/alpha).
+ * The exit test and the pass count follow the standard iteration's. */
+#define DEFINE_CG1(T, SUF, FMA)                                                            \
+    int oracle_pcg_cg1_##SUF(const T *S, const T *Pinv, const T *gamma, T *lam, uint32_t n, \
+                             uint32_t N, uint32_t max_iter, double tol, uint32_t flags,     \
+                             uint32_t *iters_out, double *eta_out, double *rr_out) {        \
+        const size_t nN = (size_t)n * N;                                                   \
+        const int rel = (flags & ORACLE_EXIT_RELRES) != 0;                                 \
+        const int acc64 = (flags & ORACLE_ACC64) != 0;                                     \
+        T *r = (T *)malloc(nN * sizeof(T)), *u = (T *)malloc(nN * sizeof(T));              \
+        T *w = (T *)malloc(nN * sizeof(T)), *p = (T *)calloc(nN, sizeof(T));               \
+        T *s = (T *)calloc(nN, sizeof(T));                                                 \
+        int status = ORACLE_MAX_ITER;                                                      \
+        uint32_t iter;                                                                     \
+        double g, d, gn = 0, dn, rr = 0;                                                   \
+        const double gg = dot_##SUF(gamma, gamma, nN, 1);                                  \
+        const double thr = tol * tol * gg;                                                 \
+        matvec_##SUF(r, S, lam, n, N, 0);                                                  \
+        for (size_t i = 0; i < nN; ++i) r[i] = gamma[i] - r[i];                            \
+        matvec_##SUF(u, Pinv, r, n, N, 1);                                                 \
+        matvec_##SUF(w, S, u, n, N, 0);                                                    \
+        g = dot_##SUF(r, u, nN, acc64);                                                    \
+        d = dot_##SUF(w, u, nN, acc64);                                                    \
+        T alpha = (d == 0.0) ? (T)0 : (T)(acc64 ? g / d : (double)((T)g / (T)d));          \
+        T beta = (T)0;                                                                     \
+        for (iter = 0; iter < max_iter; ++iter) {                                          \
+            for (size_t i = 0; i < nN; ++i) {                                              \
+                p[i] = FMA(beta, p[i], u[i]);                                              \
+                s[i] = FMA(beta, s[i], w[i]);                                              \
+                lam[i] = FMA(alpha, p[i], lam[i]);                                         \
+                r[i] = FMA(-alpha, s[i], r[i]);                                            \
+            }                                                                              \
+            matvec_##SUF(u, Pinv, r, n, N, 1);                                             \
+            matvec_##SUF(w, S, u, n, N, 0);                                                \
+            gn = dot_##SUF(r, u, nN, acc64);                                               \
+            dn = dot_##SUF(w, u, nN, acc64);                                               \
+            if (rel) rr = dot_##SUF(r, r, nN, acc64);                                      \
+            if (!isfinite(gn) || !isfinite(dn)) { ++iter; status = ORACLE_BREAKDOWN; break; } \
+            if (rel ? (rr <= thr) : (fabs(gn) < tol)) { ++iter; status = ORACLE_CONVERGED; break; } \
+            if (acc64) {                                                                   \
+                const double b = gn / g;                                                   \
+                const double den = dn - b * gn / (double)alpha;                            \
+                beta = (T)b;                                                               \
+                alpha = (den == 0.0) ? (T)0 : (T)(gn / den);                               \
+            } else {                                                                       \
+                const T b = (T)gn / (T)g;                                                  \
+                const T den = (T)dn - b * (T)gn / alpha;                                   \
+                beta = b;                                                                  \
+                alpha = (den == (T)0) ? (T)0 : (T)gn / den;                                \
+            }                                                                              \
+            g = gn;                                                                        \
+        }                                                                                  \
+        if (iters_out) *iters_out = iter;                                                  \
+        if (eta_out) *eta_out = gn;                                                        \
+        if (rr_out) *rr_out = rel ? rr : dot_##SUF(r, r, nN, 1);                           \
+        free(r); free(u); free(w); free(p); free(s);                                       \
+        return status;                                                                     \
+    }
+DEFINE_CG1(float, f32, fmaf)
+DEFINE_CG1(double, f64, fma)

@@ -30,6 +30,12 @@ int oracle_pcg_f32(const float *S, const float *Pinv, const float *gamma, float 
 int oracle_pcg_f64(const double *S, const double *Pinv, const double *gamma, double *lambda,
                    uint32_t n, uint32_t N, uint32_t max_iter, double tol, uint32_t flags,
                    uint32_t *iters, double *eta, double *rr);
+int oracle_pcg_cg1_f32(const float *S, const float *Pinv, const float *gamma, float *lambda,
+                       uint32_t n, uint32_t N, uint32_t max_iter, double tol, uint32_t flags,
+                       uint32_t *iters, double *eta, double *rr);
+int oracle_pcg_cg1_f64(const double *S, const double *Pinv, const double *gamma, double *lambda,
+                       uint32_t n, uint32_t N, uint32_t max_iter, double tol, uint32_t flags,
+                       uint32_t *iters, double *eta, double *rr);
 void oracle_matvec_f32(double *y, const float *S, const float *x, uint32_t n, uint32_t N);
 void oracle_matvec_f64(double *y, const double *S, const double *x, uint32_t n, uint32_t N);
 int oracle_pcg_batch(oracle_system *sys, uint32_t count, int is_f64, uint32_t flags,

@@ -246,3 +246,58 @@ def test_every_storage_variant(gb, oracle_mod, handle, dts, storage, n, N):
     assert r.status == gb.CONVERGED and abs(int(r.iters) - it_o) <= 1, (r, it_o)
     x = O.block_cholesky_solve(S.astype(np.float64), n, N, g.astype(np.float64))
     assert relerr(lam.cpu().numpy(), x) <= 1.5 * relerr(lam_o, x) + (1e-6 if dts == "f32" else 1e-13)
+
+
+@pytest.mark.parametrize("dts", ["f32", "f64"])
+@pytest.mark.parametrize("storage", ["auto", "registers", "shared", "split"])
+@pytest.mark.parametrize("n,N,C", [(14, 128, 0), (6, 64, 1), (24, 100, 0), (12, 40, 3), (7, 19, 2), (14, 1, 0)])
+def test_single_reduction_vs_oracle(gb, oracle_mod, handle, dts, storage, n, N, C):
+    """The opt-in single-reduction (Chronopoulos-Gear) kernel against its CPU
+    restatement: same passes +-1, as accurate against the FP64 solution."""
+    import torch
+    O = oracle_mod
+    dt = _dt(dts)
+    sy, S, P, g = system(O, n, N, 31, dt, "compact")
+    tol = 1e-6 if dts == "f32" else 1e-12
+    lam_o, it_o, st_o, _, _ = O.pcg_single_reduction(S, P, g, np.zeros(n * N, dt), n, N, 500, tol,
+                                                     flags=O.EXIT_RELRES)
+    d = torch.device("cuda:0")
+    lam = torch.zeros(n * N, dtype=torch.float64 if dts == "f64" else torch.float32, device=d)
+    st = {"auto": gb.STORAGE_AUTO, "registers": gb.STORAGE_REGISTERS, "shared": gb.STORAGE_SHARED,
+          "split": gb.STORAGE_SPLIT}[storage]
+    try:
+        r = handle.solve(*(torch.from_numpy(a).to(d) for a in (S, P, g)), lam, n, N, gb.PINV_BLOCKDIAG,
+                         gb.config(max_iter=500, exit_tol=tol, exit_mode=gb.EXIT_RELRES, storage=st,
+                                   cluster_size=C, algorithm=gb.ALGO_SINGLE_REDUCTION))
+    except gb.GbdpcgError as e:
+        assert e.code == gb.ERR_UNSUPPORTED
+        pytest.skip(f"no {storage} shape at n={n} N={N} C={C}")
+    assert r.status == gb.CONVERGED and abs(int(r.iters) - it_o) <= 1, (r, it_o)
+    x = O.block_cholesky_solve(S.astype(np.float64), n, N, g.astype(np.float64))
+    assert relerr(lam.cpu().numpy(), x) <= 1.5 * relerr(lam_o, x) + (1e-6 if dts == "f32" else 1e-13)
+
+
+def test_single_reduction_reference_exit(gb, oracle_mod, handle):
+    """With the reference's exit test |r.z| < tol the single-reduction kernel
+    takes the reference's pass count on the n=14 configurations."""
+    import torch
+    O = oracle_mod
+    d = torch.device("cuda:0")
+    for N in (32, 128):
+        sy, S, Pt, g = system(O, 14, N, 0, np.float32)
+        Pc = O.block_jacobi(sy.D, "compact").astype(np.float32)
+        lam_r, it_r, _ = O.ref_pcg(S, Pt, g, np.zeros(14 * N, np.float32), 14, N, 200, 1e-6)
+        lam = torch.zeros(14 * N, device=d)
+        r = handle.solve(*(torch.from_numpy(a).to(d) for a in (S, Pc, g)), lam, 14, N, gb.PINV_BLOCKDIAG,
+                         gb.config(max_iter=200, algorithm=gb.ALGO_SINGLE_REDUCTION))
+        assert r.iters == it_r
+        assert relerr(lam.cpu().numpy(), lam_r) < 2e-5
+
+
+def test_single_reduction_rejects_tridiagonal_pinv(gb, oracle_mod, handle):
+    O = oracle_mod
+    _, S, P, g = system(O, 6, 10, 0, np.float32)
+    lam = np.zeros(60, np.float32)
+    with pytest.raises(gb.GbdpcgError) as e:
+        gb.solve(S, P, g, lam, 6, 10, gb.config(algorithm=gb.ALGO_SINGLE_REDUCTION))
+    assert e.value.code == gb.ERR_UNSUPPORTED

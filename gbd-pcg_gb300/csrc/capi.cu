@@ -30,9 +30,9 @@
 #include "pcg_variants.h"
 
 namespace gbdpcg {
-cudaError_t launch_block_jacobi(bool f64, bool fp64_compute, const SysDesc *d_descs,
-                                const uint64_t *d_prefix, uint32_t nsys, uint64_t total_knots,
-                                int tri_layout, cudaStream_t stream);
+cudaError_t launch_block_jacobi(int kind, const SysDesc *d_descs, const uint64_t *d_prefix,
+                                uint32_t nsys, uint64_t total_knots, int tri_layout,
+                                cudaStream_t stream);
 }
 
 using namespace gbdpcg;
@@ -182,10 +182,14 @@ std::vector<Pref> storage_prefs(bool f64, bool ptri, uint32_t storage) {
 }
 
 int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layout,
-                 const gbdpcg_config &cfg, Shape *out) {
+                 const gbdpcg_config &cfg, Shape *out, bool refine = false) {
     Shape s;
     const int np = np_for(n);
-    const bool want_plain = cfg.algorithm == GBDPCG_ALGO_PLAIN || np == 0;
+    if (refine) {
+        if (np == 0 || layout != GBDPCG_PINV_BLOCKDIAG || cfg.algorithm == GBDPCG_ALGO_PLAIN)
+            return fail(GBDPCG_ERR_UNSUPPORTED, "refinement needs n <= 32 and a compact Phi^-1");
+    }
+    const bool want_plain = !refine && (cfg.algorithm == GBDPCG_ALGO_PLAIN || np == 0);
     if (want_plain) {
         if (layout != GBDPCG_PINV_CBTD)
             return fail(GBDPCG_ERR_UNSUPPORTED, "plain algorithm needs a cbtd Phi^-1");
@@ -194,13 +198,13 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
         return GBDPCG_SUCCESS;
     }
     const bool ptri = layout == GBDPCG_PINV_CBTD;
-    const bool acc64 = cfg.dot_precision == GBDPCG_DOT_FP64;
-    const int alg = cfg.algorithm == GBDPCG_ALGO_SINGLE_REDUCTION ? 1 : 0;
+    const bool acc64 = refine || cfg.dot_precision == GBDPCG_DOT_FP64;
+    const int alg = refine ? 2 : (cfg.algorithm == GBDPCG_ALGO_SINGLE_REDUCTION ? 1 : 0);
     if (alg == 1 && ptri)
         return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm needs a block-diagonal Phi^-1");
-    for (const Pref &pf : storage_prefs(f64, ptri, cfg.storage)) {
+    for (const Pref &pf : storage_prefs(f64 && !refine, ptri, cfg.storage)) {
         if (pf.rpt > 1 && (n % pf.rpt) != 0) continue;
-        VariantInfo *vi = find_variant(reg, f64, acc64, np, ptri, pf.st, pf.rpt, alg);
+        VariantInfo *vi = find_variant(reg, f64 && !refine, acc64, np, ptri, pf.st, pf.rpt, alg);
         if (!vi) continue;
         uint32_t cap = cfg.max_threads ? cfg.max_threads : (uint32_t)vi->max_threads;
         cap = std::min<uint32_t>(cap, (uint32_t)vi->max_threads);
@@ -268,6 +272,8 @@ void to_public(const SysResult &r, gbdpcg_result *o) {
     o->status = r.status;
     o->eta = r.eta;
     o->relres = (r.rr >= 0 && r.gg > 0) ? sqrt(r.rr / r.gg) : (r.rr >= 0 ? 0.0 : -1.0);
+    o->outer = r.outer;
+    o->reserved = 0;
 }
 
 SysDesc make_desc(const void *S, const void *P, const void *g, const void *l0, void *l,
@@ -281,7 +287,8 @@ SysDesc make_desc(const void *S, const void *P, const void *g, const void *l0, v
     d.lambda0 = l0;
     d.lambda = l;
     d.tol = cfg.exit_tol;
-    d.inner_tol = 0;
+    d.inner_tol = cfg.inner_tol;
+    d.max_outer = cfg.max_outer;
     d.n = n;
     d.N = N;
     d.max_iter = cfg.max_iter;
@@ -297,7 +304,8 @@ int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
     if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad pinv_layout");
     if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FP64 ||
         cfg->algorithm > GBDPCG_ALGO_SINGLE_REDUCTION || cfg->storage > GBDPCG_STORAGE_SPLIT ||
-        cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1)
+        cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1 ||
+        !(cfg->inner_tol >= 0) || cfg->inner_tol >= 1)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad config field");
     if (!(cfg->exit_tol >= 0)) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "exit_tol must be >= 0");
     return GBDPCG_SUCCESS;
@@ -376,13 +384,13 @@ int max_active_clusters(const Shape &sh, size_t smem, int *out) {
 
 // One system, device pointers; result left in h->d_last.
 int solve_one(gbdpcg_handle_s *h, bool f64, const SysDesc &d0, const gbdpcg_config &cfg,
-              uint32_t layout, cudaStream_t stream) {
+              uint32_t layout, cudaStream_t stream, bool refine = false) {
     SysResult *d_res = h->ws.as<SysResult>();
     int rc;
     SysDesc d = d0;
     d.result = 0;
     Shape sh;
-    rc = choose_shape(h->reg, f64, d.n, d.N, layout, cfg, &sh);
+    rc = choose_shape(h->reg, f64, d.n, d.N, layout, cfg, &sh, refine);
     if (rc) return rc;
     h->d_last = d_res;
     h->last_stream = stream;
@@ -415,6 +423,7 @@ struct PlanClass {
 struct gbdpcg_plan_s {
     gbdpcg_handle_s *h = nullptr;
     bool f64 = false;
+    bool refine = false;  // FP64 systems by FP32 PCG + FP64 refinement
     uint32_t layout = 0;
     gbdpcg_config cfg;
     uint32_t count = 0;
@@ -505,6 +514,8 @@ void gbdpcg_config_init(gbdpcg_config *cfg) {
     cfg->dot_precision = GBDPCG_DOT_NATIVE;
     cfg->algorithm = GBDPCG_ALGO_AUTO;
     cfg->use_graph = 1;
+    cfg->max_outer = 50;
+    cfg->inner_tol = 0.05;
 }
 
 int gbdpcg_create(gbdpcg_handle_t *handle, int device) {
@@ -572,7 +583,7 @@ int gbdpcg_last_result(gbdpcg_handle_t h, gbdpcg_result *result) {
     return GBDPCG_SUCCESS;
 }
 
-static int block_jacobi(gbdpcg_handle_t h, bool f64, const void *S, void *P, uint32_t layout,
+static int block_jacobi(gbdpcg_handle_t h, int kind, const void *S, void *P, uint32_t layout,
                         uint32_t n, uint32_t N, cudaStream_t stream) {
     if (!h || !S || !P) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
     if (n == 0 || N == 0 || n > 32) return fail(GBDPCG_ERR_UNSUPPORTED, "block-Jacobi needs 1 <= n <= 32");
@@ -590,7 +601,7 @@ static int block_jacobi(gbdpcg_handle_t h, bool f64, const void *S, void *P, uin
     GB_CUDA(cudaMemcpyAsync(base, &d, sizeof(d), cudaMemcpyHostToDevice, stream));
     GB_CUDA(cudaMemcpyAsync(base + sizeof(SysDesc), &prefix, sizeof(prefix),
                             cudaMemcpyHostToDevice, stream));
-    GB_CUDA(launch_block_jacobi(f64, false, reinterpret_cast<SysDesc *>(base),
+    GB_CUDA(launch_block_jacobi(kind, reinterpret_cast<SysDesc *>(base),
                                 reinterpret_cast<uint64_t *>(base + sizeof(SysDesc)), 1, N,
                                 layout == GBDPCG_PINV_CBTD, stream));
     // the host-side sources above must outlive the copies
@@ -601,13 +612,40 @@ static int block_jacobi(gbdpcg_handle_t h, bool f64, const void *S, void *P, uin
 int gbdpcg_block_jacobi_f32(gbdpcg_handle_t h, const float *d_S, float *d_Pinv,
                             uint32_t pinv_layout, uint32_t n, uint32_t N,
                             gbdpcg_stream_t stream) {
-    return block_jacobi(h, false, d_S, d_Pinv, pinv_layout, n, N, (cudaStream_t)stream);
+    return block_jacobi(h, 0, d_S, d_Pinv, pinv_layout, n, N, (cudaStream_t)stream);
 }
 
 int gbdpcg_block_jacobi_f64(gbdpcg_handle_t h, const double *d_S, double *d_Pinv,
                             uint32_t pinv_layout, uint32_t n, uint32_t N,
                             gbdpcg_stream_t stream) {
-    return block_jacobi(h, true, d_S, d_Pinv, pinv_layout, n, N, (cudaStream_t)stream);
+    return block_jacobi(h, 1, d_S, d_Pinv, pinv_layout, n, N, (cudaStream_t)stream);
+}
+
+int gbdpcg_block_jacobi_f64to32(gbdpcg_handle_t h, const double *d_S, float *d_Pinv, uint32_t n,
+                                uint32_t N, gbdpcg_stream_t stream) {
+    return block_jacobi(h, 2, d_S, d_Pinv, GBDPCG_PINV_BLOCKDIAG, n, N, (cudaStream_t)stream);
+}
+
+int gbdpcg_refine_solve_dev(gbdpcg_handle_t h, const double *d_S, const float *d_Pinv,
+                            const double *d_gamma, double *d_lambda, uint32_t n, uint32_t N,
+                            const gbdpcg_config *cfg, gbdpcg_result *result,
+                            gbdpcg_stream_t stream) {
+    if (!h || !d_S || !d_Pinv || !d_gamma || !d_lambda)
+        return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (n == 0 || N == 0) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "n and N must be positive");
+    int rc = check_cfg(cfg, GBDPCG_PINV_BLOCKDIAG);
+    if (rc) return rc;
+    if (cfg->exit_mode != GBDPCG_EXIT_RELRES)
+        return fail(GBDPCG_ERR_UNSUPPORTED, "refinement exits on the relative residual");
+    HandleScope scope(h->device);
+    SysDesc d = make_desc(d_S, d_Pinv, d_gamma, d_lambda, d_lambda, n, N, *cfg,
+                          GBDPCG_PINV_BLOCKDIAG, 0);
+    d.flags |= SYS_REFINE;
+    rc = solve_one(h, false, d, *cfg, GBDPCG_PINV_BLOCKDIAG, (cudaStream_t)stream, true);
+    if (rc) return rc;
+    h->last_f64 = true;
+    if (result) return gbdpcg_last_result(h, result);
+    return GBDPCG_SUCCESS;
 }
 
 // ---- host-pointer solves (per-thread handle on the current device)
@@ -658,7 +696,7 @@ static int solve_host(bool f64, const void *S, const void *P, const void *g, voi
     GB_CUDA(cudaMemcpyAsync(dl, l, vec, cudaMemcpyHostToDevice, st));
     if (!P) {
         if (n > 32) return fail(GBDPCG_ERR_UNSUPPORTED, "block-Jacobi builder needs n <= 32");
-        rc = block_jacobi(h, f64, dS, dP, build_layout, n, N, st);
+        rc = block_jacobi(h, f64 ? 1 : 0, dS, dP, build_layout, n, N, st);
         if (rc) return rc;
     }
     rc = solve_dev(h, f64, dS, dP, build_layout, dg, dl, n, N, &c, nullptr, st);
@@ -711,13 +749,16 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
                        uint32_t pinv_layout, const gbdpcg_config *cfg, gbdpcg_plan_t *plan) {
     if (!h || !systems || !plan || count == 0)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer or empty batch");
-    if (dtype != 0 && dtype != 1) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "dtype must be 0 or 1");
+    if (dtype < 0 || dtype > 2) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "dtype must be 0, 1 or 2");
     int rc = check_cfg(cfg, pinv_layout);
     if (rc) return rc;
+    if (dtype == 2 && (pinv_layout != GBDPCG_PINV_BLOCKDIAG || cfg->exit_mode != GBDPCG_EXIT_RELRES))
+        return fail(GBDPCG_ERR_UNSUPPORTED, "refinement needs a compact Phi^-1 and the relative-residual exit");
     HandleScope scope(h->device);
     auto p = std::make_unique<gbdpcg_plan_s>();
     p->h = h;
     p->f64 = dtype == 1;
+    p->refine = dtype == 2;
     p->layout = pinv_layout;
     p->cfg = *cfg;
     p->count = count;
@@ -733,15 +774,17 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
         SysDesc d = make_desc(s.S, s.Pinv, s.gamma, s.lambda, s.lambda, s.n, s.N, *cfg,
                               pinv_layout, i);
         if (adjoint) {
+            if (p->refine) return fail(GBDPCG_ERR_UNSUPPORTED, "no adjoint of a refined solve");
             d.flags |= SYS_ADJOINT | SYS_LAMBDA0_ZERO;
             d.lam_fwd = s.lambda_fwd;
             d.dS = s.dS;
         }
+        if (p->refine) d.flags |= SYS_REFINE;
         prefix[i] = p->total_knots;
         p->total_knots += s.N;
         p->descs.push_back(d);
         Shape sh;
-        rc = choose_shape(h->reg, p->f64, s.n, s.N, pinv_layout, *cfg, &sh);
+        rc = choose_shape(h->reg, p->f64, s.n, s.N, pinv_layout, *cfg, &sh, p->refine);
         if (rc) return rc;
         if (sh.plain) {
             if (adjoint) return fail(GBDPCG_ERR_UNSUPPORTED, "adjoint needs n <= 32");
@@ -845,7 +888,8 @@ int gbdpcg_plan_create_packed(gbdpcg_handle_t h, int dtype, const gbdpcg_packed_
     if (!systems || !d_S || !d_Pinv || !d_gamma || !d_lambda || !plan || count == 0)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer or empty batch");
     if (dtype != 0 && dtype != 1) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "dtype must be 0 or 1");
-    const size_t s = dtype ? 8 : 4;
+    const size_t s = dtype ? 8 : 4;  // refinement: S, gamma, lambda double, Pinv float
+    const size_t sP = dtype == 1 ? 8 : 4;
     std::vector<gbdpcg_system> sys(count);
     size_t eS = 0, eP = 0, eV = 0;
     for (uint32_t i = 0; i < count; ++i) {
@@ -853,7 +897,7 @@ int gbdpcg_plan_create_packed(gbdpcg_handle_t h, int dtype, const gbdpcg_packed_
         const size_t n = q.n, N = q.N;
         const size_t pm = pinv_layout == GBDPCG_PINV_CBTD ? 3 * n * n * N : n * n * N;
         sys[i].S = static_cast<const char *>(d_S) + q.S_off * s;
-        sys[i].Pinv = static_cast<const char *>(d_Pinv) + q.Pinv_off * s;
+        sys[i].Pinv = static_cast<const char *>(d_Pinv) + q.Pinv_off * sP;
         sys[i].gamma = static_cast<const char *>(d_gamma) + q.vec_off * s;
         sys[i].lambda = static_cast<char *>(d_lambda) + q.vec_off * s;
         sys[i].lambda_fwd = nullptr;
@@ -873,7 +917,7 @@ int gbdpcg_plan_create_packed(gbdpcg_handle_t h, int dtype, const gbdpcg_packed_
     p->arena_g = d_gamma;
     p->arena_l = d_lambda;
     p->bytes_S = eS * s;
-    p->bytes_P = eP * s;
+    p->bytes_P = eP * sP;
     p->bytes_vec = eV * s;
     return GBDPCG_SUCCESS;
 }
@@ -906,7 +950,7 @@ int gbdpcg_plan_build_block_jacobi(gbdpcg_plan_t p, gbdpcg_stream_t stream) {
     for (auto &d : p->descs)
         if (d.n > 32) return fail(GBDPCG_ERR_UNSUPPORTED, "block-Jacobi builder needs n <= 32");
     HandleScope scope(p->h->device);
-    GB_CUDA(launch_block_jacobi(p->f64, false, p->d_descs.as<SysDesc>(), p->d_prefix.as<uint64_t>(),
+    GB_CUDA(launch_block_jacobi(p->refine ? 2 : (p->f64 ? 1 : 0), p->d_descs.as<SysDesc>(), p->d_prefix.as<uint64_t>(),
                                 p->count, p->total_knots, p->layout == GBDPCG_PINV_CBTD,
                                 (cudaStream_t)stream));
     return GBDPCG_SUCCESS;

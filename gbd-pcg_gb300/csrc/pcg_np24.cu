@@ -9,6 +9,8 @@ int variants_np24(KernelVariant *out) {
     GBDPCG_VARIANTS_F64_SMEM(24)
     out[c++] = GBDPCG_VARIANT(double, double, 24, false, ST_REG_S, 1);
     out[c++] = GBDPCG_VARIANT_SR(double, double, 24, ST_REG_S, 1);
+    GBDPCG_VARIANTS_RF(24)
+    GBDPCG_VARIANTS_RF_RPT2(24)
     return c;
 }
 }  // namespace gbdpcg

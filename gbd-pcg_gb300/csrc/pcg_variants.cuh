@@ -2,6 +2,7 @@
 // per block-size bound, so that they compile in parallel).
 #pragma once
 #include "pcg_cluster.cuh"
+#include "pcg_refine.cuh"
 #include "pcg_variants.h"
 
 #define GBDPCG_VARIANT(T, A, NP, PTRI, ST, RPT)                                               \
@@ -16,6 +17,18 @@
             (const void *)&::gbdpcg::pcg_sr_kernel<T, A, NP, ST, RPT>,                        \
             &::gbdpcg::SmemPlanSR<T, A, NP, ST>::bytes                                        \
     }
+
+#define GBDPCG_VARIANT_RF(NP, ST, RPT)                                                        \
+    ::gbdpcg::KernelVariant {                                                                 \
+        0, 1, NP, false, ST, RPT, 2, (const void *)&::gbdpcg::pcg_refine_kernel<NP, ST, RPT>,   \
+            &::gbdpcg::SmemPlanRF<NP, ST>::bytes                                              \
+    }
+// FP32 inner solve with FP64 refinement
+#define GBDPCG_VARIANTS_RF(NP)                                                                \
+    out[c++] = GBDPCG_VARIANT_RF(NP, ST_REG, 1);                                              \
+    out[c++] = GBDPCG_VARIANT_RF(NP, ST_REG_S, 1);                                            \
+    out[c++] = GBDPCG_VARIANT_RF(NP, ST_SMEM, 1);
+#define GBDPCG_VARIANTS_RF_RPT2(NP) out[c++] = GBDPCG_VARIANT_RF(NP, ST_REG_S, 2);
 
 // FP32: rows in registers (RPT 1; RPT 2 for even bounds), S in registers with
 // Phi^-1 in shared memory, both in shared memory; FP64 dot accumulation with

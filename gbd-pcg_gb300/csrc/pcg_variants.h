@@ -13,7 +13,8 @@ struct KernelVariant {
     int st;      // storage: 0 S and Phi^-1 in registers, 1 S in registers and Phi^-1 in
                  // shared memory, 2 both in shared memory
     int rpt;     // matrix rows per thread (2 needs an even n)
-    int alg;     // 0 two reductions per iteration, 1 single reduction (block-diagonal Phi^-1)
+    int alg;     // 0 two reductions per iteration, 1 single reduction (block-diagonal Phi^-1),
+                 // 2 FP32 inner PCG with FP64 refinement
     const void *func;
     size_t (*smem_bytes)(uint32_t kmax, uint32_t C);
 };

@@ -8,7 +8,8 @@
 // column j of the inverse, and the result is symmetrised and written either as
 // a cbtd block row [0 | S_kk^-1 | 0] or compactly (n^2 per knot, column-major).
 // Work item = (system, knot) over a batch; the knot-prefix array maps a warp to
-// its system.
+// its system.  TI: element type of S, TO: of Phi^-1, CT: arithmetic (double
+// S with float Phi^-1 serves the FP32-inner refinement).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -19,7 +20,7 @@ namespace gbdpcg {
 constexpr int kPrecWarps = 2;  // knots per CTA
 constexpr int kPrecMaxN = 32;
 
-template <typename T, typename CT>
+template <typename TI, typename TO, typename CT>
 __global__ void __launch_bounds__(kPrecWarps * 32)
     block_jacobi_kernel(const SysDesc *__restrict__ descs, const uint64_t *__restrict__ knot_prefix,
                         uint32_t nsys, uint64_t total_knots, int tri_layout) {
@@ -40,7 +41,7 @@ __global__ void __launch_bounds__(kPrecWarps * 32)
     const uint32_t ld = kPrecMaxN + 1;  // padded row stride, conflict-free columns
     CT *L = sL[warp];
     CT *X = sX[warp];
-    const T *Sk = static_cast<const T *>(d.S) + (size_t)k * 3 * n * n + (size_t)n * n;
+    const TI *Sk = static_cast<const TI *>(d.S) + (size_t)k * 3 * n * n + (size_t)n * n;
     // L <- S_kk (row-major, lower triangle used); S_kk column-major: (r, c) at c*n + r
     for (uint32_t e = lane; e < n * n; e += 32) {
         const uint32_t c = e / n, r = e - c * n;
@@ -77,44 +78,39 @@ __global__ void __launch_bounds__(kPrecWarps * 32)
         }
     }
     __syncwarp();
-    T *out = static_cast<T *>(const_cast<void *>(d.P));
+    TO *out = static_cast<TO *>(const_cast<void *>(d.P));
     if (tri_layout) {
-        T *row = out + (size_t)k * 3 * n * n;
+        TO *row = out + (size_t)k * 3 * n * n;
         for (uint32_t e = lane; e < 3 * n * n; e += 32) {
             const uint32_t b = e / (n * n), w = e - b * n * n;
             const uint32_t c = w / n, r = w - c * n;
-            row[e] = (b == 1) ? T(CT(0.5) * (X[c * ld + r] + X[r * ld + c])) : T(0);
+            row[e] = (b == 1) ? TO(CT(0.5) * (X[c * ld + r] + X[r * ld + c])) : TO(0);
         }
     } else {
-        T *blk = out + (size_t)k * n * n;
+        TO *blk = out + (size_t)k * n * n;
         for (uint32_t e = lane; e < n * n; e += 32) {
             const uint32_t c = e / n, r = e - c * n;
-            blk[e] = T(CT(0.5) * (X[c * ld + r] + X[r * ld + c]));
+            blk[e] = TO(CT(0.5) * (X[c * ld + r] + X[r * ld + c]));
         }
     }
 }
 
-template __global__ void block_jacobi_kernel<float, float>(const SysDesc *, const uint64_t *,
-                                                           uint32_t, uint64_t, int);
-template __global__ void block_jacobi_kernel<float, double>(const SysDesc *, const uint64_t *,
-                                                            uint32_t, uint64_t, int);
-template __global__ void block_jacobi_kernel<double, double>(const SysDesc *, const uint64_t *,
-                                                             uint32_t, uint64_t, int);
-
-cudaError_t launch_block_jacobi(bool f64, bool fp64_compute, const SysDesc *d_descs,
-                                const uint64_t *d_prefix, uint32_t nsys, uint64_t total_knots,
-                                int tri_layout, cudaStream_t stream) {
+// kind: 0 float S -> float Phi^-1 (float arithmetic); 1 double -> double;
+// 2 double S -> float Phi^-1 (double arithmetic, for the refinement's inner solve)
+cudaError_t launch_block_jacobi(int kind, const SysDesc *d_descs, const uint64_t *d_prefix,
+                                uint32_t nsys, uint64_t total_knots, int tri_layout,
+                                cudaStream_t stream) {
     if (total_knots == 0) return cudaSuccess;
     const dim3 grid((unsigned)((total_knots + kPrecWarps - 1) / kPrecWarps)), block(kPrecWarps * 32);
-    if (f64)
-        block_jacobi_kernel<double, double><<<grid, block, 0, stream>>>(d_descs, d_prefix, nsys,
-                                                                        total_knots, tri_layout);
-    else if (fp64_compute)
-        block_jacobi_kernel<float, double><<<grid, block, 0, stream>>>(d_descs, d_prefix, nsys,
-                                                                       total_knots, tri_layout);
+    if (kind == 1)
+        block_jacobi_kernel<double, double, double><<<grid, block, 0, stream>>>(
+            d_descs, d_prefix, nsys, total_knots, tri_layout);
+    else if (kind == 2)
+        block_jacobi_kernel<double, float, double><<<grid, block, 0, stream>>>(
+            d_descs, d_prefix, nsys, total_knots, tri_layout);
     else
-        block_jacobi_kernel<float, float><<<grid, block, 0, stream>>>(d_descs, d_prefix, nsys,
-                                                                      total_knots, tri_layout);
+        block_jacobi_kernel<float, float, float><<<grid, block, 0, stream>>>(
+            d_descs, d_prefix, nsys, total_knots, tri_layout);
     return cudaGetLastError();
 }
 

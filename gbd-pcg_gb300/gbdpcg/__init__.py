@@ -44,15 +44,17 @@ class Config(ctypes.Structure):
                 ("algorithm", ctypes.c_uint32), ("cluster_size", ctypes.c_uint32),
                 ("max_threads", ctypes.c_uint32), ("storage", ctypes.c_uint32),
                 ("use_graph", ctypes.c_uint32), ("zero_guess", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 3)]
+                ("max_outer", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2),
+                ("inner_tol", ctypes.c_double)]
 
 
 class Result(ctypes.Structure):
     _fields_ = [("iters", ctypes.c_uint32), ("status", ctypes.c_int32), ("eta", ctypes.c_double),
-                ("relres", ctypes.c_double)]
+                ("relres", ctypes.c_double), ("outer", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
     def __repr__(self):
-        return f"Result(iters={self.iters}, status={self.status}, eta={self.eta:.3g}, relres={self.relres:.3g})"
+        return (f"Result(iters={self.iters}, status={self.status}, eta={self.eta:.3g}, "
+                f"relres={self.relres:.3g}, outer={self.outer})")
 
 
 class PackedSystem(ctypes.Structure):
@@ -82,6 +84,8 @@ _SIGS = {
     "gbdpcg_last_result": ([_P, _P], _I),
     "gbdpcg_block_jacobi_f32": ([_P, _P, _P, _U, _U, _U, _P], _I),
     "gbdpcg_block_jacobi_f64": ([_P, _P, _P, _U, _U, _U, _P], _I),
+    "gbdpcg_block_jacobi_f64to32": ([_P, _P, _P, _U, _U, _P], _I),
+    "gbdpcg_refine_solve_dev": ([_P, _P, _P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_adjoint_dev_f32": ([_P, _P, _P, _U, _P, _P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_plan_create": ([_P, _I, _P, _U, _U, _P, _P], _I),
     "gbdpcg_plan_execute": ([_P, _P], _I),
@@ -220,6 +224,19 @@ class Handle:
         fn = lib().gbdpcg_block_jacobi_f64 if S.dtype.itemsize == 8 else lib().gbdpcg_block_jacobi_f32
         _check(fn(self.h, _tp(S), _tp(Pinv_out), layout, n, N, _stream(stream)), "gbdpcg_block_jacobi")
 
+    def block_jacobi_f64to32(self, S64, Pinv32_out, n, N, stream=None):
+        _check(lib().gbdpcg_block_jacobi_f64to32(self.h, _tp(S64), _tp(Pinv32_out), n, N, _stream(stream)),
+               "gbdpcg_block_jacobi_f64to32")
+
+    def refine_solve(self, S64, Pinv32, gamma64, lam64, n, N, cfg=None, stream=None, sync=True):
+        """FP64 system by FP32 PCG + FP64 refinement (cfg.exit_mode must be EXIT_RELRES)."""
+        cfg = cfg or config(exit_mode=EXIT_RELRES, exit_tol=1e-10, max_iter=20000)
+        r = Result()
+        _check(lib().gbdpcg_refine_solve_dev(self.h, _tp(S64), _tp(Pinv32), _tp(gamma64), _tp(lam64), n, N,
+                                             ctypes.byref(cfg), ctypes.byref(r) if sync else None,
+                                             _stream(stream)), "gbdpcg_refine_solve_dev")
+        return r if sync else None
+
     def adjoint(self, S, Pinv, lam, grad_lam, grad_gamma, grad_S, n, N, layout=PINV_CBTD, cfg=None,
                 stream=None, sync=True):
         cfg = cfg or config()
@@ -246,7 +263,7 @@ class Plan:
             descs, S, P, g, l = packed
             arr = (PackedSystem * len(descs))(*[PackedSystem(*d) for d in descs])
             self.count = len(descs)
-            dt = 1 if S.dtype.itemsize == 8 else 0
+            dt = dtype if dtype is not None else (1 if S.dtype.itemsize == 8 else 0)
             _check(lib().gbdpcg_plan_create_packed(handle.h, dt, ctypes.cast(arr, ctypes.c_void_p), len(descs),
                                                    _tp(S), _tp(P), _tp(g), _tp(l), layout, ctypes.byref(cfg),
                                                    ctypes.byref(self.p)), "gbdpcg_plan_create_packed")

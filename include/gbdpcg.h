@@ -96,14 +96,19 @@ typedef struct {
     uint32_t storage;        /* GBDPCG_STORAGE_* */
     uint32_t use_graph;      /* plans: capture the launches in a CUDA graph (default 1) */
     uint32_t zero_guess;     /* 1: start from lambda = 0 and do not read lambda (default 0) */
-    uint32_t reserved[3];
+    uint32_t max_outer;      /* refinement: outer steps (default 50) */
+    uint32_t reserved[2];
+    double inner_tol;        /* refinement: relative residual of each FP32 inner solve (default 0.05) */
 } gbdpcg_config;
 
 typedef struct {
     uint32_t iters;        /* PCG passes, the converging one included (include/pcg.cuh:195) */
     int32_t status;        /* GBDPCG_CONVERGED / _MAX_ITER / _BREAKDOWN / _REJECTED */
     double eta;            /* last r^T Phi^-1 r */
-    double relres;         /* ||r||/||gamma|| of the recursive residual (-1 if not tracked) */
+    double relres;         /* ||r||/||gamma||: recursive residual, or the true FP64 residual of
+                              a refined solve (-1 if not tracked) */
+    uint32_t outer;        /* refinement: outer steps taken (0 otherwise) */
+    uint32_t reserved;
 } gbdpcg_result;
 
 /* One system of a batch.  Device pointers, element type of the batch.
@@ -167,6 +172,23 @@ GBDPCG_API int gbdpcg_solve_dev_f64(gbdpcg_handle_t h, const double *d_S, const 
 /* Waits for the last device-pointer solve of this handle and returns its result. */
 GBDPCG_API int gbdpcg_last_result(gbdpcg_handle_t h, gbdpcg_result *result);
 
+/* FP64 solve by FP32 PCG with FP64 iterative refinement (no reference
+ * counterpart).  S, gamma, lambda are double; Pinv is a compact block-diagonal
+ * FP32 Phi^-1 (gbdpcg_block_jacobi_f64to32).  One persistent cluster kernel:
+ * the rows of S are rounded to FP32 once and held on chip; each outer step
+ * forms the true residual gamma - S lambda in FP64, solves the correction with
+ * FP32 PCG (FP64 dot accumulation) to cfg->inner_tol relative residual, and
+ * adds it in FP64; it stops when ||gamma - S lambda|| <= cfg->exit_tol ||gamma||
+ * (exit_mode must be GBDPCG_EXIT_RELRES) or after cfg->max_iter inner passes /
+ * cfg->max_outer outer steps.  result->iters counts inner passes. */
+GBDPCG_API int gbdpcg_refine_solve_dev(gbdpcg_handle_t h, const double *d_S, const float *d_Pinv,
+                                       const double *d_gamma, double *d_lambda, uint32_t n,
+                                       uint32_t N, const gbdpcg_config *cfg,
+                                       gbdpcg_result *result, gbdpcg_stream_t stream);
+/* FP32 block-Jacobi Phi^-1 (compact) of an FP64 cbtd S, computed in FP64. */
+GBDPCG_API int gbdpcg_block_jacobi_f64to32(gbdpcg_handle_t h, const double *d_S, float *d_Pinv,
+                                           uint32_t n, uint32_t N, gbdpcg_stream_t stream);
+
 /* Block-Jacobi preconditioner Phi^-1 = blockdiag(S_kk^-1) of a cbtd S, on the
  * GPU, in cbtd or compact layout.  No reference counterpart: the reference
  * takes Phi^-1 from its caller. */
@@ -190,7 +212,9 @@ GBDPCG_API int gbdpcg_adjoint_dev_f32(gbdpcg_handle_t h, const float *d_S, const
 /* Batched solve of many independent systems of mixed n and N in persistent
  * cluster launches fed by device work queues (longest first), captured in one
  * CUDA graph.  No reference counterpart: the reference solves one system per
- * call.  `dtype` is 0 for float, 1 for double.  `systems` is a host array of
+ * call.  `dtype` is 0 for float, 1 for double, 2 for FP64 systems solved by FP32
+ * PCG with FP64 refinement (S, gamma, lambda double; Pinv compact FP32; see
+ * gbdpcg_refine_solve_dev).  `systems` is a host array of
  * device pointers; all systems of a plan share pinv_layout and whether they
  * are adjoint solves (lambda_fwd != NULL).  The plan keeps the pointers: re-
  * executing it re-solves whatever the buffers hold. */

@@ -144,8 +144,9 @@ __device__ __forceinline__ void reg_matvec(const T (&M)[RPT][NB * NP], const T *
 
 // Shared-memory block-row matvec of RPT adjacent rows i..i+RPT-1 over the
 // present blocks [b0, b1) of a column-major n x (NB n) block row; x points at
-// the window of block 0 (windows are NP apart).  Same summation order as
-// reg_matvec (padding there contributes exact zeros).
+// the window of block 0 (windows are NP apart).  Fully unrolled over the
+// compile-time bound NP with the columns j >= n predicated off, so all loads of
+// a block issue before its FMA chain; the same summation order as reg_matvec.
 template <typename T, int NP, int NB, int RPT>
 __device__ __forceinline__ void smem_matvec(const T *Mrow, int b0, int b1, const T *x, uint32_t n,
                                             uint32_t i, T (&y)[RPT]) {
@@ -156,20 +157,22 @@ __device__ __forceinline__ void smem_matvec(const T *Mrow, int b0, int b1, const
         for (int q = 0; q < RPT; ++q) acc[q][b] = T(0);
         if (b >= b0 && b < b1) {
             const T *col = Mrow + (size_t)b * n * n + i;
-            const T *xb = x + b * NP;
-#pragma unroll 4
-            for (uint32_t j = 0; j < n; ++j) {
-                const T xj = xb[j];
-                if constexpr (RPT == 2 && sizeof(T) == 4) {
-                    const float2 m = *reinterpret_cast<const float2 *>(col + (size_t)j * n);
-                    acc[0][b] = fma_rn(m.x, xj, acc[0][b]);
-                    acc[1][b] = fma_rn(m.y, xj, acc[1][b]);
-                } else if constexpr (RPT == 2) {
-                    const double2 m = *reinterpret_cast<const double2 *>(col + (size_t)j * n);
-                    acc[0][b] = fma_rn(m.x, xj, acc[0][b]);
-                    acc[1][b] = fma_rn(m.y, xj, acc[1][b]);
-                } else {
-                    acc[0][b] = fma_rn(col[(size_t)j * n], xj, acc[0][b]);
+            T xv[NP];
+            lds_row<T, NP>(xv, x + b * NP);
+#pragma unroll
+            for (int j = 0; j < NP; ++j) {
+                if ((uint32_t)j < n) {
+                    if constexpr (RPT == 2 && sizeof(T) == 4) {
+                        const float2 m = *reinterpret_cast<const float2 *>(col + (size_t)j * n);
+                        acc[0][b] = fma_rn(m.x, xv[j], acc[0][b]);
+                        acc[1][b] = fma_rn(m.y, xv[j], acc[1][b]);
+                    } else if constexpr (RPT == 2) {
+                        const double2 m = *reinterpret_cast<const double2 *>(col + (size_t)j * n);
+                        acc[0][b] = fma_rn(m.x, xv[j], acc[0][b]);
+                        acc[1][b] = fma_rn(m.y, xv[j], acc[1][b]);
+                    } else {
+                        acc[0][b] = fma_rn(col[(size_t)j * n], xv[j], acc[0][b]);
+                    }
                 }
             }
         }
@@ -190,20 +193,35 @@ __device__ __forceinline__ A warp_sum(A v) {
     return v;
 }
 
+// Butterfly over the warp for NQ values at once (the shuffles of the values
+// interleave): every lane ends with the warp's sums.
+template <typename A, int NQ>
+__device__ __forceinline__ void warp_sum_n(A (&v)[NQ]) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        A t[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) t[q] = __shfl_xor_sync(0xffffffffu, v[q], off);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) v[q] += t[q];
+    }
+}
+
 // Cluster-wide sum of NQ values, identical in every thread of the cluster.
-//   1. warp butterfly: every lane holds its warp's sum;
-//   2. lane 0 of warp w stores it into slot [rank*32 + w] of every CTA of the
-//      cluster (DSMEM stores; a local store when C == 1);
+//   1. warp butterfly: every lane holds its warp's sums;
+//   2. lane 0 of warp w stores them into slot [rank*32 + w] of every CTA of the
+//      cluster (DSMEM stores; local stores when C == 1);
 //   3. one barrier (barrier.cluster, or __syncthreads when C == 1), whose
 //      release/acquire makes the stores — and any halo pushes the caller made
 //      before this call — visible;
-//   4. every warp reduces the slots: lane l adds warp l's partials of ranks
-//      0..C-1 in rank order, then a butterfly over the lanes.
-// Every warp of every CTA reads the same slots in the same order, so all hold
-// the same bits; a warp's slot depends only on its index (rows map to threads
-// from thread 0), so the result does not depend on the CTA size either.
-// `buf` alternates between call sites so that a slot array is rewritten only
-// after a barrier that every reader has passed.  Slots: [buf][q][C*32].
+//   4. every thread sums the slots of ranks 0..C-1, warps 0..W-1 with pairwise
+//      vector loads into two accumulator chains (even / odd warps) and adds the
+//      two chains.
+// Every thread of every CTA reads the same slots in the same order, so all hold
+// the same bits; warps beyond the rows contribute exact zeros, so the result
+// does not depend on the CTA size.  `buf` alternates between call sites so
+// that a slot array is rewritten only after a barrier that every reader has
+// passed.  Slots: [buf][q][C*32].
 template <typename A, int NQ>
 __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
                                                   const cg::cluster_group &cluster, uint32_t C,
@@ -211,32 +229,51 @@ __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
     static_assert(NQ <= kMaxValues, "slot array holds kMaxValues values");
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nwarps = blockDim.x >> 5;
-    const uint32_t kMaxSlots = (uint32_t)slot_stride(C);
-    A *sl = slots + (size_t)buf * kMaxSlots * kMaxValues;
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) v[q] = warp_sum(v[q]);
+    const uint32_t stride = (uint32_t)slot_stride(C);
+    A *sl = slots + (size_t)buf * stride * kMaxValues;
+    warp_sum_n<A, NQ>(v);
     const uint32_t my = rank * 32 + warp;
     if (C == 1) {
         if (lane == 0) {
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) sl[q * kMaxSlots + my] = v[q];
+            for (int q = 0; q < NQ; ++q) sl[q * stride + my] = v[q];
         }
         __syncthreads();
     } else {
         if (lane < C) {
             A *dst = cluster.map_shared_rank(sl, lane);
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) dst[q * kMaxSlots + my] = v[q];
+            for (int q = 0; q < NQ; ++q) dst[q * stride + my] = v[q];
         }
         cluster.sync();
     }
+    A e[NQ], o[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-        A s = A(0);
-        if (lane < nwarps)
-            for (uint32_t c = 0; c < C; ++c) s += sl[q * kMaxSlots + c * 32 + lane];
-        v[q] = warp_sum(s);
+    for (int q = 0; q < NQ; ++q) e[q] = o[q] = A(0);
+    for (uint32_t c = 0; c < C; ++c) {
+        uint32_t w = 0;
+        for (; w + 1 < nwarps; w += 2) {
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                const A *pq = sl + q * stride + c * 32 + w;
+                if constexpr (sizeof(A) == 4) {
+                    const float2 t = *reinterpret_cast<const float2 *>(pq);
+                    e[q] += t.x;
+                    o[q] += t.y;
+                } else {
+                    const double2 t = *reinterpret_cast<const double2 *>(pq);
+                    e[q] += t.x;
+                    o[q] += t.y;
+                }
+            }
+        }
+        if (w < nwarps) {  // odd warp count: the last warp goes to the even chain
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) e[q] += sl[q * stride + c * 32 + w];
+        }
     }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) v[q] = e[q] + o[q];
 }
 
 __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uint32_t C) {

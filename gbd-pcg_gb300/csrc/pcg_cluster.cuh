@@ -142,37 +142,40 @@ __device__ __forceinline__ void reg_matvec(const T (&M)[RPT][NB * NP], const T *
     }
 }
 
-// Shared-memory block-row matvec of RPT adjacent rows i..i+RPT-1 over the
-// present blocks [b0, b1) of a column-major n x (NB n) block row; x points at
-// the window of block 0 (windows are NP apart).  Fully unrolled over the
-// compile-time bound NP with the columns j >= n predicated off, so all loads of
-// a block issue before its FMA chain; the same summation order as reg_matvec.
+// Shared-memory matrices are staged column-interleaved across the CTA's rows:
+// element (row r of the CTA, column c of the block row) at M[c*R + r], R the
+// row stride (even).  A warp then reads consecutive addresses for every column
+// (conflict-free 8-byte loads of two adjacent rows), where the cbtd layout
+// would put the warp's 4-5 knots on overlapping banks.
+//
+// Block-row matvec of RPT adjacent rows r..r+RPT-1 over the present blocks
+// [b0, b1) of an NB-block row; x points at the window of block 0 (windows are
+// NP apart).  Same summation order as reg_matvec (whose padding contributes
+// exact zeros).
 template <typename T, int NP, int NB, int RPT>
-__device__ __forceinline__ void smem_matvec(const T *Mrow, int b0, int b1, const T *x, uint32_t n,
-                                            uint32_t i, T (&y)[RPT]) {
+__device__ __forceinline__ void smem_matvec(const T *M, uint32_t R, uint32_t r, int b0, int b1,
+                                            const T *x, uint32_t n, T (&y)[RPT]) {
     T acc[RPT][NB];
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
         for (int q = 0; q < RPT; ++q) acc[q][b] = T(0);
         if (b >= b0 && b < b1) {
-            const T *col = Mrow + (size_t)b * n * n + i;
-            T xv[NP];
-            lds_row<T, NP>(xv, x + b * NP);
-#pragma unroll
-            for (int j = 0; j < NP; ++j) {
-                if ((uint32_t)j < n) {
-                    if constexpr (RPT == 2 && sizeof(T) == 4) {
-                        const float2 m = *reinterpret_cast<const float2 *>(col + (size_t)j * n);
-                        acc[0][b] = fma_rn(m.x, xv[j], acc[0][b]);
-                        acc[1][b] = fma_rn(m.y, xv[j], acc[1][b]);
-                    } else if constexpr (RPT == 2) {
-                        const double2 m = *reinterpret_cast<const double2 *>(col + (size_t)j * n);
-                        acc[0][b] = fma_rn(m.x, xv[j], acc[0][b]);
-                        acc[1][b] = fma_rn(m.y, xv[j], acc[1][b]);
-                    } else {
-                        acc[0][b] = fma_rn(col[(size_t)j * n], xv[j], acc[0][b]);
-                    }
+            const T *col = M + (size_t)b * n * R + r;
+            const T *xb = x + b * NP;
+#pragma unroll 4
+            for (uint32_t j = 0; j < n; ++j) {
+                const T xj = xb[j];
+                if constexpr (RPT == 2 && sizeof(T) == 4) {
+                    const float2 m = *reinterpret_cast<const float2 *>(col + (size_t)j * R);
+                    acc[0][b] = fma_rn(m.x, xj, acc[0][b]);
+                    acc[1][b] = fma_rn(m.y, xj, acc[1][b]);
+                } else if constexpr (RPT == 2) {
+                    const double2 m = *reinterpret_cast<const double2 *>(col + (size_t)j * R);
+                    acc[0][b] = fma_rn(m.x, xj, acc[0][b]);
+                    acc[1][b] = fma_rn(m.y, xj, acc[1][b]);
+                } else {
+                    acc[0][b] = fma_rn(col[(size_t)j * R], xj, acc[0][b]);
                 }
             }
         }
@@ -183,6 +186,18 @@ __device__ __forceinline__ void smem_matvec(const T *Mrow, int b0, int b1, const
 #pragma unroll
         for (int b = 1; b < NB; ++b) s += acc[q][b];
         y[q] = s;
+    }
+}
+
+// Stage the block rows of knots [kb, kb+nk) (blk = NB n^2 elements each,
+// column-major n x NB n) into the column-interleaved layout M[c*R + k*n + i].
+template <typename TO, typename TI>
+__device__ __forceinline__ void stage_rows(TO *M, uint32_t R, const TI *__restrict__ g, uint32_t nk,
+                                           uint32_t n, uint32_t blk, uint32_t tid, uint32_t nthr) {
+    for (uint32_t e = tid; e < nk * blk; e += nthr) {
+        const uint32_t kl = e / blk, w = e - kl * blk;
+        const uint32_t c = w / n, i = w - c * n;
+        M[(size_t)c * R + kl * n + i] = static_cast<TO>(__ldg(g + e));
     }
 }
 
@@ -209,19 +224,17 @@ __device__ __forceinline__ void warp_sum_n(A (&v)[NQ]) {
 
 // Cluster-wide sum of NQ values, identical in every thread of the cluster.
 //   1. warp butterfly: every lane holds its warp's sums;
-//   2. lane 0 of warp w stores them into slot [rank*32 + w] of every CTA of the
-//      cluster (DSMEM stores; local stores when C == 1);
+//   2. lane 0 of warp w stores them into slot [rank*W + w] (W warps per CTA)
+//      of every CTA of the cluster (DSMEM stores; local stores when C == 1);
 //   3. one barrier (barrier.cluster, or __syncthreads when C == 1), whose
 //      release/acquire makes the stores — and any halo pushes the caller made
 //      before this call — visible;
-//   4. every thread sums the slots of ranks 0..C-1, warps 0..W-1 with pairwise
-//      vector loads into two accumulator chains (even / odd warps) and adds the
-//      two chains.
+//   4. the C*W slots are summed: up to 8 by every thread in slot order, more by
+//      lane l summing slots l, l+32, ... followed by a butterfly.
 // Every thread of every CTA reads the same slots in the same order, so all hold
-// the same bits; warps beyond the rows contribute exact zeros, so the result
-// does not depend on the CTA size.  `buf` alternates between call sites so
-// that a slot array is rewritten only after a barrier that every reader has
-// passed.  Slots: [buf][q][C*32].
+// the same bits.  `buf` alternates between call sites so that a slot array is
+// rewritten only after a barrier that every reader has passed.
+// Slots: [buf][q][C*32].
 template <typename A, int NQ>
 __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
                                                   const cg::cluster_group &cluster, uint32_t C,
@@ -232,7 +245,7 @@ __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
     const uint32_t stride = (uint32_t)slot_stride(C);
     A *sl = slots + (size_t)buf * stride * kMaxValues;
     warp_sum_n<A, NQ>(v);
-    const uint32_t my = rank * 32 + warp;
+    const uint32_t my = rank * nwarps + warp, total = C * nwarps;
     if (C == 1) {
         if (lane == 0) {
 #pragma unroll
@@ -247,33 +260,24 @@ __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
         }
         cluster.sync();
     }
-    A e[NQ], o[NQ];
+    if (total <= 8) {
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) e[q] = o[q] = A(0);
-    for (uint32_t c = 0; c < C; ++c) {
-        uint32_t w = 0;
-        for (; w + 1 < nwarps; w += 2) {
+        for (int q = 0; q < NQ; ++q) {
+            A s = sl[q * stride];
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) {
-                const A *pq = sl + q * stride + c * 32 + w;
-                if constexpr (sizeof(A) == 4) {
-                    const float2 t = *reinterpret_cast<const float2 *>(pq);
-                    e[q] += t.x;
-                    o[q] += t.y;
-                } else {
-                    const double2 t = *reinterpret_cast<const double2 *>(pq);
-                    e[q] += t.x;
-                    o[q] += t.y;
-                }
-            }
+            for (uint32_t j = 1; j < 8; ++j)
+                if (j < total) s += sl[q * stride + j];
+            v[q] = s;
         }
-        if (w < nwarps) {  // odd warp count: the last warp goes to the even chain
+    } else {
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) e[q] += sl[q * stride + c * 32 + w];
+        for (int q = 0; q < NQ; ++q) {
+            A s = A(0);
+            for (uint32_t j = lane; j < total; j += 32) s += sl[q * stride + j];
+            v[q] = s;
         }
+        warp_sum_n<A, NQ>(v);
     }
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) v[q] = e[q] + o[q];
 }
 
 __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uint32_t C) {
@@ -351,6 +355,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         const T *__restrict__ lam0 =
             (d.flags & SYS_LAMBDA0_ZERO) ? nullptr : static_cast<const T *>(d.lambda0);
         const uint32_t blkS = 3 * n * n, blkP = NBP * n * n;
+        const uint32_t R = (K * n + 1) & ~1u;  // row stride of staged matrices (even)
         const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
         const bool first_knot = act && lk == 0 && kb > 0, last_knot = act && lk + 1 == nk && ke < N;
 
@@ -374,7 +379,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             }
         } else {
             const T *Sg = S + (size_t)kb * blkS;
-            for (uint32_t e = tid; e < nk * blkS; e += nthr) ms[e] = __ldg(Sg + e);
+            stage_rows(ms, R, Sg, nk, n, blkS, tid, nthr);
         }
         if constexpr (P_REG) {
             const T *Pk = P + (size_t)k * blkP;
@@ -392,20 +397,20 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             }
         } else {
             const T *Pg = P + (size_t)kb * blkP;
-            for (uint32_t e = tid; e < nk * blkP; e += nthr) mp[e] = __ldg(Pg + e);
+            stage_rows(mp, R, Pg, nk, n, blkP, tid, nthr);
         }
         const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
         auto matS = [&](const T *x, T(&y)[RPT]) {
             if constexpr (S_REG) reg_matvec<T, NP, 3, RPT>(Sr, x, y);
-            else smem_matvec<T, NP, 3, RPT>(ms + lk * blkS, sb0, sb1, x, n, i, y);
+            else smem_matvec<T, NP, 3, RPT>(ms, R, lk * n + i, sb0, sb1, x, n, y);
         };
         auto matP = [&](const T *x, T(&y)[RPT]) {
             if constexpr (P_REG) {
                 if constexpr (PTRI) reg_matvec<T, NP, 3, RPT>(Pr, x, y);
                 else reg_matvec<T, NP, 1, RPT>(Pr, x + NP, y);
             } else {
-                if constexpr (PTRI) smem_matvec<T, NP, 3, RPT>(mp + lk * blkP, sb0, sb1, x, n, i, y);
-                else smem_matvec<T, NP, 1, RPT>(mp + lk * blkP, 0, 1, x + NP, n, i, y);
+                if constexpr (PTRI) smem_matvec<T, NP, 3, RPT>(mp, R, lk * n + i, sb0, sb1, x, n, y);
+                else smem_matvec<T, NP, 1, RPT>(mp, R, lk * n + i, 0, 1, x + NP, n, y);
             }
         };
         T *my_p = vp + (lk + 1) * NP + i;  // this thread's rows in the windows
@@ -739,6 +744,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
         const T *__restrict__ lam0 =
             (d.flags & SYS_LAMBDA0_ZERO) ? nullptr : static_cast<const T *>(d.lambda0);
         const uint32_t blkS = 3 * n * n, blkP = n * n;
+        const uint32_t R = (K * n + 1) & ~1u;  // row stride of staged matrices (even)
         const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
         const bool first_knot = act && lk == 0 && kb > 0, last_knot = act && lk + 1 == nk && ke < N;
 
@@ -767,7 +773,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
             }
         } else {
             const T *Sg = S + (size_t)kb * blkS;
-            for (uint32_t e = tid; e < nk * blkS; e += nthr) ms[e] = __ldg(Sg + e);
+            stage_rows(ms, R, Sg, nk, n, blkS, tid, nthr);
         }
         if constexpr (P_REG) {
             const T *Pk = P + (size_t)k * blkP;
@@ -778,16 +784,16 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
                     Pr[q][j] = (act && (uint32_t)j < n) ? __ldg(Pk + j * n + i + q) : T(0);
         } else {
             const T *Pg = P + (size_t)kb * blkP;
-            for (uint32_t e = tid; e < nk * blkP; e += nthr) mp[e] = __ldg(Pg + e);
+            stage_rows(mp, R, Pg, nk, n, blkP, tid, nthr);
         }
         const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
         auto matS = [&](const T *x, T(&y)[RPT]) {
             if constexpr (S_REG) reg_matvec<T, NP, 3, RPT>(Sr, x, y);
-            else smem_matvec<T, NP, 3, RPT>(ms + lk * blkS, sb0, sb1, x, n, i, y);
+            else smem_matvec<T, NP, 3, RPT>(ms, R, lk * n + i, sb0, sb1, x, n, y);
         };
         auto matP = [&](const T *x, T(&y)[RPT]) {
             if constexpr (P_REG) reg_matvec<T, NP, 1, RPT>(Pr, x + NP, y);
-            else smem_matvec<T, NP, 1, RPT>(mp + lk * blkP, 0, 1, x + NP, n, i, y);
+            else smem_matvec<T, NP, 1, RPT>(mp, R, lk * n + i, 0, 1, x + NP, n, y);
         };
         // u of halo row t (0..n-1 left knot, n..2n-1 right knot) from the r halo,
         // in the order of the owner's Phi^-1 matvec (j ascending from 0)

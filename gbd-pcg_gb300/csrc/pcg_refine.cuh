@@ -96,6 +96,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
         const double *__restrict__ lam0 =
             (d.flags & SYS_LAMBDA0_ZERO) ? nullptr : static_cast<const double *>(d.lambda0);
         const uint32_t blkS = 3 * n * n, blkP = n * n;
+        const uint32_t R = (K * n + 1) & ~1u;  // row stride of staged matrices (even)
         const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
         const bool first_knot = act && lk == 0 && kb > 0, last_knot = act && lk + 1 == nk && ke < N;
         const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
             }
         } else {
             const double *Sg = S64 + (size_t)kb * blkS;
-            for (uint32_t e = tid; e < nk * blkS; e += nthr) ms[e] = __double2float_rn(__ldg(Sg + e));
+            stage_rows(ms, R, Sg, nk, n, blkS, tid, nthr);
         }
         if constexpr (P_REG) {
             const T *Pk = P + (size_t)k * blkP;
@@ -132,15 +133,15 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
                     Pr[q][j] = (act && (uint32_t)j < n) ? __ldg(Pk + j * n + i + q) : T(0);
         } else {
             const T *Pg = P + (size_t)kb * blkP;
-            for (uint32_t e = tid; e < nk * blkP; e += nthr) mp[e] = __ldg(Pg + e);
+            stage_rows(mp, R, Pg, nk, n, blkP, tid, nthr);
         }
         auto matS = [&](const T *x, T(&y)[RPT]) {
             if constexpr (S_REG) reg_matvec<T, NP, 3, RPT>(Sr, x, y);
-            else smem_matvec<T, NP, 3, RPT>(ms + lk * blkS, sb0, sb1, x, n, i, y);
+            else smem_matvec<T, NP, 3, RPT>(ms, R, lk * n + i, sb0, sb1, x, n, y);
         };
         auto matP = [&](const T *x, T(&y)[RPT]) {
             if constexpr (P_REG) reg_matvec<T, NP, 1, RPT>(Pr, x + NP, y);
-            else smem_matvec<T, NP, 1, RPT>(mp + lk * blkP, 0, 1, x + NP, n, i, y);
+            else smem_matvec<T, NP, 1, RPT>(mp, R, lk * n + i, 0, 1, x + NP, n, y);
         };
         T *my_p = vp + (lk + 1) * NP + i;
         T *my_r = vr + (lk + 1) * NP + i;

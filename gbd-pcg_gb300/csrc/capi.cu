@@ -199,7 +199,9 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
     }
     const bool ptri = layout == GBDPCG_PINV_CBTD;
     const bool acc64 = refine || cfg.dot_precision == GBDPCG_DOT_FP64;
-    const int alg = refine ? 2 : (cfg.algorithm == GBDPCG_ALGO_SINGLE_REDUCTION ? 1 : 0);
+    const int alg = refine ? 2
+                           : (cfg.algorithm == GBDPCG_ALGO_SINGLE_REDUCTION ? 1
+                                                                             : (cfg.algorithm == GBDPCG_ALGO_RECURRENCE ? 3 : 0));
     if (alg == 1 && ptri)
         return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm needs a block-diagonal Phi^-1");
     for (const Pref &pf : storage_prefs(f64 && !refine, ptri, cfg.storage)) {
@@ -215,7 +217,7 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
             const uint32_t K = (N + C - 1) / C;
             const uint32_t thr = (K * n + pf.rpt - 1) / pf.rpt;
             if (thr > cap) continue;
-            if (vi->v.smem_bytes(K, C) > (size_t)reg->max_smem_optin) continue;
+            if (vi->v.smem_bytes(K, C, 32) > (size_t)reg->max_smem_optin) continue;
             s.vi = vi;
             s.C = C;
             s.K = K;
@@ -303,7 +305,7 @@ int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
     if (!cfg) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "config is NULL");
     if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad pinv_layout");
     if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FP64 ||
-        cfg->algorithm > GBDPCG_ALGO_SINGLE_REDUCTION || cfg->storage > GBDPCG_STORAGE_SPLIT ||
+        cfg->algorithm > GBDPCG_ALGO_RECURRENCE || cfg->storage > GBDPCG_STORAGE_SPLIT ||
         cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1 ||
         !(cfg->inner_tol >= 0) || cfg->inner_tol >= 1)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad config field");
@@ -342,7 +344,7 @@ int launch_plain(gbdpcg_handle_s *h, bool f64, const SysDesc &d, SysResult *d_re
 
 int launch_cluster(const Shape &sh, const LaunchParams &lp, uint32_t grid_clusters,
                    cudaStream_t stream) {
-    const size_t smem = sh.vi->v.smem_bytes(lp.kmax, sh.C);
+    const size_t smem = sh.vi->v.smem_bytes(lp.kmax, sh.C, sh.threads / 32);
     int rc = prepare_variant(sh.vi, smem, sh.C);
     if (rc) return rc;
     cudaLaunchConfig_t cfg;
@@ -817,7 +819,7 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
         pc.order_off = (uint32_t)order.size();
         order.insert(order.end(), pc.items.begin(), pc.items.end());
         int active = 0;
-        rc = max_active_clusters(pc.sh, pc.sh.vi->v.smem_bytes(pc.kmax, pc.sh.C), &active);
+        rc = max_active_clusters(pc.sh, pc.sh.vi->v.smem_bytes(pc.kmax, pc.sh.C, pc.sh.threads / 32), &active);
         if (rc) return rc;
         if (active <= 0)
             return fail(GBDPCG_ERR_UNSUPPORTED, "cluster shape cannot be scheduled (C=" +

@@ -68,8 +68,12 @@ struct SmemPlan {
     __host__ __device__ static size_t slots(uint32_t C) {
         return round_up(2 * kMaxValues * slot_stride(C) * sizeof(A), 32);
     }
-    __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C) {
-        return 2 * vec(kmax) + 2 * halo() + slots(C) + 32 + mat_s(kmax) + mat_p(kmax);
+    // per-warp scratch of the first reduction stage: [warp][value][lane]
+    __host__ __device__ static size_t wscr(uint32_t nwarps) {
+        return round_up((size_t)nwarps * kMaxValues * 32 * sizeof(A), 32);
+    }
+    __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C, uint32_t nwarps) {
+        return 2 * vec(kmax) + 2 * halo() + slots(C) + wscr(nwarps) + 32 + mat_s(kmax) + mat_p(kmax);
     }
 };
 
@@ -222,21 +226,45 @@ __device__ __forceinline__ void warp_sum_n(A (&v)[NQ]) {
     }
 }
 
+// Sum of the 32 values at p (A-typed, 16-byte aligned) with vector loads into
+// four accumulator chains (element j into chain j mod 4), then (c0+c1)+(c2+c3).
+template <typename A>
+__device__ __forceinline__ A sum32(const A *p) {
+    A c0 = A(0), c1 = A(0), c2 = A(0), c3 = A(0);
+    if constexpr (sizeof(A) == 4) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float4 t = reinterpret_cast<const float4 *>(p)[j];
+            c0 += t.x; c1 += t.y; c2 += t.z; c3 += t.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const double2 t0 = reinterpret_cast<const double2 *>(p)[2 * j];
+            const double2 t1 = reinterpret_cast<const double2 *>(p)[2 * j + 1];
+            c0 += t0.x; c1 += t0.y; c2 += t1.x; c3 += t1.y;
+        }
+    }
+    return (c0 + c1) + (c2 + c3);
+}
+
 // Cluster-wide sum of NQ values, identical in every thread of the cluster.
-//   1. warp butterfly: every lane holds its warp's sums;
-//   2. lane 0 of warp w stores them into slot [rank*W + w] (W warps per CTA)
-//      of every CTA of the cluster (DSMEM stores; local stores when C == 1);
-//   3. one barrier (barrier.cluster, or __syncthreads when C == 1), whose
+//   1. each lane stores its values in its warp's scratch row; after a warp
+//      barrier, lanes 0..max(C,1)-1 each re-read the 32 values (vector loads,
+//      four chains: no shuffle chain) and store the warp's sums into slot
+//      [rank*W + w] of CTA `lane` (DSMEM stores; local when C == 1);
+//   2. one barrier (barrier.cluster, or __syncthreads when C == 1), whose
 //      release/acquire makes the stores — and any halo pushes the caller made
 //      before this call — visible;
-//   4. the C*W slots are summed: up to 8 by every thread in slot order, more by
-//      lane l summing slots l, l+32, ... followed by a butterfly.
+//   3. every thread sums the slots: the first 32 (zero beyond C*W) with sum32;
+//      when C*W > 32, lane l sums slots l, l+32, ... and a warp butterfly
+//      finishes.
 // Every thread of every CTA reads the same slots in the same order, so all hold
 // the same bits.  `buf` alternates between call sites so that a slot array is
-// rewritten only after a barrier that every reader has passed.
-// Slots: [buf][q][C*32].
+// rewritten only after a barrier that every reader has passed.  Slots
+// [buf][q][C*32] are zeroed at kernel start; wscr is [warp][q][32].
 template <typename A, int NQ>
-__device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
+__device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, A *wscr, int buf,
                                                   const cg::cluster_group &cluster, uint32_t C,
                                                   uint32_t rank) {
     static_assert(NQ <= kMaxValues, "slot array holds kMaxValues values");
@@ -244,31 +272,23 @@ __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, int buf,
     const uint32_t nwarps = blockDim.x >> 5;
     const uint32_t stride = (uint32_t)slot_stride(C);
     A *sl = slots + (size_t)buf * stride * kMaxValues;
-    warp_sum_n<A, NQ>(v);
+    A *ws = wscr + (size_t)warp * kMaxValues * 32;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) ws[q * 32 + lane] = v[q];
+    __syncwarp();
     const uint32_t my = rank * nwarps + warp, total = C * nwarps;
-    if (C == 1) {
-        if (lane == 0) {
+    if (lane < C) {
+        A *dst = (C == 1) ? sl : cluster.map_shared_rank(sl, lane);
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) sl[q * stride + my] = v[q];
-        }
-        __syncthreads();
-    } else {
-        if (lane < C) {
-            A *dst = cluster.map_shared_rank(sl, lane);
-#pragma unroll
-            for (int q = 0; q < NQ; ++q) dst[q * stride + my] = v[q];
-        }
-        cluster.sync();
+        for (int q = 0; q < NQ; ++q) dst[q * stride + my] = sum32(ws + q * 32);
     }
-    if (total <= 8) {
+    if (C == 1)
+        __syncthreads();
+    else
+        cluster.sync();
+    if (total <= 32) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            A s = sl[q * stride];
-#pragma unroll
-            for (uint32_t j = 1; j < 8; ++j)
-                if (j < total) s += sl[q * stride + j];
-            v[q] = s;
-        }
+        for (int q = 0; q < NQ; ++q) v[q] = sum32(sl + q * stride);
     } else {
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
@@ -291,7 +311,12 @@ __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uin
 // A: accumulation type of the dot products (T, or double for mixed precision);
 // NP: compile-time block-size bound (n <= NP); PTRI: Phi^-1 is block-
 // tridiagonal; ST: storage of the matrix rows; RPT: rows per thread.
-template <typename T, typename A, int NP, bool PTRI, int ST, int RPT>
+// REC: recurrence form — y = S p and z = Phi^-1 r are carried by
+// y = S z + beta y and z -= alpha Phi^-1 y, with each matvec done right after
+// the reduction that precedes it, so an iteration has only the two reduction
+// barriers (the direct form also needs a barrier after each vector update).
+// Same passes on well-conditioned systems; iterates differ at roundoff level.
+template <typename T, typename A, int NP, bool PTRI, int ST, int RPT, bool REC>
 __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threads), 1)
     pcg_cluster_kernel(const LaunchParams lp) {
     using Plan = SmemPlan<T, A, NP, PTRI, ST>;
@@ -309,11 +334,13 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     T *uh = reinterpret_cast<T *>(sp); sp += Plan::halo();
     T *zh = reinterpret_cast<T *>(sp); sp += Plan::halo();
     A *slots = reinterpret_cast<A *>(sp); sp += Plan::slots(C);
+    A *wscr = reinterpret_cast<A *>(sp); sp += Plan::wscr(nthr >> 5);
     uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp);
     const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
 
+    for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     for (uint32_t pass = 0;; ++pass) {
         // ---- pull the next system (cluster leader pops, broadcasts by DSMEM)
@@ -482,7 +509,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 v2[0] += A(r[q]) * A(z[q]);
                 v2[1] += A(gam[q]) * A(gam[q]);
             }
-            cluster_allreduce<A, 2>(v2, slots, 1, cluster, C, rank);
+            cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
             eta = v2[0];
             gg = v2[1];
         }
@@ -494,93 +521,180 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         int32_t status = ST_MAX_ITER;
         A eta_new = A(0), rr = A(0);
         const uint32_t max_iter = d.max_iter;
-        for (; iter < max_iter;) {
+        if constexpr (REC) {
+            // y = S p0 (p0 = z0 and its halos are in vp after the barrier above)
             if (act) matS(vp + lk * NP, y);
             else {
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) y[q] = T(0);
             }
-            if constexpr (PTRI) {  // neighbours need this CTA's boundary upsilon for their r halo
-                if (first_knot) {
-                    T *dst = cluster.map_shared_rank(uh, rank - 1) + NP + i;
+            for (; iter < max_iter;) {
+                // y into the vr window (own rows; PTRI: boundary into the neighbours' halos)
+                if (act) {
 #pragma unroll
-                    for (int q = 0; q < RPT; ++q) dst[q] = y[q];
+                    for (int q = 0; q < RPT; ++q) my_r[q] = y[q];
                 }
-                if (last_knot) {
-                    T *dst = cluster.map_shared_rank(uh, rank + 1) + i;
+                if constexpr (PTRI) {
+                    if (first_knot) {
+                        T *dst = cluster.map_shared_rank(vr, rank - 1) + (K + 1) * NP + i;
 #pragma unroll
-                    for (int q = 0; q < RPT; ++q) dst[q] = y[q];
-                }
-            }
-            A pap;
-            {
-                A v1[1] = {A(0)};
+                        for (int q = 0; q < RPT; ++q) dst[q] = y[q];
+                    }
+                    if (last_knot) {
+                        T *dst = cluster.map_shared_rank(vr, rank + 1) + i;
 #pragma unroll
-                for (int q = 0; q < RPT; ++q) v1[0] += A(p[q]) * A(y[q]);
-                cluster_allreduce<A, 1>(v1, slots, 0, cluster, C, rank);
-                pap = v1[0];
-            }
-            const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
-#pragma unroll
-            for (int q = 0; q < RPT; ++q) {
-                lam[q] = fma_rn(alpha, p[q], lam[q]);
-                r[q] = fma_rn(-alpha, y[q], r[q]);
-                if (act) my_r[q] = r[q];
-            }
-            if constexpr (PTRI) {
-                for (uint32_t t = tid; t < 2 * n; t += nthr) {
-                    if (t < n && has_left) vr[t] = fma_rn(-alpha, uh[t], vr[t]);
-                    if (t >= n && has_right) {
-                        T *h = vr + (nk + 1) * NP + (t - n);
-                        *h = fma_rn(-alpha, uh[NP + t - n], *h);
+                        for (int q = 0; q < RPT; ++q) dst[q] = y[q];
                     }
                 }
-            }
-            __syncthreads();
-            if (act) matP(vr + lk * NP, z);
-            else {
+                A pap;
+                {
+                    A v1[1] = {A(0)};
 #pragma unroll
-                for (int q = 0; q < RPT; ++q) z[q] = T(0);
-            }
-            if (first_knot) {
-                T *dst = cluster.map_shared_rank(zh, rank - 1) + NP + i;
+                    for (int q = 0; q < RPT; ++q) v1[0] += A(p[q]) * A(y[q]);
+                    cluster_allreduce<A, 1>(v1, slots, wscr, 0, cluster, C, rank);
+                    pap = v1[0];
+                }
+                const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
+                T qv[RPT];
+                if (act) matP(vr + lk * NP, qv);
+                else {
 #pragma unroll
-                for (int q = 0; q < RPT; ++q) dst[q] = z[q];
-            }
-            if (last_knot) {
-                T *dst = cluster.map_shared_rank(zh, rank + 1) + i;
-#pragma unroll
-                for (int q = 0; q < RPT; ++q) dst[q] = z[q];
-            }
-            {
-                A v2[2] = {A(0), A(0)};
+                    for (int q = 0; q < RPT; ++q) qv[q] = T(0);
+                }
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
-                    v2[0] += A(r[q]) * A(z[q]);
-                    if (relres) v2[1] += A(r[q]) * A(r[q]);
+                    lam[q] = fma_rn(alpha, p[q], lam[q]);
+                    r[q] = fma_rn(-alpha, y[q], r[q]);
+                    z[q] = act ? fma_rn(-alpha, qv[q], z[q]) : T(0);
+                    if (act) my_p[q] = z[q];
                 }
-                cluster_allreduce<A, 2>(v2, slots, 1, cluster, C, rank);
-                eta_new = v2[0];
-                rr = v2[1];
-            }
-            ++iter;
-            if (!isfinite(eta_new) || !isfinite(pap)) { status = ST_BREAKDOWN; break; }
-            if (relres ? (rr <= thr) : (fabs(eta_new) < tol)) { status = ST_CONVERGED; break; }
-            const T beta = T(eta_new / eta);
-            eta = eta_new;
+                if (first_knot) {
+                    T *dst = cluster.map_shared_rank(vp, rank - 1) + (K + 1) * NP + i;
 #pragma unroll
-            for (int q = 0; q < RPT; ++q) {
-                p[q] = fma_rn(beta, p[q], z[q]);
-                if (act) my_p[q] = p[q];
-            }
-            for (uint32_t t = tid; t < 2 * n; t += nthr) {
-                if (t < n && has_left) vp[t] = fma_rn(beta, vp[t], zh[t]);
-                if (t >= n && has_right) {
-                    T *h = vp + (nk + 1) * NP + (t - n);
-                    *h = fma_rn(beta, *h, zh[NP + t - n]);
+                    for (int q = 0; q < RPT; ++q) dst[q] = z[q];
+                }
+                if (last_knot) {
+                    T *dst = cluster.map_shared_rank(vp, rank + 1) + i;
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) dst[q] = z[q];
+                }
+                {
+                    A v2[2] = {A(0), A(0)};
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) {
+                        v2[0] += A(r[q]) * A(z[q]);
+                        if (relres) v2[1] += A(r[q]) * A(r[q]);
+                    }
+                    cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
+                    eta_new = v2[0];
+                    rr = v2[1];
+                }
+                ++iter;
+                if (!isfinite(eta_new) || !isfinite(pap)) { status = ST_BREAKDOWN; break; }
+                if (relres ? (rr <= thr) : (fabs(eta_new) < tol)) { status = ST_CONVERGED; break; }
+                const T beta = T(eta_new / eta);
+                eta = eta_new;
+                T w[RPT];
+                if (act) matS(vp + lk * NP, w);
+                else {
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) w[q] = T(0);
+                }
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) {
+                    p[q] = fma_rn(beta, p[q], z[q]);
+                    y[q] = fma_rn(beta, y[q], w[q]);
                 }
             }
-            __syncthreads();
+        } else {
+            for (; iter < max_iter;) {
+                if (act) matS(vp + lk * NP, y);
+                else {
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) y[q] = T(0);
+                }
+                if constexpr (PTRI) {  // neighbours need this CTA's boundary upsilon for their r halo
+                    if (first_knot) {
+                        T *dst = cluster.map_shared_rank(uh, rank - 1) + NP + i;
+#pragma unroll
+                        for (int q = 0; q < RPT; ++q) dst[q] = y[q];
+                    }
+                    if (last_knot) {
+                        T *dst = cluster.map_shared_rank(uh, rank + 1) + i;
+#pragma unroll
+                        for (int q = 0; q < RPT; ++q) dst[q] = y[q];
+                    }
+                }
+                A pap;
+                {
+                    A v1[1] = {A(0)};
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) v1[0] += A(p[q]) * A(y[q]);
+                    cluster_allreduce<A, 1>(v1, slots, wscr, 0, cluster, C, rank);
+                    pap = v1[0];
+                }
+                const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) {
+                    lam[q] = fma_rn(alpha, p[q], lam[q]);
+                    r[q] = fma_rn(-alpha, y[q], r[q]);
+                    if (act) my_r[q] = r[q];
+                }
+                if constexpr (PTRI) {
+                    for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                        if (t < n && has_left) vr[t] = fma_rn(-alpha, uh[t], vr[t]);
+                        if (t >= n && has_right) {
+                            T *h = vr + (nk + 1) * NP + (t - n);
+                            *h = fma_rn(-alpha, uh[NP + t - n], *h);
+                        }
+                    }
+                }
+                __syncthreads();
+                if (act) matP(vr + lk * NP, z);
+                else {
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) z[q] = T(0);
+                }
+                if (first_knot) {
+                    T *dst = cluster.map_shared_rank(zh, rank - 1) + NP + i;
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) dst[q] = z[q];
+                }
+                if (last_knot) {
+                    T *dst = cluster.map_shared_rank(zh, rank + 1) + i;
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) dst[q] = z[q];
+                }
+                {
+                    A v2[2] = {A(0), A(0)};
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) {
+                        v2[0] += A(r[q]) * A(z[q]);
+                        if (relres) v2[1] += A(r[q]) * A(r[q]);
+                    }
+                    cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
+                    eta_new = v2[0];
+                    rr = v2[1];
+                }
+                ++iter;
+                if (!isfinite(eta_new) || !isfinite(pap)) { status = ST_BREAKDOWN; break; }
+                if (relres ? (rr <= thr) : (fabs(eta_new) < tol)) { status = ST_CONVERGED; break; }
+                const T beta = T(eta_new / eta);
+                eta = eta_new;
+#pragma unroll
+                for (int q = 0; q < RPT; ++q) {
+                    p[q] = fma_rn(beta, p[q], z[q]);
+                    if (act) my_p[q] = p[q];
+                }
+                for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                    if (t < n && has_left) vp[t] = fma_rn(beta, vp[t], zh[t]);
+                    if (t >= n && has_right) {
+                        T *h = vp + (nk + 1) * NP + (t - n);
+                        *h = fma_rn(beta, *h, zh[NP + t - n]);
+                    }
+                }
+                __syncthreads();
+            }
         }
 
         // ---- outputs   (include/pcg.cuh:212-217)
@@ -658,8 +772,8 @@ template <typename T, typename A, int NP, int ST>
 struct SmemPlanSR {
     using Base = SmemPlan<T, A, NP, false, ST>;
     __host__ __device__ static size_t mhalo() { return round_up((size_t)2 * NP * NP * sizeof(T), 32); }
-    __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C) {
-        return Base::bytes(kmax, C) + mhalo() + 2 * Base::halo();
+    __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C, uint32_t nwarps) {
+        return Base::bytes(kmax, C, nwarps) + mhalo() + 2 * Base::halo();
     }
 };
 
@@ -697,6 +811,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
     T *sh = reinterpret_cast<T *>(sp); sp += Plan::halo();          // s of the halo knots
     T *wh0 = reinterpret_cast<T *>(sp); sp += Plan::halo();         // received w halos, buffer 0
     A *slots = reinterpret_cast<A *>(sp); sp += Plan::slots(C);
+    A *wscr = reinterpret_cast<A *>(sp); sp += Plan::wscr(nthr >> 5);
     uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp); sp += Plan::mat_p(lp.kmax);
@@ -704,6 +819,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
     T *wh1 = reinterpret_cast<T *>(sp);                              // received w halos, buffer 1
     const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
 
+    for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     for (uint32_t pass = 0;; ++pass) {
         uint32_t item;
@@ -884,7 +1000,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
                 v3[1] += A(w[q]) * A(u[q]);
                 v3[2] += A(gam[q]) * A(gam[q]);
             }
-            cluster_allreduce<A, 3>(v3, slots, 0, cluster, C, rank);
+            cluster_allreduce<A, 3>(v3, slots, wscr, 0, cluster, C, rank);
             g = v3[0];
             dlt = v3[1];
             gg = v3[2];
@@ -960,7 +1076,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
                     v3[1] += A(w[q]) * A(u[q]);
                     if (relres) v3[2] += A(r[q]) * A(r[q]);
                 }
-                cluster_allreduce<A, 3>(v3, slots, (iter + 1) & 1, cluster, C, rank);
+                cluster_allreduce<A, 3>(v3, slots, wscr, (iter + 1) & 1, cluster, C, rank);
                 g_new = v3[0];
                 dn = v3[1];
                 rr = v3[2];

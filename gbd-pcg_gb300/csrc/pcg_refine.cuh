@@ -25,8 +25,8 @@ struct SmemPlanRF {
     __host__ __device__ static size_t dwin(uint32_t kmax) {
         return round_up((size_t)(kmax + 2) * NP * sizeof(double), 32);
     }
-    __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C) {
-        return Base::bytes(kmax, C) + dwin(kmax);
+    __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C, uint32_t nwarps) {
+        return Base::bytes(kmax, C, nwarps) + dwin(kmax);
     }
 };
 
@@ -49,6 +49,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
     T *uh = reinterpret_cast<T *>(sp); sp += Plan::halo();  // unused (block-diagonal Phi^-1)
     T *zh = reinterpret_cast<T *>(sp); sp += Plan::halo();
     A *slots = reinterpret_cast<A *>(sp); sp += Plan::slots(C);
+    A *wscr = reinterpret_cast<A *>(sp); sp += Plan::wscr(nthr >> 5);
     uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp); sp += Plan::mat_p(lp.kmax);
@@ -57,6 +58,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
     const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
     const uint32_t zero_d = (uint32_t)(SmemPlanRF<NP, ST>::dwin(lp.kmax) / sizeof(double));
 
+    for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     for (uint32_t pass = 0;; ++pass) {
         uint32_t item;
@@ -159,7 +161,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
             A v1[1] = {0.0};
 #pragma unroll
             for (int q = 0; q < RPT; ++q) v1[0] = fma(gam[q], gam[q], v1[0]);
-            cluster_allreduce<A, 1>(v1, slots, buf, cluster, C, rank);
+            cluster_allreduce<A, 1>(v1, slots, wscr, buf, cluster, C, rank);
             buf ^= 1;
             gg = v1[0];
         }
@@ -206,7 +208,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
                 A v1[1] = {0.0};
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) v1[0] = fma(r64[q], r64[q], v1[0]);
-                cluster_allreduce<A, 1>(v1, slots, buf, cluster, C, rank);
+                cluster_allreduce<A, 1>(v1, slots, wscr, buf, cluster, C, rank);
                 buf ^= 1;
                 rr64 = v1[0];
             }
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
                     v2[0] += A(r[q]) * A(z[q]);
                     v2[1] += A(r[q]) * A(r[q]);
                 }
-                cluster_allreduce<A, 2>(v2, slots, buf, cluster, C, rank);
+                cluster_allreduce<A, 2>(v2, slots, wscr, buf, cluster, C, rank);
                 buf ^= 1;
                 eta = v2[0];
                 rr_in0 = v2[1];
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
                     A v1[1] = {A(0)};
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) v1[0] += A(p[q]) * A(y[q]);
-                    cluster_allreduce<A, 1>(v1, slots, buf, cluster, C, rank);
+                    cluster_allreduce<A, 1>(v1, slots, wscr, buf, cluster, C, rank);
                     buf ^= 1;
                     pap = v1[0];
                 }
@@ -306,7 +308,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
                         v2[0] += A(r[q]) * A(z[q]);
                         v2[1] += A(r[q]) * A(r[q]);
                     }
-                    cluster_allreduce<A, 2>(v2, slots, buf, cluster, C, rank);
+                    cluster_allreduce<A, 2>(v2, slots, wscr, buf, cluster, C, rank);
                     buf ^= 1;
                     eta_new = v2[0];
                     rr = v2[1];

@@ -8,9 +8,24 @@
 #define GBDPCG_VARIANT(T, A, NP, PTRI, ST, RPT)                                               \
     ::gbdpcg::KernelVariant {                                                                 \
         sizeof(T) == 8, sizeof(A) == 8, NP, PTRI, ST, RPT, 0,                                 \
-            (const void *)&::gbdpcg::pcg_cluster_kernel<T, A, NP, PTRI, ST, RPT>,             \
+            (const void *)&::gbdpcg::pcg_cluster_kernel<T, A, NP, PTRI, ST, RPT, false>,      \
             &::gbdpcg::SmemPlan<T, A, NP, PTRI, ST>::bytes                                    \
     }
+#define GBDPCG_VARIANT_REC(T, A, NP, PTRI, ST, RPT)                                           \
+    ::gbdpcg::KernelVariant {                                                                 \
+        sizeof(T) == 8, sizeof(A) == 8, NP, PTRI, ST, RPT, 3,                                 \
+            (const void *)&::gbdpcg::pcg_cluster_kernel<T, A, NP, PTRI, ST, RPT, true>,       \
+            &::gbdpcg::SmemPlan<T, A, NP, PTRI, ST>::bytes                                    \
+    }
+// recurrence form (two barriers per iteration)
+#define GBDPCG_VARIANTS_REC(NP)                                                               \
+    out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_REG, 1);                        \
+    out[c++] = GBDPCG_VARIANT_REC(float, float, NP, true, ST_REG, 1);                         \
+    out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_REG_S, 1);                      \
+    out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_SMEM, 1);                       \
+    out[c++] = GBDPCG_VARIANT_REC(float, double, NP, false, ST_REG, 1);                       \
+    out[c++] = GBDPCG_VARIANT_REC(double, double, NP, false, ST_SMEM, 1);
+#define GBDPCG_VARIANTS_REC_RPT2(NP) out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_REG_S, 2);
 #define GBDPCG_VARIANT_SR(T, A, NP, ST, RPT)                                                  \
     ::gbdpcg::KernelVariant {                                                                 \
         sizeof(T) == 8, sizeof(A) == 8, NP, false, ST, RPT, 1,                                \

@@ -14,13 +14,14 @@ struct KernelVariant {
                  // shared memory, 2 both in shared memory
     int rpt;     // matrix rows per thread (2 needs an even n)
     int alg;     // 0 two reductions per iteration, 1 single reduction (block-diagonal Phi^-1),
-                 // 2 FP32 inner PCG with FP64 refinement
+                 // 2 FP32 inner PCG with FP64 refinement, 3 recurrence form (two barriers
+                 // per iteration)
     const void *func;
-    size_t (*smem_bytes)(uint32_t kmax, uint32_t C);
+    size_t (*smem_bytes)(uint32_t kmax, uint32_t C, uint32_t nwarps);
 };
 
 // Each returns the number of variants written to `out` (at most kMaxVariantsPerNP).
-constexpr int kMaxVariantsPerNP = 32;
+constexpr int kMaxVariantsPerNP = 48;
 int variants_np6(KernelVariant *out);
 int variants_np8(KernelVariant *out);
 int variants_np12(KernelVariant *out);

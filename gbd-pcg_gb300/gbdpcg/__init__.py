@@ -27,7 +27,7 @@ SUCCESS, ERR_INVALID_ARGUMENT, ERR_UNSUPPORTED, ERR_CUDA, ERR_NO_MEMORY = 0, 1, 
 CONVERGED, MAX_ITER, BREAKDOWN, REJECTED = 0, 1, 2, -1
 EXIT_REFERENCE, EXIT_RELRES = 0, 1
 PINV_CBTD, PINV_BLOCKDIAG = 0, 1
-ALGO_AUTO, ALGO_CLUSTER, ALGO_PLAIN, ALGO_SINGLE_REDUCTION = 0, 1, 2, 3
+ALGO_AUTO, ALGO_CLUSTER, ALGO_PLAIN, ALGO_SINGLE_REDUCTION, ALGO_RECURRENCE = 0, 1, 2, 3, 4
 DOT_NATIVE, DOT_FP64 = 0, 1
 STORAGE_AUTO, STORAGE_REGISTERS, STORAGE_SHARED, STORAGE_SPLIT = 0, 1, 2, 3
 

@@ -301,3 +301,49 @@ def test_single_reduction_rejects_tridiagonal_pinv(gb, oracle_mod, handle):
     with pytest.raises(gb.GbdpcgError) as e:
         gb.solve(S, P, g, lam, 6, 10, gb.config(algorithm=gb.ALGO_SINGLE_REDUCTION))
     assert e.value.code == gb.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("dts", ["f32", "f64"])
+@pytest.mark.parametrize("storage", ["auto", "registers", "shared", "split"])
+@pytest.mark.parametrize("n,N,C,layout", [(14, 128, 0, "compact"), (6, 64, 1, "compact"), (24, 100, 0, "compact"),
+                                          (12, 40, 3, "compact"), (7, 19, 2, "compact"), (14, 1, 0, "compact"),
+                                          (14, 64, 4, "cbtd"), (5, 30, 2, "cbtd")])
+def test_recurrence_vs_oracle(gb, oracle_mod, handle, dts, storage, n, N, C, layout):
+    """The recurrence form (y = S p, z = Phi^-1 r by recurrences, two barriers
+    per iteration) against the oracle's direct iteration: same passes +-1, as
+    accurate against the FP64 solution."""
+    import torch
+    O = oracle_mod
+    dt = _dt(dts)
+    sy, S, P, g = system(O, n, N, 41, dt, layout)
+    tol = 1e-6 if dts == "f32" else 1e-12
+    flags = O.EXIT_RELRES | (O.PINV_BLOCKDIAG if layout == "compact" else 0)
+    lam_o, it_o, st_o, _, _ = O.pcg(S, P, g, np.zeros(n * N, dt), n, N, 500, tol, flags=flags)
+    d = torch.device("cuda:0")
+    lam = torch.zeros(n * N, dtype=torch.float64 if dts == "f64" else torch.float32, device=d)
+    st = {"auto": gb.STORAGE_AUTO, "registers": gb.STORAGE_REGISTERS, "shared": gb.STORAGE_SHARED,
+          "split": gb.STORAGE_SPLIT}[storage]
+    lay = gb.PINV_BLOCKDIAG if layout == "compact" else gb.PINV_CBTD
+    try:
+        r = handle.solve(*(torch.from_numpy(a).to(d) for a in (S, P, g)), lam, n, N, lay,
+                         gb.config(max_iter=500, exit_tol=tol, exit_mode=gb.EXIT_RELRES, storage=st,
+                                   cluster_size=C, algorithm=gb.ALGO_RECURRENCE))
+    except gb.GbdpcgError as e:
+        assert e.code == gb.ERR_UNSUPPORTED
+        pytest.skip(f"no {storage} recurrence shape at n={n} N={N} C={C} {layout}")
+    assert r.status == gb.CONVERGED and abs(int(r.iters) - it_o) <= 1, (r, it_o)
+    x = O.block_cholesky_solve(S.astype(np.float64), n, N, g.astype(np.float64))
+    assert relerr(lam.cpu().numpy(), x) <= 1.5 * relerr(lam_o, x) + (1e-6 if dts == "f32" else 1e-13)
+
+
+def test_recurrence_reference_exit(gb, oracle_mod, handle):
+    """Reference exit test: the recurrence form takes the reference's passes on
+    the n=14 configurations (cbtd Phi^-1, as solvePCG is called)."""
+    O = oracle_mod
+    for N in (32, 128):
+        sy, S, Pt, g = system(O, 14, N, 0, np.float32)
+        lam_r, it_r, _ = O.ref_pcg(S, Pt, g, np.zeros(14 * N, np.float32), 14, N, 200, 1e-6)
+        lam = np.zeros(14 * N, np.float32)
+        r = gb.solve(S, Pt, g, lam, 14, N, gb.config(max_iter=200, algorithm=gb.ALGO_RECURRENCE))
+        assert r.iters == it_r
+        assert relerr(lam, lam_r) < 2e-5

@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--systems", type=int, default=4096)
-    ap.add_argument("--no-extras", action="store_true", help="skip the CPU and plain baselines")
+    ap.add_argument("--no-extras", action="store_true", help="skip the baselines and the other configurations")
+    ap.add_argument("--algorithm", default="auto", choices=["auto", "standard", "recurrence", "single-reduction"])
     return ap.parse_args()
 
 
@@ -141,6 +142,175 @@ def cpu_port_baseline(Sa, Pa, ga, descs, sample, threads):
     return sample / dt, dt, used, iters, status
 
 
+def single_system_latency(gbdpcg, h, dev):
+    """us per PCG iteration of one system solved alone (n=14; N=32 and N=128;
+    FP32 tol 1e-6 and FP64 tol 1e-12, reference exit test, seed 0), for the
+    cluster solver (standard and recurrence forms) and the plain kernel."""
+    import torch
+    from gbdpcg.workload import generate
+    out = []
+    for N, dts in ((32, "f32"), (128, "f32"), (128, "f64")):
+        n = 14
+        tdt = torch.float64 if dts == "f64" else torch.float32
+        npdt = np.float64 if dts == "f64" else np.float32
+        sy = generate(n, N, 0)
+        S = torch.from_numpy(sy.cbtd(npdt)).to(dev)
+        g = torch.from_numpy(sy.gamma.astype(npdt)).to(dev)
+        P = torch.empty(n * n * N, dtype=tdt, device=dev)
+        h.block_jacobi(S, P, n, N, gbdpcg.PINV_BLOCKDIAG)
+        Pt = torch.zeros(N, 3 * n, n, dtype=tdt, device=dev)
+        Pt[:, n:2 * n, :] = P.view(N, n, n)
+        Pt = Pt.view(-1)
+        lam = torch.zeros(n * N, dtype=tdt, device=dev)
+        tol = 1e-12 if dts == "f64" else 1e-6
+        row = {"n": n, "N": N, "dtype": dts}
+        for name, algo, PP, lay in (("cluster", gbdpcg.ALGO_CLUSTER, P, gbdpcg.PINV_BLOCKDIAG),
+                                    ("recurrence", gbdpcg.ALGO_RECURRENCE, P, gbdpcg.PINV_BLOCKDIAG),
+                                    ("plain", gbdpcg.ALGO_PLAIN, Pt, gbdpcg.PINV_CBTD)):
+            cfg = gbdpcg.config(max_iter=500, exit_tol=tol, algorithm=algo, zero_guess=1)
+            best = None
+            for C in ((0,) if algo == gbdpcg.ALGO_PLAIN else (0, 1, 2, 4, 8, 16)):
+                cfg.cluster_size = C
+                try:
+                    r = h.solve(S, PP, g, lam, n, N, lay, cfg)
+                except gbdpcg.GbdpcgError:
+                    continue
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                for _ in range(20):
+                    h.solve(S, PP, g, lam, n, N, lay, cfg, sync=False)
+                b.record()
+                b.synchronize()
+                us = 1e3 * a.elapsed_time(b) / 20
+                if best is None or us < best[0]:
+                    best = (us, r.iters, C)
+            if best:
+                row[name] = {"us_per_solve": best[0], "iters": best[1], "us_per_iteration": best[0] / best[1],
+                             "cluster_size": best[2]}
+        out.append(row)
+    return out
+
+
+def adjoint_config(gbdpcg, h, dev, count=1024, n=14, N=64):
+    """Forward + adjoint cost: batch 1024, n=14, N=64, FP32, L = 1/2 ||lambda - lambda*||^2."""
+    import torch
+    from gbdpcg.workload import generate
+    fwd, adj = [], []
+    rng = np.random.default_rng(12345)
+    for b in range(count):
+        sy = generate(n, N, 100000 + b)
+        S = torch.from_numpy(sy.cbtd(np.float32)).to(dev)
+        g = torch.from_numpy(sy.gamma.astype(np.float32)).to(dev)
+        P = torch.empty(n * n * N, device=dev)
+        fwd.append({"S": S, "Pinv": P, "gamma": g, "lambda": torch.zeros(n * N, device=dev), "n": n, "N": N})
+        adj.append({"star": torch.from_numpy(rng.standard_normal(n * N).astype(np.float32)).to(dev)})
+    cfg = gbdpcg.config(max_iter=500, exit_tol=1e-6, exit_mode=gbdpcg.EXIT_RELRES, zero_guess=1)
+    pf = gbdpcg.Plan(h, fwd, gbdpcg.PINV_BLOCKDIAG, cfg)
+    pf.build_block_jacobi()
+    pf.execute()
+    torch.cuda.synchronize()
+    systems = []
+    for f, a in zip(fwd, adj):
+        a["gl"] = f["lambda"] - a["star"]
+        systems.append({"S": f["S"], "Pinv": f["Pinv"], "gamma": a["gl"], "lambda": torch.empty_like(a["gl"]),
+                        "lambda_fwd": f["lambda"], "dS": torch.empty_like(f["S"]), "n": n, "N": N})
+    pa = gbdpcg.Plan(h, systems, gbdpcg.PINV_BLOCKDIAG, cfg)
+
+    def timeit(fn, reps=5):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    t_f = timeit(pf.execute)
+    t_a = timeit(pa.execute)
+    res_a = pa.results()
+    out = {"systems": count, "n": n, "N": N, "forward_ms": t_f, "adjoint_ms": t_a,
+           "forward_plus_adjoint_over_forward": (t_f + t_a) / t_f,
+           "adjoint_all_converged": all(r.status == 0 for r in res_a),
+           "note": "adjoint = PCG solve of S mu = lambda - lambda* plus the fused dS, dgamma epilogue"}
+    pf.close()
+    pa.close()
+    return out
+
+
+def precision_config(gbdpcg, h, dev, count=256, n=24, N=256, workers=8):
+    """FP32 PCG + FP64 refinement vs plain FP64 PCG, both to relative residual
+    1e-10, on ill-conditioned systems (Q log-U[1e-2,1e4], R log-U[1e-3,1])."""
+    import torch
+    from gbdpcg.workload import generate
+    import multiprocessing as mp
+    seeds = list(range(200000, 200000 + count))
+    with mp.get_context("spawn").Pool(workers) as pool:
+        syss = pool.starmap(_gen_ill, [(n, N, sd) for sd in seeds], chunksize=4)
+    S64 = [torch.from_numpy(S).to(dev) for S, g in syss]
+    g64 = [torch.from_numpy(g).to(dev) for S, g in syss]
+    out = {"systems": count, "n": n, "N": N, "target_relres": 1e-10}
+    # FP32 + FP64 refinement: one plan, dtype 2
+    systems = [{"S": S64[i], "Pinv": torch.empty(n * n * N, dtype=torch.float32, device=dev), "gamma": g64[i],
+                "lambda": torch.zeros(n * N, dtype=torch.float64, device=dev), "n": n, "N": N} for i in range(count)]
+    cfg = gbdpcg.config(exit_mode=gbdpcg.EXIT_RELRES, exit_tol=1e-10, max_iter=40000, max_outer=60, zero_guess=1)
+    pr = gbdpcg.Plan(h, systems, gbdpcg.PINV_BLOCKDIAG, cfg, dtype=2)
+    pr.build_block_jacobi()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    pr.execute()
+    e1.record()
+    e1.synchronize()
+    rr = pr.results()
+    out["refined"] = {"ms": e0.elapsed_time(e1), "converged": sum(r.status == 0 for r in rr),
+                      "inner_iters_mean": float(np.mean([r.iters for r in rr])),
+                      "outer_mean": float(np.mean([r.outer for r in rr])),
+                      "relres_max": float(max(r.relres for r in rr))}
+    lam_ref = [s["lambda"] for s in systems]
+    pr.close()
+    # plain FP64 PCG (the reference scheme: cbtd Phi^-1, one cooperative launch per system)
+    t64, it64, conv64 = 0.0, [], 0
+    nsamp = min(count, 32)
+    for i in range(nsamp):
+        P64 = torch.empty(3 * n * n * N, dtype=torch.float64, device=dev)
+        h.block_jacobi(S64[i], P64, n, N, gbdpcg.PINV_CBTD)
+        lam = torch.zeros(n * N, dtype=torch.float64, device=dev)
+        cfg64 = gbdpcg.config(exit_mode=gbdpcg.EXIT_RELRES, exit_tol=1e-10, max_iter=40000, zero_guess=1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        r = h.solve(S64[i], P64, g64[i], lam, n, N, gbdpcg.PINV_CBTD, cfg64, sync=False)
+        b.record()
+        b.synchronize()
+        r = h.last_result()
+        t64 += a.elapsed_time(b)
+        it64.append(r.iters)
+        conv64 += r.status == 0
+    out["fp64_pcg"] = {"ms_for_batch_extrapolated": t64 / nsamp * count, "sample": nsamp, "converged": conv64,
+                       "iters_mean": float(np.mean(it64)),
+                       "how": "best FP64 path that holds n=24, N=256: one cooperative launch per system"}
+    out["speedup_refined_vs_fp64"] = out["fp64_pcg"]["ms_for_batch_extrapolated"] / out["refined"]["ms"]
+    # accuracy against the FP64 block-Cholesky oracle on a few systems (host)
+    try:
+        from oracle import oracle as O
+        errs = []
+        for i in range(0, count, max(1, count // 4)):
+            S, g = syss[i]
+            x = O.block_cholesky_solve(S, n, N, g)
+            errs.append(float(np.linalg.norm(lam_ref[i].cpu().numpy() - x) / np.linalg.norm(x)))
+        out["refined"]["error_vs_block_cholesky_max"] = max(errs)
+    except Exception as e:  # the oracle is optional on this leg
+        out["refined"]["error_vs_block_cholesky_max"] = f"unavailable: {e}"
+    return out
+
+
+def _gen_ill(n, N, seed):
+    from gbdpcg.workload import generate
+    sy = generate(n, N, seed, ill=True)
+    return sy.cbtd(), sy.gamma
+
+
 def run_reference(args):
     """--impl reference: the reference has no CPU implementation of its PCG; the
     oracle's C port of it runs on all host threads over the same workload."""
@@ -206,7 +376,9 @@ def main():
     dP = torch.empty(nP, dtype=torch.float32, device=dev)
     dl = torch.zeros(ga.size, dtype=torch.float32, device=dev)
     h = gbdpcg.Handle(local)
-    cfg = gbdpcg.config(max_iter=MAX_ITER, exit_tol=TOL, exit_mode=gbdpcg.EXIT_RELRES, zero_guess=1)
+    algo = {"auto": gbdpcg.ALGO_AUTO, "standard": gbdpcg.ALGO_CLUSTER, "recurrence": gbdpcg.ALGO_RECURRENCE,
+            "single-reduction": gbdpcg.ALGO_SINGLE_REDUCTION}[args.algorithm]
+    cfg = gbdpcg.config(max_iter=MAX_ITER, exit_tol=TOL, exit_mode=gbdpcg.EXIT_RELRES, zero_guess=1, algorithm=algo)
     plan = gbdpcg.Plan(h, layout=gbdpcg.PINV_BLOCKDIAG, cfg=cfg, packed=(descs, dS, dP, dg, dl))
     plan.build_block_jacobi()
     torch.cuda.synchronize()
@@ -304,7 +476,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, see config)",
-        "config": {"workload": WORKLOAD, "systems_per_gpu": count, "global_batch": count * world,
+        "config": {"workload": WORKLOAD, "algorithm": args.algorithm, "systems_per_gpu": count,
+                   "global_batch": count * world,
                    "seeds": f"rank*{count} + [0, {count})", "l2": "inputs (1.1 GB/GPU) larger than L2",
                    "parallelism": f"replicas{world} (independent systems per GPU)",
                    "launches_per_step": len(launches)},
@@ -369,6 +542,14 @@ def main():
         line["cpu_baseline"] = {"value": rate, "unit": "solves/s", "cores": used, "kind": "port",
                                 "sample": f"first {csample} of the {count} systems, oracle/pcg_oracle.c, "
                                           f"{dt:.1f} s"}
+    if not args.no_extras and world == 1:
+        for key, fn in (("single_system", lambda: single_system_latency(gbdpcg, h, dev)),
+                        ("adjoint", lambda: adjoint_config(gbdpcg, h, dev)),
+                        ("precision", lambda: precision_config(gbdpcg, h, dev))):
+            try:
+                line[key] = fn()
+            except Exception as e:  # report, do not lose the headline line
+                line[key] = {"error": repr(e)}
     print(json.dumps(line), flush=True)
     plan.close()
     h.close()

@@ -311,11 +311,13 @@ __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uin
 // A: accumulation type of the dot products (T, or double for mixed precision);
 // NP: compile-time block-size bound (n <= NP); PTRI: Phi^-1 is block-
 // tridiagonal; ST: storage of the matrix rows; RPT: rows per thread.
-// REC: recurrence form — y = S p and z = Phi^-1 r are carried by
-// y = S z + beta y and z -= alpha Phi^-1 y, with each matvec done right after
-// the reduction that precedes it, so an iteration has only the two reduction
-// barriers (the direct form also needs a barrier after each vector update).
-// Same passes on well-conditioned systems; iterates differ at roundoff level.
+// REC: recurrence form — y = S p is carried by y = S z + beta y, with S z
+// computed right after the reduction that yields beta (z and its halos are in
+// the p window by then), so the barrier after the p update disappears: three
+// barriers per iteration instead of four.  (Carrying z = Phi^-1 r by a
+// recurrence too would remove a fourth, but in FP32 that recurrence drifts
+// and the iteration stalls.)  Same passes on well-conditioned systems;
+// iterates differ at roundoff level.
 template <typename T, typename A, int NP, bool PTRI, int ST, int RPT, bool REC>
 __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threads), 1)
     pcg_cluster_kernel(const LaunchParams lp) {
@@ -529,19 +531,14 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 for (int q = 0; q < RPT; ++q) y[q] = T(0);
             }
             for (; iter < max_iter;) {
-                // y into the vr window (own rows; PTRI: boundary into the neighbours' halos)
-                if (act) {
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) my_r[q] = y[q];
-                }
-                if constexpr (PTRI) {
+                if constexpr (PTRI) {  // neighbours need this CTA's boundary y for their r halo
                     if (first_knot) {
-                        T *dst = cluster.map_shared_rank(vr, rank - 1) + (K + 1) * NP + i;
+                        T *dst = cluster.map_shared_rank(uh, rank - 1) + NP + i;
 #pragma unroll
                         for (int q = 0; q < RPT; ++q) dst[q] = y[q];
                     }
                     if (last_knot) {
-                        T *dst = cluster.map_shared_rank(vr, rank + 1) + i;
+                        T *dst = cluster.map_shared_rank(uh, rank + 1) + i;
 #pragma unroll
                         for (int q = 0; q < RPT; ++q) dst[q] = y[q];
                     }
@@ -555,18 +552,31 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                     pap = v1[0];
                 }
                 const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
-                T qv[RPT];
-                if (act) matP(vr + lk * NP, qv);
-                else {
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) qv[q] = T(0);
-                }
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
                     lam[q] = fma_rn(alpha, p[q], lam[q]);
                     r[q] = fma_rn(-alpha, y[q], r[q]);
-                    z[q] = act ? fma_rn(-alpha, qv[q], z[q]) : T(0);
-                    if (act) my_p[q] = z[q];
+                    if (act) my_r[q] = r[q];
+                }
+                if constexpr (PTRI) {
+                    for (uint32_t t = tid; t < 2 * n; t += nthr) {
+                        if (t < n && has_left) vr[t] = fma_rn(-alpha, uh[t], vr[t]);
+                        if (t >= n && has_right) {
+                            T *h = vr + (nk + 1) * NP + (t - n);
+                            *h = fma_rn(-alpha, uh[NP + t - n], *h);
+                        }
+                    }
+                }
+                __syncthreads();
+                if (act) matP(vr + lk * NP, z);
+                else {
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) z[q] = T(0);
+                }
+                // z into the vp window (own rows; boundary into the neighbours' halos)
+                if (act) {
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) my_p[q] = z[q];
                 }
                 if (first_knot) {
                     T *dst = cluster.map_shared_rank(vp, rank - 1) + (K + 1) * NP + i;

@@ -72,9 +72,9 @@ enum {
     GBDPCG_ALGO_SINGLE_REDUCTION = 3, /* cluster solver, Chronopoulos-Gear recurrences: one
                                          cluster-wide reduction per iteration; block-diagonal
                                          Phi^-1 only; iterates differ at roundoff level */
-    GBDPCG_ALGO_RECURRENCE = 4 /* cluster solver with S p and Phi^-1 r carried by recurrences:
-                                  two barriers per iteration instead of four; iterates differ
-                                  at roundoff level */
+    GBDPCG_ALGO_RECURRENCE = 4 /* cluster solver with S p carried by a recurrence: three
+                                  barriers per iteration instead of four; iterates differ at
+                                  roundoff level */
 };
 /* dot-product accumulation for float systems */
 enum { GBDPCG_DOT_NATIVE = 0, GBDPCG_DOT_FP64 = 1 };

@@ -240,6 +240,12 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
 
 }  // namespace
 
+namespace gbdpcg {
+// Message returned by gbdpcg_last_error() on this thread (for entry points in
+// other translation units).
+void set_last_error(const std::string &msg) { t_last_error = msg; }
+}  // namespace gbdpcg
+
 // ------------------------------------------------------------------ handle
 constexpr size_t kWorkspaceBytes = 4096;  // 2 result slots + 256 pad + descriptor + prefix
 

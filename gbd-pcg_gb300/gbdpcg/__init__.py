@@ -86,6 +86,7 @@ _SIGS = {
     "gbdpcg_block_jacobi_f64": ([_P, _P, _P, _U, _U, _U, _P], _I),
     "gbdpcg_block_jacobi_f64to32": ([_P, _P, _P, _U, _U, _P], _I),
     "gbdpcg_refine_solve_dev": ([_P, _P, _P, _P, _P, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_solve_plain_noalloc_f32": ([_P, _P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_adjoint_dev_f32": ([_P, _P, _P, _U, _P, _P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_plan_create": ([_P, _I, _P, _U, _U, _P, _P], _I),
     "gbdpcg_plan_execute": ([_P, _P], _I),

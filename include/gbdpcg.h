@@ -175,6 +175,27 @@ GBDPCG_API int gbdpcg_solve_dev_f64(gbdpcg_handle_t h, const double *d_S, const 
 /* Waits for the last device-pointer solve of this handle and returns its result. */
 GBDPCG_API int gbdpcg_last_result(gbdpcg_handle_t h, gbdpcg_result *result);
 
+/* Allocation-free solve of one FP32 system (no counterpart in the reference).
+ * For callers that must not allocate device memory while they run: a
+ * controller solving at a fixed rate, where an allocation in the loop costs
+ * unbounded time; a process whose device memory another allocator already
+ * owns; deployments that forbid allocation after start-up.  It runs the plain
+ * algorithm (one CTA per knot, the reference's arithmetic order; cbtd Pinv)
+ * with its scratch in one array of about 1 MiB compiled into the library,
+ * which every GPU that loads the library reserves until the process exits.
+ * Limits: n*N <= GBDPCG_NOALLOC_MAX_ELEMS and N <= GBDPCG_NOALLOC_MAX_KNOTS,
+ * else GBDPCG_ERR_UNSUPPORTED.  No handle, no cudaMalloc/cudaFree.  The first
+ * call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * with that device current; make it before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race.  If `result` is non-NULL the
+ * call waits for the stream and fills it. */
+#define GBDPCG_NOALLOC_MAX_ELEMS 131072
+#define GBDPCG_NOALLOC_MAX_KNOTS 4096
+GBDPCG_API int gbdpcg_solve_plain_noalloc_f32(const float *d_S, const float *d_Pinv,
+                                              const float *d_gamma, float *d_lambda, uint32_t n,
+                                              uint32_t N, const gbdpcg_config *cfg,
+                                              gbdpcg_result *result, gbdpcg_stream_t stream);
+
 /* FP64 solve by FP32 PCG with FP64 iterative refinement (no reference
  * counterpart).  S, gamma, lambda are double; Pinv is a compact block-diagonal
  * FP32 Phi^-1 (gbdpcg_block_jacobi_f64to32).  One persistent cluster kernel:

@@ -523,6 +523,7 @@ void gbdpcg_config_init(gbdpcg_config *cfg) {
     cfg->algorithm = GBDPCG_ALGO_AUTO;
     cfg->use_graph = 1;
     cfg->max_outer = 50;
+    cfg->streams = 8;
     cfg->inner_tol = 0.05;
 }
 
@@ -844,7 +845,8 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
                            cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(p->d_prefix.p, prefix.data(), sizeof(uint64_t) * count, cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemset(p->d_results.p, 0, sizeof(SysResult) * count));
-    const uint32_t ns = (uint32_t)std::min<size_t>(4, std::max<size_t>(1, nc));
+    const uint32_t ns = (uint32_t)std::min<size_t>(std::max<uint32_t>(1, std::min<uint32_t>(cfg->streams, 32)),
+                                                   std::max<size_t>(1, nc));
     for (uint32_t s = 0; s < ns; ++s) {
         cudaStream_t st;
         GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));

@@ -100,7 +100,8 @@ typedef struct {
     uint32_t use_graph;      /* plans: capture the launches in a CUDA graph (default 1) */
     uint32_t zero_guess;     /* 1: start from lambda = 0 and do not read lambda (default 0) */
     uint32_t max_outer;      /* refinement: outer steps (default 50) */
-    uint32_t reserved[2];
+    uint32_t streams;        /* plans: streams the launches of one execution spread over (default 8) */
+    uint32_t reserved[1];
     double inner_tol;        /* refinement: relative residual of each FP32 inner solve (default 0.05) */
 } gbdpcg_config;
 

@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--no-extras", action="store_true", help="skip the baselines and the other configurations")
     ap.add_argument("--algorithm", default="auto", choices=["auto", "standard", "recurrence", "single-reduction"])
+    ap.add_argument("--tune", default="shapes", choices=["off", "shapes", "shapes+recurrence", "shapes+algorithms"],
+                    help="autotune the plan before timing (untimed set-up, like building the plan)")
     return ap.parse_args()
 
 
@@ -409,6 +411,12 @@ def main():
     plan = gbdpcg.Plan(h, layout=gbdpcg.PINV_BLOCKDIAG, cfg=cfg, packed=(descs, dS, dP, dg, dl))
     plan.build_block_jacobi()
     torch.cuda.synchronize()
+    tune_s = 0.0
+    if args.tune != "off":
+        t0 = time.perf_counter()
+        plan.autotune(flags={"shapes": 0, "shapes+recurrence": gbdpcg.TUNE_RECURRENCE,
+                             "shapes+algorithms": gbdpcg.TUNE_RECURRENCE | gbdpcg.TUNE_SINGLE_REDUCTION}[args.tune])
+        tune_s = time.perf_counter() - t0
     launches = plan.launches()
     stream = torch.cuda.current_stream()
     for _ in range(max(3, args.warmup)):
@@ -489,7 +497,10 @@ def main():
                    "global_batch": count * world,
                    "seeds": f"rank*{count} + [0, {count})", "l2": "inputs (1.1 GB/GPU) larger than L2",
                    "parallelism": f"replicas{world} (independent systems per GPU)",
-                   "launches_per_step": len(launches)},
+                   "launches_per_step": len(launches), "autotune": args.tune,
+                   "autotune_s": round(tune_s, 2),
+                   "launch_shapes": [[l["cluster"], l["threads"], l["storage"], l["rows_per_thread"],
+                                      l["algorithm"], l["systems"]] for l in launches]},
         "iterations": {"mean": float(np.mean(iters)), "max": int(np.max(iters)), "min": int(np.min(iters)),
                        "all_converged": bool(all(s == 0 for s in status))},
         "true_relres_max_sample": worst,

@@ -157,6 +157,24 @@ struct DevBuf {
     }
 };
 
+// ------------------------------------------------------------------ tuning table
+// Key: what selects the kernel family (precision, refinement, dot precision,
+// Phi^-1 layout, adjoint epilogue, the requested algorithm and storage) and
+// the system size.  Value: the launch shape the autotuner measured fastest.
+struct TuneKey {
+    uint8_t f64, refine, acc64, ptri, adjoint, alg_req, storage_req;
+    uint32_t n, N;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(f64, refine, acc64, ptri, adjoint, alg_req, storage_req, n, N) <
+               std::tie(o.f64, o.refine, o.acc64, o.ptri, o.adjoint, o.alg_req, o.storage_req, o.n, o.N);
+    }
+};
+
+struct TuneChoice {
+    int st, rpt, alg;
+    uint32_t C, threads;
+};
+
 // ------------------------------------------------------------------ launch shapes
 struct Shape {
     VariantInfo *vi = nullptr;
@@ -181,8 +199,27 @@ std::vector<Pref> storage_prefs(bool f64, bool ptri, uint32_t storage) {
     return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{1, 2}, {0, 1}, {1, 1}, {2, 1}};
 }
 
+// A tuned shape for one system, if its variant exists and holds the system.
+bool tuned_shape(Registry *reg, bool f64, bool acc64, int np, bool ptri, uint32_t n, uint32_t N,
+                 const TuneChoice &tc, Shape *out) {
+    if (tc.rpt < 1 || n % tc.rpt || tc.C < 1 || tc.C > 16 || tc.threads == 0 || tc.threads % 32) return false;
+    VariantInfo *vi = find_variant(reg, f64, acc64, np, ptri, tc.st, tc.rpt, tc.alg);
+    if (!vi) return false;
+    const uint32_t K = (N + tc.C - 1) / tc.C;
+    const uint32_t thr = (K * n + tc.rpt - 1) / tc.rpt;
+    if (thr > tc.threads || tc.threads > (uint32_t)vi->max_threads) return false;
+    if (vi->v.smem_bytes(K, tc.C, tc.threads / 32) > (size_t)reg->max_smem_optin) return false;
+    out->vi = vi;
+    out->C = tc.C;
+    out->K = K;
+    out->threads = tc.threads;
+    out->plain = false;
+    return true;
+}
+
 int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layout,
-                 const gbdpcg_config &cfg, Shape *out, bool refine = false) {
+                 const gbdpcg_config &cfg, Shape *out, bool refine = false,
+                 const TuneChoice *tuned = nullptr) {
     Shape s;
     const int np = np_for(n);
     if (refine) {
@@ -204,6 +241,7 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
                                                                              : (cfg.algorithm == GBDPCG_ALGO_RECURRENCE ? 3 : 0));
     if (alg == 1 && ptri)
         return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm needs a block-diagonal Phi^-1");
+    if (tuned && tuned_shape(reg, f64 && !refine, acc64, np, ptri, n, N, *tuned, out)) return GBDPCG_SUCCESS;
     for (const Pref &pf : storage_prefs(f64 && !refine, ptri, cfg.storage)) {
         if (pf.rpt > 1 && (n % pf.rpt) != 0) continue;
         VariantInfo *vi = find_variant(reg, f64 && !refine, acc64, np, ptri, pf.st, pf.rpt, alg);
@@ -258,6 +296,8 @@ struct gbdpcg_handle_s {
     SysResult *d_last = nullptr;
     cudaStream_t last_stream = nullptr;
     bool last_f64 = false;
+    std::mutex tune_mu;  // guards `tune`
+    std::map<TuneKey, TuneChoice> tune;
 };
 
 namespace {
@@ -459,6 +499,74 @@ struct gbdpcg_plan_s {
 };
 
 namespace {
+
+TuneKey tune_key(const gbdpcg_plan_s *p, bool adjoint, uint32_t n, uint32_t N) {
+    TuneKey k;
+    memset(&k, 0, sizeof(k));
+    k.f64 = p->f64;
+    k.refine = p->refine;
+    k.acc64 = p->refine || p->cfg.dot_precision == GBDPCG_DOT_FP64;
+    k.ptri = p->layout == GBDPCG_PINV_CBTD;
+    k.adjoint = adjoint;
+    k.alg_req = (uint8_t)p->cfg.algorithm;
+    k.storage_req = (uint8_t)p->cfg.storage;
+    k.n = n;
+    k.N = N;
+    return k;
+}
+
+// Merges classes with the same launch shape, orders each class's systems
+// longest first and the classes by their largest system, builds the device
+// work list, sizes each persistent grid to the clusters that fit at once, and
+// drops a captured graph (the next execution captures the new launches).
+int plan_layout(gbdpcg_plan_s *p) {
+    std::vector<PlanClass> merged;
+    std::map<std::tuple<const void *, uint32_t, uint32_t>, size_t> index;
+    for (auto &pc : p->classes) {
+        auto key = std::make_tuple((const void *)pc.sh.vi, pc.sh.C, pc.sh.threads);
+        auto it = index.find(key);
+        if (it == index.end()) {
+            index.emplace(key, merged.size());
+            merged.push_back(pc);
+        } else {
+            PlanClass &m = merged[it->second];
+            m.items.insert(m.items.end(), pc.items.begin(), pc.items.end());
+            m.kmax = std::max(m.kmax, pc.kmax);
+        }
+    }
+    p->classes.swap(merged);
+    auto cost = [&](uint32_t i) { return (double)p->descs[i].n * p->descs[i].n * p->descs[i].N; };
+    for (auto &pc : p->classes)
+        std::stable_sort(pc.items.begin(), pc.items.end(),
+                         [&](uint32_t a, uint32_t b) { return cost(a) > cost(b); });
+    std::stable_sort(p->classes.begin(), p->classes.end(),
+                     [&](const PlanClass &a, const PlanClass &b) {
+                         return cost(a.items[0]) > cost(b.items[0]);
+                     });
+    std::vector<uint32_t> order;
+    for (auto &pc : p->classes) {
+        pc.order_off = (uint32_t)order.size();
+        order.insert(order.end(), pc.items.begin(), pc.items.end());
+        int active = 0;
+        int rc = max_active_clusters(pc.sh, pc.sh.vi->v.smem_bytes(pc.kmax, pc.sh.C, pc.sh.threads / 32), &active);
+        if (rc) return rc;
+        if (active <= 0)
+            return fail(GBDPCG_ERR_UNSUPPORTED, "cluster shape cannot be scheduled (C=" +
+                                                    std::to_string(pc.sh.C) + ")");
+        pc.grid_clusters = std::min<uint32_t>((uint32_t)pc.items.size(), (uint32_t)active);
+    }
+    int rc;
+    if ((rc = p->d_order.ensure(sizeof(uint32_t) * std::max<size_t>(1, order.size())))) return rc;
+    if ((rc = p->d_queues.ensure(sizeof(uint32_t) * std::max<size_t>(1, p->classes.size())))) return rc;
+    if (!order.empty())
+        GB_CUDA(cudaMemcpy(p->d_order.p, order.data(), sizeof(uint32_t) * order.size(),
+                           cudaMemcpyHostToDevice));
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    p->gexec = nullptr;
+    p->graph = nullptr;
+    return GBDPCG_SUCCESS;
+}
 
 int plan_enqueue(gbdpcg_plan_s *p, cudaStream_t stream) {
     const uint32_t nc = (uint32_t)p->classes.size();
@@ -774,6 +882,9 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
     const bool adjoint = systems[0].lambda_fwd != nullptr;
     std::map<std::tuple<const void *, uint32_t, uint32_t>, uint32_t> class_of;
     std::vector<uint64_t> prefix(count);
+    // tuned shapes apply unless the config pins the cluster or CTA size
+    const bool use_table = !cfg->cluster_size && !cfg->max_threads;
+    std::unique_lock<std::mutex> tune_lock(h->tune_mu);
     for (uint32_t i = 0; i < count; ++i) {
         const gbdpcg_system &s = systems[i];
         if (!s.S || !s.Pinv || !s.gamma || !s.lambda || s.n == 0 || s.N == 0)
@@ -793,7 +904,16 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
         p->total_knots += s.N;
         p->descs.push_back(d);
         Shape sh;
-        rc = choose_shape(h->reg, p->f64, s.n, s.N, pinv_layout, *cfg, &sh, p->refine);
+        const TuneChoice *tc = nullptr;
+        TuneChoice tcv;
+        if (use_table) {
+            auto tt = h->tune.find(tune_key(p.get(), adjoint, s.n, s.N));
+            if (tt != h->tune.end()) {
+                tcv = tt->second;
+                tc = &tcv;
+            }
+        }
+        rc = choose_shape(h->reg, p->f64, s.n, s.N, pinv_layout, *cfg, &sh, p->refine, tc);
         if (rc) return rc;
         if (sh.plain) {
             if (adjoint) return fail(GBDPCG_ERR_UNSUPPORTED, "adjoint needs n <= 32");
@@ -812,39 +932,15 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
         pc.items.push_back(i);
         pc.kmax = std::max(pc.kmax, sh.K);
     }
-    // longest first within a class; classes with the most work first
-    auto cost = [&](uint32_t i) { return (double)p->descs[i].n * p->descs[i].n * p->descs[i].N; };
-    for (auto &pc : p->classes)
-        std::stable_sort(pc.items.begin(), pc.items.end(),
-                         [&](uint32_t a, uint32_t b) { return cost(a) > cost(b); });
-    std::stable_sort(p->classes.begin(), p->classes.end(),
-                     [&](const PlanClass &a, const PlanClass &b) {
-                         return cost(a.items[0]) > cost(b.items[0]);
-                     });
-    std::vector<uint32_t> order;
-    for (auto &pc : p->classes) {
-        pc.order_off = (uint32_t)order.size();
-        order.insert(order.end(), pc.items.begin(), pc.items.end());
-        int active = 0;
-        rc = max_active_clusters(pc.sh, pc.sh.vi->v.smem_bytes(pc.kmax, pc.sh.C, pc.sh.threads / 32), &active);
-        if (rc) return rc;
-        if (active <= 0)
-            return fail(GBDPCG_ERR_UNSUPPORTED, "cluster shape cannot be scheduled (C=" +
-                                                    std::to_string(pc.sh.C) + ")");
-        pc.grid_clusters = std::min<uint32_t>((uint32_t)pc.items.size(), (uint32_t)active);
-    }
-    const size_t nc = p->classes.size();
+    tune_lock.unlock();
     if ((rc = p->d_descs.ensure(sizeof(SysDesc) * count))) return rc;
-    if ((rc = p->d_order.ensure(sizeof(uint32_t) * std::max<size_t>(1, order.size())))) return rc;
-    if ((rc = p->d_queues.ensure(sizeof(uint32_t) * std::max<size_t>(1, nc)))) return rc;
     if ((rc = p->d_results.ensure(sizeof(SysResult) * count))) return rc;
     if ((rc = p->d_prefix.ensure(sizeof(uint64_t) * count))) return rc;
     GB_CUDA(cudaMemcpy(p->d_descs.p, p->descs.data(), sizeof(SysDesc) * count, cudaMemcpyHostToDevice));
-    if (!order.empty())
-        GB_CUDA(cudaMemcpy(p->d_order.p, order.data(), sizeof(uint32_t) * order.size(),
-                           cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(p->d_prefix.p, prefix.data(), sizeof(uint64_t) * count, cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemset(p->d_results.p, 0, sizeof(SysResult) * count));
+    if ((rc = plan_layout(p.get()))) return rc;
+    const size_t nc = p->classes.size();
     const uint32_t ns = (uint32_t)std::min<size_t>(std::max<uint32_t>(1, std::min<uint32_t>(cfg->streams, 32)),
                                                    std::max<size_t>(1, nc));
     for (uint32_t s = 0; s < ns; ++s) {
@@ -1006,10 +1102,303 @@ int gbdpcg_plan_launch_info(gbdpcg_plan_t p, uint32_t i, uint32_t *cluster, uint
     return GBDPCG_SUCCESS;
 }
 
+int gbdpcg_plan_launch_kernel(gbdpcg_plan_t p, uint32_t i, uint32_t *storage, uint32_t *rows_per_thread,
+                              uint32_t *algorithm) {
+    if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (i < p->classes.size()) {
+        const KernelVariant &v = p->classes[i].sh.vi->v;
+        if (storage) *storage = (uint32_t)v.st;
+        if (rows_per_thread) *rows_per_thread = (uint32_t)v.rpt;
+        if (algorithm)
+            *algorithm = v.alg == 1 ? GBDPCG_ALGO_SINGLE_REDUCTION
+                         : v.alg == 3 ? GBDPCG_ALGO_RECURRENCE
+                         : v.alg == 0 ? GBDPCG_ALGO_CLUSTER
+                                      : 0u;
+        return GBDPCG_SUCCESS;
+    }
+    if (i - p->classes.size() >= p->plain_items.size()) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "launch index");
+    if (storage) *storage = 2;
+    if (rows_per_thread) *rows_per_thread = 1;
+    if (algorithm) *algorithm = GBDPCG_ALGO_PLAIN;
+    return GBDPCG_SUCCESS;
+}
+
 int gbdpcg_plan_destroy(gbdpcg_plan_t p) {
     if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
     HandleScope scope(p->h->device);
     delete p;
+    return GBDPCG_SUCCESS;
+}
+
+// ------------------------------------------------------------------ autotuner
+namespace {
+
+struct Candidate {
+    Shape sh;
+    uint32_t kmax = 0, grid = 0;
+};
+
+// Launch shapes that hold every system of `items` with the variant family of
+// `base` (precision, NP, Phi^-1 layout), honouring the config's storage,
+// cluster-size and CTA-size requests.
+std::vector<Candidate> tune_candidates(gbdpcg_plan_s *p, const PlanClass &base,
+                                       const std::vector<uint32_t> &items, uint32_t flags) {
+    std::vector<Candidate> out;
+    Registry *reg = p->h->reg;
+    const KernelVariant &bv = base.sh.vi->v;
+    std::vector<int> algs = {bv.alg};
+    if ((flags & GBDPCG_TUNE_RECURRENCE) && p->cfg.algorithm == GBDPCG_ALGO_AUTO && bv.alg == 0)
+        algs.push_back(3);
+    if ((flags & GBDPCG_TUNE_SINGLE_REDUCTION) && p->cfg.algorithm == GBDPCG_ALGO_AUTO && bv.alg == 0 && !bv.ptri)
+        algs.push_back(1);
+    const int want_st = p->cfg.storage == GBDPCG_STORAGE_REGISTERS ? 0
+                        : p->cfg.storage == GBDPCG_STORAGE_SHARED  ? 2
+                        : p->cfg.storage == GBDPCG_STORAGE_SPLIT   ? 1
+                                                                   : -1;
+    static const uint32_t kC[] = {1, 2, 3, 4, 5, 6, 7, 8, 16};
+    for (auto &vi : reg->list) {
+        const KernelVariant &v = vi.v;
+        if (v.f64 != bv.f64 || v.acc64 != bv.acc64 || v.np != bv.np || v.ptri != bv.ptri) continue;
+        if (std::find(algs.begin(), algs.end(), v.alg) == algs.end()) continue;
+        if (want_st >= 0 && v.st != want_st) continue;
+        bool rows_ok = true;
+        for (uint32_t i : items) rows_ok &= p->descs[i].n % v.rpt == 0;
+        if (!rows_ok) continue;
+        uint32_t cap = std::min<uint32_t>((uint32_t)vi.max_threads,
+                                          p->cfg.max_threads ? p->cfg.max_threads : 1024u);
+        for (uint32_t C : kC) {
+            if (p->cfg.cluster_size && C != p->cfg.cluster_size) continue;
+            uint32_t kmax = 0, thr = 0;
+            bool ok = true;
+            for (uint32_t i : items) {
+                const uint32_t n = p->descs[i].n, N = p->descs[i].N;
+                const uint32_t K = (N + C - 1) / C;
+                ok &= N > (C - 1) * K;  // every CTA of the cluster owns a knot
+                kmax = std::max(kmax, K);
+                thr = std::max(thr, (K * n + v.rpt - 1) / v.rpt);
+            }
+            const uint32_t threads = (thr + 31) / 32 * 32;
+            if (!ok || threads > cap) continue;
+            if (v.smem_bytes(kmax, C, threads / 32) > (size_t)reg->max_smem_optin) continue;
+            Candidate cd;
+            cd.sh.vi = &vi;
+            cd.sh.C = C;
+            cd.sh.K = kmax;
+            cd.sh.threads = threads;
+            cd.kmax = kmax;
+            int active = 0;
+            if (max_active_clusters(cd.sh, v.smem_bytes(kmax, C, threads / 32), &active) != GBDPCG_SUCCESS) {
+                cudaGetLastError();
+                continue;
+            }
+            if (active <= 0) continue;
+            cd.grid = std::min<uint32_t>((uint32_t)items.size(), (uint32_t)active);
+            out.push_back(cd);
+        }
+    }
+    return out;
+}
+
+}  // namespace
+
+int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_stream_t stream_) {
+    if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (flags & ~(uint32_t)(GBDPCG_TUNE_RECURRENCE | GBDPCG_TUNE_SINGLE_REDUCTION))
+        return fail(GBDPCG_ERR_INVALID_ARGUMENT, "unknown tune flag");
+    if (p->classes.empty()) return GBDPCG_SUCCESS;
+    HandleScope scope(p->h->device);
+    cudaStream_t st = (cudaStream_t)stream_;
+    if (reps == 0) reps = 2;
+    const bool adjoint = (p->descs[0].flags & SYS_ADJOINT) != 0;
+    const size_t sv = (p->f64 || p->refine) ? 8 : 4;  // lambda element (refinement: double)
+    const size_t sS = p->f64 ? 8 : 4;                 // dS element (adjoint: the plan's type)
+    // scratch for the largest class: lambda (and dS) of each of its systems
+    size_t need = 0;
+    for (auto &pc : p->classes) {
+        size_t b = 0;
+        for (uint32_t i : pc.items) {
+            const size_t n = p->descs[i].n, N = p->descs[i].N;
+            b += round_up(n * N * sv, 256) + (adjoint ? round_up(3 * n * n * N * sS, 256) : 0);
+        }
+        need = std::max(need, b);
+    }
+    DevBuf scratch, d_td, d_ord, d_q, d_res;
+    int rc;
+    if ((rc = scratch.ensure(std::max<size_t>(need, 256)))) return rc;
+    if ((rc = d_td.ensure(sizeof(SysDesc) * p->count))) return rc;
+    if ((rc = d_ord.ensure(sizeof(uint32_t) * p->count))) return rc;
+    if ((rc = d_q.ensure(sizeof(uint32_t)))) return rc;
+    if ((rc = d_res.ensure(sizeof(SysResult) * p->count))) return rc;
+    cudaEvent_t e0, e1;
+    GB_CUDA(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        GB_CUDA(ce);
+    }
+    struct Events {
+        cudaEvent_t a, b;
+        ~Events() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } ev{e0, e1};
+
+    std::vector<SysDesc> td = p->descs;
+    std::vector<std::pair<TuneKey, TuneChoice>> learned;
+    for (auto &pc : p->classes) {
+        // this class's systems solve from zero into the scratch buffers
+        size_t off = 0;
+        char *base = scratch.as<char>();
+        for (uint32_t i : pc.items) {
+            SysDesc &d = td[i];
+            const size_t n = d.n, N = d.N;
+            d.lambda = base + off;
+            d.lambda0 = nullptr;
+            d.flags |= SYS_LAMBDA0_ZERO;
+            off += round_up(n * N * sv, 256);
+            if (adjoint) {
+                d.dS = base + off;
+                off += round_up(3 * n * n * N * sS, 256);
+            }
+        }
+        GB_CUDA(cudaMemcpyAsync(d_td.p, td.data(), sizeof(SysDesc) * p->count, cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemcpyAsync(d_ord.p, pc.items.data(), sizeof(uint32_t) * pc.items.size(),
+                                cudaMemcpyHostToDevice, st));
+        auto time_shape = [&](const Shape &sh, uint32_t kmax, uint32_t grid, float *ms) -> int {
+            LaunchParams lp;
+            memset(&lp, 0, sizeof(lp));
+            lp.descs = d_td.as<SysDesc>();
+            lp.order = d_ord.as<uint32_t>();
+            lp.count = (uint32_t)pc.items.size();
+            lp.kmax = kmax;
+            lp.queue = d_q.as<uint32_t>();
+            lp.results = d_res.as<SysResult>();
+            float best = 1e30f;
+            for (uint32_t r = 0; r <= reps; ++r) {
+                GB_CUDA(cudaMemsetAsync(d_q.p, 0, sizeof(uint32_t), st));
+                GB_CUDA(cudaEventRecord(e0, st));
+                int lrc = launch_cluster(sh, lp, grid, st);
+                if (lrc) return lrc;
+                GB_CUDA(cudaEventRecord(e1, st));
+                GB_CUDA(cudaEventSynchronize(e1));
+                float t = 0;
+                GB_CUDA(cudaEventElapsedTime(&t, e0, e1));
+                if (r > 0) best = std::min(best, t);
+            }
+            *ms = best;
+            return GBDPCG_SUCCESS;
+        };
+        float best_ms = 0;
+        if ((rc = time_shape(pc.sh, pc.kmax, pc.grid_clusters, &best_ms))) return rc;
+        Candidate best;
+        best.sh = pc.sh;
+        best.kmax = pc.kmax;
+        best.grid = pc.grid_clusters;
+        for (const Candidate &cd : tune_candidates(p, pc, pc.items, flags)) {
+            if (cd.sh.vi == pc.sh.vi && cd.sh.C == pc.sh.C && cd.sh.threads == pc.sh.threads) continue;
+            float ms = 0;
+            if (time_shape(cd.sh, cd.kmax, cd.grid, &ms) != GBDPCG_SUCCESS) {
+                // a shape the launch rejects is skipped (launch errors are not
+                // sticky); anything that leaves the stream failing ends tuning
+                cudaGetLastError();
+                GB_CUDA(cudaStreamSynchronize(st));
+                continue;
+            }
+            if (ms < best_ms * 0.98f) {
+                best_ms = ms;
+                best = cd;
+            }
+        }
+        pc.sh = best.sh;
+        pc.kmax = best.kmax;
+        TuneChoice ch{best.sh.vi->v.st, best.sh.vi->v.rpt, best.sh.vi->v.alg, best.sh.C, best.sh.threads};
+        for (uint32_t i : pc.items) learned.emplace_back(tune_key(p, adjoint, p->descs[i].n, p->descs[i].N), ch);
+        for (uint32_t i : pc.items) td[i] = p->descs[i];
+    }
+    GB_CUDA(cudaStreamSynchronize(st));
+    {
+        std::lock_guard<std::mutex> lk(p->h->tune_mu);
+        for (auto &kv : learned) p->h->tune[kv.first] = kv.second;
+    }
+    return plan_layout(p);
+}
+
+int gbdpcg_tune_export(gbdpcg_handle_t h, char *buffer, size_t capacity, size_t *length) {
+    if (!h || !length || (capacity && !buffer)) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    std::string s;
+    {
+        std::lock_guard<std::mutex> lk(h->tune_mu);
+        char line[160];
+        for (auto &kv : h->tune) {
+            const TuneKey &k = kv.first;
+            const TuneChoice &c = kv.second;
+            snprintf(line, sizeof(line), "%u %u %u %u %u %u %u %u %u : %d %d %d %u %u\n", k.f64, k.refine,
+                     k.acc64, k.ptri, k.adjoint, k.alg_req, k.storage_req, k.n, k.N, c.st, c.rpt, c.alg, c.C,
+                     c.threads);
+            s += line;
+        }
+    }
+    *length = s.size();
+    if (capacity) {
+        const size_t m = std::min(capacity - 1, s.size());
+        memcpy(buffer, s.data(), m);
+        buffer[m] = 0;
+    }
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_tune_import(gbdpcg_handle_t h, const char *text) {
+    if (!h || !text) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    std::vector<std::pair<TuneKey, TuneChoice>> add;
+    const char *p = text;
+    uint32_t lineno = 0;
+    while (*p) {
+        const char *e = strchr(p, '\n');
+        std::string line = e ? std::string(p, e - p) : std::string(p);
+        p = e ? e + 1 : p + line.size();
+        ++lineno;
+        if (line.find_first_not_of(" \t\r") == std::string::npos) continue;
+        unsigned f[9];
+        int st, rpt, alg;
+        unsigned C, thr;
+        char colon = 0;
+        if (sscanf(line.c_str(), "%u %u %u %u %u %u %u %u %u %c %d %d %d %u %u", &f[0], &f[1], &f[2], &f[3],
+                   &f[4], &f[5], &f[6], &f[7], &f[8], &colon, &st, &rpt, &alg, &C, &thr) != 15 ||
+            colon != ':')
+            return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno) + " is malformed");
+        for (int i = 0; i < 5; ++i)
+            if (f[i] > 1) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno));
+        if (f[5] > GBDPCG_ALGO_RECURRENCE || f[6] > GBDPCG_STORAGE_SPLIT || f[7] == 0 || f[8] == 0 || C == 0 ||
+            C > 16 || thr == 0 || thr > 1024 || thr % 32)
+            return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno));
+        const int np = np_for(f[7]);
+        const bool f64v = f[0] && !f[1];
+        if (!np || !find_variant(h->reg, f64v, f[2] != 0, np, f[3] != 0, st, rpt, alg))
+            return fail(GBDPCG_ERR_UNSUPPORTED, "tuning table line " + std::to_string(lineno) +
+                                                    " names a kernel variant this build lacks");
+        TuneKey k;
+        memset(&k, 0, sizeof(k));
+        k.f64 = (uint8_t)f[0];
+        k.refine = (uint8_t)f[1];
+        k.acc64 = (uint8_t)f[2];
+        k.ptri = (uint8_t)f[3];
+        k.adjoint = (uint8_t)f[4];
+        k.alg_req = (uint8_t)f[5];
+        k.storage_req = (uint8_t)f[6];
+        k.n = f[7];
+        k.N = f[8];
+        add.emplace_back(k, TuneChoice{st, rpt, alg, C, thr});
+    }
+    std::lock_guard<std::mutex> lk(h->tune_mu);
+    for (auto &kv : add) h->tune[kv.first] = kv.second;
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_tune_clear(gbdpcg_handle_t h) {
+    if (!h) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->tune_mu);
+    h->tune.clear();
     return GBDPCG_SUCCESS;
 }
 

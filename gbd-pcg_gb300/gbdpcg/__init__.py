@@ -28,6 +28,7 @@ CONVERGED, MAX_ITER, BREAKDOWN, REJECTED = 0, 1, 2, -1
 EXIT_REFERENCE, EXIT_RELRES = 0, 1
 PINV_CBTD, PINV_BLOCKDIAG = 0, 1
 ALGO_AUTO, ALGO_CLUSTER, ALGO_PLAIN, ALGO_SINGLE_REDUCTION, ALGO_RECURRENCE = 0, 1, 2, 3, 4
+TUNE_RECURRENCE, TUNE_SINGLE_REDUCTION = 1, 2
 DOT_NATIVE, DOT_FP64 = 0, 1
 STORAGE_AUTO, STORAGE_REGISTERS, STORAGE_SHARED, STORAGE_SPLIT = 0, 1, 2, 3
 
@@ -96,7 +97,12 @@ _SIGS = {
     "gbdpcg_plan_results": ([_P, _P, _P], _I),
     "gbdpcg_plan_launch_count": ([_P, _P], _I),
     "gbdpcg_plan_launch_info": ([_P, _U, _P, _P, _P, _P, _P], _I),
+    "gbdpcg_plan_launch_kernel": ([_P, _U, _P, _P, _P], _I),
     "gbdpcg_plan_destroy": ([_P], _I),
+    "gbdpcg_plan_autotune": ([_P, _U, _U, _P], _I),
+    "gbdpcg_tune_export": ([_P, _P, ctypes.c_size_t, _P], _I),
+    "gbdpcg_tune_import": ([_P, ctypes.c_char_p], _I),
+    "gbdpcg_tune_clear": ([_P], _I),
 }
 
 _lib = None
@@ -238,6 +244,20 @@ class Handle:
                                              _stream(stream)), "gbdpcg_refine_solve_dev")
         return r if sync else None
 
+    def tune_export(self) -> str:
+        """The handle's tuning table as text."""
+        n = ctypes.c_size_t()
+        _check(lib().gbdpcg_tune_export(self.h, None, 0, ctypes.byref(n)), "gbdpcg_tune_export")
+        buf = ctypes.create_string_buffer(n.value + 1)
+        _check(lib().gbdpcg_tune_export(self.h, buf, n.value + 1, ctypes.byref(n)), "gbdpcg_tune_export")
+        return buf.value.decode()
+
+    def tune_import(self, text: str):
+        _check(lib().gbdpcg_tune_import(self.h, text.encode()), "gbdpcg_tune_import")
+
+    def tune_clear(self):
+        _check(lib().gbdpcg_tune_clear(self.h), "gbdpcg_tune_clear")
+
     def adjoint(self, S, Pinv, lam, grad_lam, grad_gamma, grad_S, n, N, layout=PINV_CBTD, cfg=None,
                 stream=None, sync=True):
         cfg = cfg or config()
@@ -313,8 +333,19 @@ class Plan:
             v = [ctypes.c_uint32() for _ in range(5)]
             _check(lib().gbdpcg_plan_launch_info(self.p, i, *[ctypes.byref(x) for x in v]),
                    "gbdpcg_plan_launch_info")
-            out.append(dict(zip(("cluster", "threads", "kmax", "systems", "ctas"), [x.value for x in v])))
+            d = dict(zip(("cluster", "threads", "kmax", "systems", "ctas"), [x.value for x in v]))
+            k = [ctypes.c_uint32() for _ in range(3)]
+            _check(lib().gbdpcg_plan_launch_kernel(self.p, i, *[ctypes.byref(x) for x in k]),
+                   "gbdpcg_plan_launch_kernel")
+            d.update(zip(("storage", "rows_per_thread", "algorithm"), [x.value for x in k]))
+            out.append(d)
         return out
+
+    def autotune(self, flags=0, reps=0, stream=None):
+        """Times each launch class's candidate shapes on the plan's systems and
+        keeps the fastest (see gbdpcg_plan_autotune); returns launches()."""
+        _check(lib().gbdpcg_plan_autotune(self.p, flags, reps, _stream(stream)), "gbdpcg_plan_autotune")
+        return self.launches()
 
     def close(self):
         if self.p:

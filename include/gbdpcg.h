@@ -280,7 +280,44 @@ GBDPCG_API int gbdpcg_plan_launch_count(gbdpcg_plan_t plan, uint32_t *launches);
 /* Describes launch i: cluster size, threads per CTA, knots per CTA, systems, CTAs in the grid. */
 GBDPCG_API int gbdpcg_plan_launch_info(gbdpcg_plan_t plan, uint32_t i, uint32_t *cluster, uint32_t *threads,
                             uint32_t *kmax, uint32_t *systems, uint32_t *ctas);
+/* Kernel of launch i: storage (0 S and Phi^-1 in registers, 1 S in registers
+ * and Phi^-1 in shared memory, 2 both in shared memory), matrix rows per
+ * thread, and algorithm (GBDPCG_ALGO_CLUSTER, _SINGLE_REDUCTION, _RECURRENCE,
+ * or _PLAIN for a one-system plain launch; refinement launches report 0). */
+GBDPCG_API int gbdpcg_plan_launch_kernel(gbdpcg_plan_t plan, uint32_t i, uint32_t *storage,
+                                         uint32_t *rows_per_thread, uint32_t *algorithm);
 GBDPCG_API int gbdpcg_plan_destroy(gbdpcg_plan_t plan);
+
+/* Autotuner (no reference counterpart: the reference fixes 64 threads per CTA
+ * and one CTA per knot).  For every launch class of the plan it times, on the
+ * plan's own systems, the class alone with each launch shape that holds all
+ * of its systems — Phi^-1/S storage (registers, shared memory, split), rows
+ * per thread, cluster size C (1-8, 16; every CTA owns at least one knot),
+ * CTA size rounded to a warp — and keeps the fastest (a change must win by
+ * more than 2%).  Classes that end up with the same shape are merged and the
+ * plan's graph is rebuilt on its next execution.  Tuning solves from a zero
+ * initial guess into scratch buffers: the plan's lambda, dS and results are
+ * not written.  The choices are also stored in the handle's tuning table,
+ * which later plans of the same handle use for systems of the same (n, N),
+ * precision, Phi^-1 layout, algorithm and storage request when the config
+ * leaves cluster_size and max_threads at 0.  `flags`: GBDPCG_TUNE_* bits.
+ * `reps` timed launches per shape (0 means 2).  Synchronous. */
+enum {
+    GBDPCG_TUNE_RECURRENCE = 1,      /* with GBDPCG_ALGO_AUTO also try the recurrence form */
+    GBDPCG_TUNE_SINGLE_REDUCTION = 2 /* with GBDPCG_ALGO_AUTO and a compact Phi^-1 also try the
+                                        single-reduction (Chronopoulos-Gear) form */
+};
+GBDPCG_API int gbdpcg_plan_autotune(gbdpcg_plan_t plan, uint32_t flags, uint32_t reps, gbdpcg_stream_t stream);
+/* The handle's tuning table as text, one line per (n, N) entry:
+ * "f64 refine acc64 ptri adjoint algorithm storage n N : st rpt alg C threads".
+ * Writes at most `capacity` bytes including the terminating NUL and sets
+ * *length to the full length without the NUL (call with capacity 0 to size). */
+GBDPCG_API int gbdpcg_tune_export(gbdpcg_handle_t h, char *buffer, size_t capacity, size_t *length);
+/* Adds the entries of a text produced by gbdpcg_tune_export (replacing equal
+ * keys).  Entries naming a kernel variant this build lacks are rejected. */
+GBDPCG_API int gbdpcg_tune_import(gbdpcg_handle_t h, const char *text);
+/* Empties the handle's tuning table. */
+GBDPCG_API int gbdpcg_tune_clear(gbdpcg_handle_t h);
 
 #ifdef __cplusplus
 }

@@ -293,25 +293,34 @@ def precision_config(gbdpcg, h, dev, count=256, n=24, N=256, workers=8):
     S64 = [torch.from_numpy(S).to(dev) for S, g in syss]
     g64 = [torch.from_numpy(g).to(dev) for S, g in syss]
     out = {"systems": count, "n": n, "N": N, "target_relres": 1e-10}
-    # FP32 + FP64 refinement: one plan, dtype 2
-    systems = [{"S": S64[i], "Pinv": torch.empty(n * n * N, dtype=torch.float32, device=dev), "gamma": g64[i],
-                "lambda": torch.zeros(n * N, dtype=torch.float64, device=dev), "n": n, "N": N} for i in range(count)]
-    cfg = gbdpcg.config(exit_mode=gbdpcg.EXIT_RELRES, exit_tol=1e-10, max_iter=40000, max_outer=60, zero_guess=1)
-    pr = gbdpcg.Plan(h, systems, gbdpcg.PINV_BLOCKDIAG, cfg, dtype=2)
-    pr.build_block_jacobi()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    pr.execute()
-    e1.record()
-    e1.synchronize()
-    rr = pr.results()
-    out["refined"] = {"ms": e0.elapsed_time(e1), "converged": sum(r.status == 0 for r in rr),
-                      "inner_iters_mean": float(np.mean([r.iters for r in rr])),
-                      "outer_mean": float(np.mean([r.outer for r in rr])),
-                      "relres_max": float(max(r.relres for r in rr))}
-    lam_ref = [s["lambda"] for s in systems]
-    pr.close()
+    # FP32 + FP64 refinement: one plan, dtype 2; inner dots in FP64, then in float-float
+    for key, dot in (("refined", gbdpcg.DOT_FP64), ("refined_float2", gbdpcg.DOT_FLOAT2)):
+        systems = [{"S": S64[i], "Pinv": torch.empty(n * n * N, dtype=torch.float32, device=dev),
+                    "gamma": g64[i], "lambda": torch.zeros(n * N, dtype=torch.float64, device=dev),
+                    "n": n, "N": N} for i in range(count)]
+        cfg = gbdpcg.config(exit_mode=gbdpcg.EXIT_RELRES, exit_tol=1e-10, max_iter=40000, max_outer=60,
+                            zero_guess=1, dot_precision=dot)
+        pr = gbdpcg.Plan(h, systems, gbdpcg.PINV_BLOCKDIAG, cfg, dtype=2)
+        pr.build_block_jacobi()
+        pr.execute()  # warm (the graph is captured on the first execution)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        pr.execute()
+        e1.record()
+        e1.synchronize()
+        rr = pr.results()
+        out[key] = {"ms": e0.elapsed_time(e1), "converged": sum(r.status == 0 for r in rr),
+                    "inner_dots": "fp64" if dot == gbdpcg.DOT_FP64 else "float-float",
+                    "inner_iters_mean": float(np.mean([r.iters for r in rr])),
+                    "outer_mean": float(np.mean([r.outer for r in rr])),
+                    "relres_max": float(max(r.relres for r in rr))}
+        lam = [s["lambda"] for s in systems]
+        # true FP64 relative residual of the refined solutions, recomputed on the host
+        out[key]["true_relres_fp64_max_sample"] = max(
+            relres64(syss[i][0], syss[i][1], lam[i].cpu().numpy(), n, N)
+            for i in range(0, count, max(1, count // 16)))
+        pr.close()
     # plain FP64 PCG (the reference scheme: cbtd Phi^-1, one cooperative launch per system)
     t64, it64, conv64 = 0.0, [], 0
     nsamp = min(count, 32)
@@ -332,11 +341,8 @@ def precision_config(gbdpcg, h, dev, count=256, n=24, N=256, workers=8):
     out["fp64_pcg"] = {"ms_for_batch_extrapolated": t64 / nsamp * count, "sample": nsamp, "converged": conv64,
                        "iters_mean": float(np.mean(it64)),
                        "how": "best FP64 path that holds n=24, N=256: one cooperative launch per system"}
-    out["speedup_refined_vs_fp64"] = out["fp64_pcg"]["ms_for_batch_extrapolated"] / out["refined"]["ms"]
-    # true FP64 relative residual of the refined solutions, recomputed on the host
-    out["refined"]["true_relres_fp64_max_sample"] = max(
-        relres64(syss[i][0], syss[i][1], lam_ref[i].cpu().numpy(), n, N)
-        for i in range(0, count, max(1, count // 16)))
+    for key in ("refined", "refined_float2"):
+        out["speedup_" + key + "_vs_fp64"] = out["fp64_pcg"]["ms_for_batch_extrapolated"] / out[key]["ms"]
     return out
 
 

@@ -90,8 +90,11 @@ int get_registry(int device, Registry **out) {
     }
     auto reg = std::make_unique<Registry>();
     KernelVariant buf[kMaxVariantsPerNP];
-    int (*fns[])(KernelVariant *) = {variants_np6, variants_np8, variants_np12, variants_np14,
-                                     variants_np16, variants_np24, variants_np32};
+    int (*fns[])(KernelVariant *) = {variants_np6,      variants_np8,      variants_np12,
+                                     variants_np14,     variants_np16,     variants_np24,
+                                     variants_np32,     variants_np6_ext,  variants_np8_ext,
+                                     variants_np12_ext, variants_np14_ext, variants_np16_ext,
+                                     variants_np24_ext, variants_np32_ext};
     for (auto fn : fns) {
         const int c = fn(buf);
         for (int i = 0; i < c; ++i) {
@@ -112,10 +115,12 @@ int get_registry(int device, Registry **out) {
     return GBDPCG_SUCCESS;
 }
 
-VariantInfo *find_variant(Registry *reg, bool f64, bool acc64, int np, bool ptri, int st, int rpt,
+// acc: dot accumulation of FP32 systems (0 float, 1 double, 2 float-float);
+// FP64 systems always accumulate in double.
+VariantInfo *find_variant(Registry *reg, bool f64, int acc, int np, bool ptri, int st, int rpt,
                           int alg) {
     for (auto &vi : reg->list)
-        if (vi.v.f64 == (int)f64 && vi.v.acc64 == (int)(acc64 || f64) && vi.v.np == np &&
+        if (vi.v.f64 == (int)f64 && vi.v.acc == (f64 ? 1 : acc) && vi.v.np == np &&
             vi.v.ptri == (int)ptri && vi.v.st == st && vi.v.rpt == rpt && vi.v.alg == alg)
             return &vi;
     return nullptr;
@@ -162,11 +167,11 @@ struct DevBuf {
 // Phi^-1 layout, adjoint epilogue, the requested algorithm and storage) and
 // the system size.  Value: the launch shape the autotuner measured fastest.
 struct TuneKey {
-    uint8_t f64, refine, acc64, ptri, adjoint, alg_req, storage_req;
+    uint8_t f64, refine, acc, ptri, adjoint, alg_req, storage_req;
     uint32_t n, N;
     bool operator<(const TuneKey &o) const {
-        return std::tie(f64, refine, acc64, ptri, adjoint, alg_req, storage_req, n, N) <
-               std::tie(o.f64, o.refine, o.acc64, o.ptri, o.adjoint, o.alg_req, o.storage_req, o.n, o.N);
+        return std::tie(f64, refine, acc, ptri, adjoint, alg_req, storage_req, n, N) <
+               std::tie(o.f64, o.refine, o.acc, o.ptri, o.adjoint, o.alg_req, o.storage_req, o.n, o.N);
     }
 };
 
@@ -200,10 +205,10 @@ std::vector<Pref> storage_prefs(bool f64, bool ptri, uint32_t storage) {
 }
 
 // A tuned shape for one system, if its variant exists and holds the system.
-bool tuned_shape(Registry *reg, bool f64, bool acc64, int np, bool ptri, uint32_t n, uint32_t N,
+bool tuned_shape(Registry *reg, bool f64, int acc, int np, bool ptri, uint32_t n, uint32_t N,
                  const TuneChoice &tc, Shape *out) {
     if (tc.rpt < 1 || n % tc.rpt || tc.C < 1 || tc.C > 16 || tc.threads == 0 || tc.threads % 32) return false;
-    VariantInfo *vi = find_variant(reg, f64, acc64, np, ptri, tc.st, tc.rpt, tc.alg);
+    VariantInfo *vi = find_variant(reg, f64, acc, np, ptri, tc.st, tc.rpt, tc.alg);
     if (!vi) return false;
     const uint32_t K = (N + tc.C - 1) / tc.C;
     const uint32_t thr = (K * n + tc.rpt - 1) / tc.rpt;
@@ -215,6 +220,14 @@ bool tuned_shape(Registry *reg, bool f64, bool acc64, int np, bool ptri, uint32_
     out->threads = tc.threads;
     out->plain = false;
     return true;
+}
+
+// Dot accumulation of a launch: FP64 systems in double; refinement's inner
+// solve in double unless float-float is asked for; FP32 systems as configured.
+int acc_kind(bool f64_system, bool refine, uint32_t dot_precision) {
+    if (f64_system) return 1;
+    if (refine) return dot_precision == GBDPCG_DOT_FLOAT2 ? 2 : 1;
+    return (int)dot_precision;
 }
 
 int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layout,
@@ -235,16 +248,18 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
         return GBDPCG_SUCCESS;
     }
     const bool ptri = layout == GBDPCG_PINV_CBTD;
-    const bool acc64 = refine || cfg.dot_precision == GBDPCG_DOT_FP64;
+    const int acc = acc_kind(f64 && !refine, refine, cfg.dot_precision);
     const int alg = refine ? 2
                            : (cfg.algorithm == GBDPCG_ALGO_SINGLE_REDUCTION ? 1
                                                                              : (cfg.algorithm == GBDPCG_ALGO_RECURRENCE ? 3 : 0));
     if (alg == 1 && ptri)
         return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm needs a block-diagonal Phi^-1");
-    if (tuned && tuned_shape(reg, f64 && !refine, acc64, np, ptri, n, N, *tuned, out)) return GBDPCG_SUCCESS;
+    if (alg == 1 && acc == 2)
+        return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm has no float-float accumulation");
+    if (tuned && tuned_shape(reg, f64 && !refine, acc, np, ptri, n, N, *tuned, out)) return GBDPCG_SUCCESS;
     for (const Pref &pf : storage_prefs(f64 && !refine, ptri, cfg.storage)) {
         if (pf.rpt > 1 && (n % pf.rpt) != 0) continue;
-        VariantInfo *vi = find_variant(reg, f64 && !refine, acc64, np, ptri, pf.st, pf.rpt, alg);
+        VariantInfo *vi = find_variant(reg, f64 && !refine, acc, np, ptri, pf.st, pf.rpt, alg);
         if (!vi) continue;
         uint32_t cap = cfg.max_threads ? cfg.max_threads : (uint32_t)vi->max_threads;
         cap = std::min<uint32_t>(cap, (uint32_t)vi->max_threads);
@@ -350,7 +365,7 @@ SysDesc make_desc(const void *S, const void *P, const void *g, const void *l0, v
 int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
     if (!cfg) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "config is NULL");
     if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad pinv_layout");
-    if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FP64 ||
+    if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FLOAT2 ||
         cfg->algorithm > GBDPCG_ALGO_RECURRENCE || cfg->storage > GBDPCG_STORAGE_SPLIT ||
         cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1 ||
         !(cfg->inner_tol >= 0) || cfg->inner_tol >= 1)
@@ -505,7 +520,7 @@ TuneKey tune_key(const gbdpcg_plan_s *p, bool adjoint, uint32_t n, uint32_t N) {
     memset(&k, 0, sizeof(k));
     k.f64 = p->f64;
     k.refine = p->refine;
-    k.acc64 = p->refine || p->cfg.dot_precision == GBDPCG_DOT_FP64;
+    k.acc = (uint8_t)acc_kind(p->f64, p->refine, p->cfg.dot_precision);
     k.ptri = p->layout == GBDPCG_PINV_CBTD;
     k.adjoint = adjoint;
     k.alg_req = (uint8_t)p->cfg.algorithm;
@@ -1158,7 +1173,7 @@ std::vector<Candidate> tune_candidates(gbdpcg_plan_s *p, const PlanClass &base,
     static const uint32_t kC[] = {1, 2, 3, 4, 5, 6, 7, 8, 16};
     for (auto &vi : reg->list) {
         const KernelVariant &v = vi.v;
-        if (v.f64 != bv.f64 || v.acc64 != bv.acc64 || v.np != bv.np || v.ptri != bv.ptri) continue;
+        if (v.f64 != bv.f64 || v.acc != bv.acc || v.np != bv.np || v.ptri != bv.ptri) continue;
         if (std::find(algs.begin(), algs.end(), v.alg) == algs.end()) continue;
         if (want_st >= 0 && v.st != want_st) continue;
         bool rows_ok = true;
@@ -1334,7 +1349,7 @@ int gbdpcg_tune_export(gbdpcg_handle_t h, char *buffer, size_t capacity, size_t 
             const TuneKey &k = kv.first;
             const TuneChoice &c = kv.second;
             snprintf(line, sizeof(line), "%u %u %u %u %u %u %u %u %u : %d %d %d %u %u\n", k.f64, k.refine,
-                     k.acc64, k.ptri, k.adjoint, k.alg_req, k.storage_req, k.n, k.N, c.st, c.rpt, c.alg, c.C,
+                     k.acc, k.ptri, k.adjoint, k.alg_req, k.storage_req, k.n, k.N, c.st, c.rpt, c.alg, c.C,
                      c.threads);
             s += line;
         }
@@ -1368,20 +1383,21 @@ int gbdpcg_tune_import(gbdpcg_handle_t h, const char *text) {
             colon != ':')
             return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno) + " is malformed");
         for (int i = 0; i < 5; ++i)
-            if (f[i] > 1) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno));
+            if (f[i] > (i == 2 ? 2u : 1u))
+                return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno));
         if (f[5] > GBDPCG_ALGO_RECURRENCE || f[6] > GBDPCG_STORAGE_SPLIT || f[7] == 0 || f[8] == 0 || C == 0 ||
             C > 16 || thr == 0 || thr > 1024 || thr % 32)
             return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno));
         const int np = np_for(f[7]);
         const bool f64v = f[0] && !f[1];
-        if (!np || !find_variant(h->reg, f64v, f[2] != 0, np, f[3] != 0, st, rpt, alg))
+        if (!np || !find_variant(h->reg, f64v, (int)f[2], np, f[3] != 0, st, rpt, alg))
             return fail(GBDPCG_ERR_UNSUPPORTED, "tuning table line " + std::to_string(lineno) +
                                                     " names a kernel variant this build lacks");
         TuneKey k;
         memset(&k, 0, sizeof(k));
         k.f64 = (uint8_t)f[0];
         k.refine = (uint8_t)f[1];
-        k.acc64 = (uint8_t)f[2];
+        k.acc = (uint8_t)f[2];
         k.ptri = (uint8_t)f[3];
         k.adjoint = (uint8_t)f[4];
         k.alg_req = (uint8_t)f[5];

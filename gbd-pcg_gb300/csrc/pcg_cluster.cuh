@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "accum.cuh"
 #include "pcg_types.h"
 
 namespace gbdpcg {
@@ -208,7 +209,7 @@ __device__ __forceinline__ void stage_rows(TO *M, uint32_t R, const TI *__restri
 template <typename A>
 __device__ __forceinline__ A warp_sum(A v) {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    for (int off = 16; off > 0; off >>= 1) v += acc_shfl_xor(v, off);
     return v;
 }
 
@@ -220,7 +221,7 @@ __device__ __forceinline__ void warp_sum_n(A (&v)[NQ]) {
     for (int off = 16; off > 0; off >>= 1) {
         A t[NQ];
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) t[q] = __shfl_xor_sync(0xffffffffu, v[q], off);
+        for (int q = 0; q < NQ; ++q) t[q] = acc_shfl_xor(v[q], off);
 #pragma unroll
         for (int q = 0; q < NQ; ++q) v[q] += t[q];
     }
@@ -231,7 +232,14 @@ __device__ __forceinline__ void warp_sum_n(A (&v)[NQ]) {
 template <typename A>
 __device__ __forceinline__ A sum32(const A *p) {
     A c0 = A(0), c1 = A(0), c2 = A(0), c3 = A(0);
-    if constexpr (sizeof(A) == 4) {
+    if constexpr (std::is_same<A, f2acc>::value) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float4 t0 = reinterpret_cast<const float4 *>(p)[2 * j];
+            const float4 t1 = reinterpret_cast<const float4 *>(p)[2 * j + 1];
+            c0 += f2acc(t0.x, t0.y); c1 += f2acc(t0.z, t0.w); c2 += f2acc(t1.x, t1.y); c3 += f2acc(t1.z, t1.w);
+        }
+    } else if constexpr (sizeof(A) == 4) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const float4 t = reinterpret_cast<const float4 *>(p)[j];
@@ -298,6 +306,8 @@ __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, A *wscr,
         }
         warp_sum_n<A, NQ>(v);
     }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) v[q] = acc_normalize(v[q]);
 }
 
 __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uint32_t C) {
@@ -508,8 +518,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             A v2[2] = {A(0), A(0)};
 #pragma unroll
             for (int q = 0; q < RPT; ++q) {
-                v2[0] += A(r[q]) * A(z[q]);
-                v2[1] += A(gam[q]) * A(gam[q]);
+                acc_madd(v2[0], r[q], z[q]);
+                acc_madd(v2[1], gam[q], gam[q]);
             }
             cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
             eta = v2[0];
@@ -547,11 +557,11 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 {
                     A v1[1] = {A(0)};
 #pragma unroll
-                    for (int q = 0; q < RPT; ++q) v1[0] += A(p[q]) * A(y[q]);
+                    for (int q = 0; q < RPT; ++q) acc_madd(v1[0], p[q], y[q]);
                     cluster_allreduce<A, 1>(v1, slots, wscr, 0, cluster, C, rank);
                     pap = v1[0];
                 }
-                const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
+                const T alpha = (pap == A(0)) ? T(0) : acc_ratio<T>(eta, pap);
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
                     lam[q] = fma_rn(alpha, p[q], lam[q]);
@@ -592,17 +602,17 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                     A v2[2] = {A(0), A(0)};
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) {
-                        v2[0] += A(r[q]) * A(z[q]);
-                        if (relres) v2[1] += A(r[q]) * A(r[q]);
+                        acc_madd(v2[0], r[q], z[q]);
+                        if (relres) acc_madd(v2[1], r[q], r[q]);
                     }
                     cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
                     eta_new = v2[0];
                     rr = v2[1];
                 }
                 ++iter;
-                if (!isfinite(eta_new) || !isfinite(pap)) { status = ST_BREAKDOWN; break; }
-                if (relres ? (rr <= thr) : (fabs(eta_new) < tol)) { status = ST_CONVERGED; break; }
-                const T beta = T(eta_new / eta);
+                if (!acc_finite(eta_new) || !acc_finite(pap)) { status = ST_BREAKDOWN; break; }
+                if (relres ? (rr <= thr) : (acc_abs(eta_new) < tol)) { status = ST_CONVERGED; break; }
+                const T beta = acc_ratio<T>(eta_new, eta);
                 eta = eta_new;
                 T w[RPT];
                 if (act) matS(vp + lk * NP, w);
@@ -639,11 +649,11 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 {
                     A v1[1] = {A(0)};
 #pragma unroll
-                    for (int q = 0; q < RPT; ++q) v1[0] += A(p[q]) * A(y[q]);
+                    for (int q = 0; q < RPT; ++q) acc_madd(v1[0], p[q], y[q]);
                     cluster_allreduce<A, 1>(v1, slots, wscr, 0, cluster, C, rank);
                     pap = v1[0];
                 }
-                const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
+                const T alpha = (pap == A(0)) ? T(0) : acc_ratio<T>(eta, pap);
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
                     lam[q] = fma_rn(alpha, p[q], lam[q]);
@@ -679,17 +689,17 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                     A v2[2] = {A(0), A(0)};
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) {
-                        v2[0] += A(r[q]) * A(z[q]);
-                        if (relres) v2[1] += A(r[q]) * A(r[q]);
+                        acc_madd(v2[0], r[q], z[q]);
+                        if (relres) acc_madd(v2[1], r[q], r[q]);
                     }
                     cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
                     eta_new = v2[0];
                     rr = v2[1];
                 }
                 ++iter;
-                if (!isfinite(eta_new) || !isfinite(pap)) { status = ST_BREAKDOWN; break; }
-                if (relres ? (rr <= thr) : (fabs(eta_new) < tol)) { status = ST_CONVERGED; break; }
-                const T beta = T(eta_new / eta);
+                if (!acc_finite(eta_new) || !acc_finite(pap)) { status = ST_BREAKDOWN; break; }
+                if (relres ? (rr <= thr) : (acc_abs(eta_new) < tol)) { status = ST_CONVERGED; break; }
+                const T beta = acc_ratio<T>(eta_new, eta);
                 eta = eta_new;
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
@@ -1006,9 +1016,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
             A v3[3] = {A(0), A(0), A(0)};
 #pragma unroll
             for (int q = 0; q < RPT; ++q) {
-                v3[0] += A(r[q]) * A(u[q]);
-                v3[1] += A(w[q]) * A(u[q]);
-                v3[2] += A(gam[q]) * A(gam[q]);
+                acc_madd(v3[0], r[q], u[q]);
+                acc_madd(v3[1], w[q], u[q]);
+                acc_madd(v3[2], gam[q], gam[q]);
             }
             cluster_allreduce<A, 3>(v3, slots, wscr, 0, cluster, C, rank);
             g = v3[0];
@@ -1082,9 +1092,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
                 A v3[3] = {A(0), A(0), A(0)};
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
-                    v3[0] += A(r[q]) * A(u[q]);
-                    v3[1] += A(w[q]) * A(u[q]);
-                    if (relres) v3[2] += A(r[q]) * A(r[q]);
+                    acc_madd(v3[0], r[q], u[q]);
+                    acc_madd(v3[1], w[q], u[q]);
+                    if (relres) acc_madd(v3[2], r[q], r[q]);
                 }
                 cluster_allreduce<A, 3>(v3, slots, wscr, (iter + 1) & 1, cluster, C, rank);
                 g_new = v3[0];

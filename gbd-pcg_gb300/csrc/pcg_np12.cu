@@ -12,12 +12,6 @@ int variants_np12(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT(double, double, 12, true, ST_REG, 1);
     out[c++] = GBDPCG_VARIANT(double, double, 12, false, ST_REG_S, 1);
     out[c++] = GBDPCG_VARIANT_SR(double, double, 12, ST_REG_S, 1);
-    GBDPCG_VARIANTS_RF(12)
-    GBDPCG_VARIANTS_RF_RPT2(12)
-    GBDPCG_VARIANTS_REC(12)
-    GBDPCG_VARIANTS_REC_RPT2(12)
-    out[c++] = GBDPCG_VARIANT_REC(double, double, 12, false, ST_REG, 1);
-    out[c++] = GBDPCG_VARIANT_REC(double, double, 12, false, ST_REG_S, 1);
     return c;
 }
 }  // namespace gbdpcg

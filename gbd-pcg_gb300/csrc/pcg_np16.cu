@@ -11,12 +11,6 @@ int variants_np16(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT_SR(double, double, 16, ST_REG, 1);
     out[c++] = GBDPCG_VARIANT(double, double, 16, false, ST_REG_S, 1);
     out[c++] = GBDPCG_VARIANT_SR(double, double, 16, ST_REG_S, 1);
-    GBDPCG_VARIANTS_RF(16)
-    GBDPCG_VARIANTS_RF_RPT2(16)
-    GBDPCG_VARIANTS_REC(16)
-    GBDPCG_VARIANTS_REC_RPT2(16)
-    out[c++] = GBDPCG_VARIANT_REC(double, double, 16, false, ST_REG, 1);
-    out[c++] = GBDPCG_VARIANT_REC(double, double, 16, false, ST_REG_S, 1);
     return c;
 }
 }  // namespace gbdpcg

@@ -9,11 +9,6 @@ int variants_np24(KernelVariant *out) {
     GBDPCG_VARIANTS_F64_SMEM(24)
     out[c++] = GBDPCG_VARIANT(double, double, 24, false, ST_REG_S, 1);
     out[c++] = GBDPCG_VARIANT_SR(double, double, 24, ST_REG_S, 1);
-    GBDPCG_VARIANTS_RF(24)
-    GBDPCG_VARIANTS_RF_RPT2(24)
-    GBDPCG_VARIANTS_REC(24)
-    GBDPCG_VARIANTS_REC_RPT2(24)
-    out[c++] = GBDPCG_VARIANT_REC(double, double, 24, false, ST_REG_S, 1);
     return c;
 }
 }  // namespace gbdpcg

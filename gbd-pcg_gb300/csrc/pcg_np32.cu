@@ -6,8 +6,6 @@ int variants_np32(KernelVariant *out) {
     int c = 0;
     GBDPCG_VARIANTS_F32(32)
     GBDPCG_VARIANTS_F64_SMEM(32)
-    GBDPCG_VARIANTS_RF(32)
-    GBDPCG_VARIANTS_REC(32)
     return c;
 }
 }  // namespace gbdpcg

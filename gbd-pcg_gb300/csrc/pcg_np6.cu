@@ -12,12 +12,6 @@ int variants_np6(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT(double, double, 6, true, ST_REG, 1);
     out[c++] = GBDPCG_VARIANT(double, double, 6, false, ST_REG_S, 1);
     out[c++] = GBDPCG_VARIANT_SR(double, double, 6, ST_REG_S, 1);
-    GBDPCG_VARIANTS_RF(6)
-    GBDPCG_VARIANTS_RF_RPT2(6)
-    GBDPCG_VARIANTS_REC(6)
-    GBDPCG_VARIANTS_REC_RPT2(6)
-    out[c++] = GBDPCG_VARIANT_REC(double, double, 6, false, ST_REG, 1);
-    out[c++] = GBDPCG_VARIANT_REC(double, double, 6, false, ST_REG_S, 1);
     return c;
 }
 }  // namespace gbdpcg

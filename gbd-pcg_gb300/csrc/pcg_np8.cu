@@ -12,12 +12,6 @@ int variants_np8(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT(double, double, 8, true, ST_REG, 1);
     out[c++] = GBDPCG_VARIANT(double, double, 8, false, ST_REG_S, 1);
     out[c++] = GBDPCG_VARIANT_SR(double, double, 8, ST_REG_S, 1);
-    GBDPCG_VARIANTS_RF(8)
-    GBDPCG_VARIANTS_RF_RPT2(8)
-    GBDPCG_VARIANTS_REC(8)
-    GBDPCG_VARIANTS_REC_RPT2(8)
-    out[c++] = GBDPCG_VARIANT_REC(double, double, 8, false, ST_REG, 1);
-    out[c++] = GBDPCG_VARIANT_REC(double, double, 8, false, ST_REG_S, 1);
     return c;
 }
 }  // namespace gbdpcg

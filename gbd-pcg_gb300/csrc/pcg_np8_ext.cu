@@ -1,0 +1,19 @@
+// Cluster-kernel variants for blocks of size n <= 8: the recurrence form,
+// FP32 + FP64 refinement and float-float accumulation (a second translation
+// unit so that the variants of one block size compile in parallel).
+#include "pcg_variants.cuh"
+
+namespace gbdpcg {
+int variants_np8_ext(KernelVariant *out) {
+    int c = 0;
+    GBDPCG_VARIANTS_RF(8)
+    GBDPCG_VARIANTS_RF_RPT2(8)
+    GBDPCG_VARIANTS_REC(8)
+    GBDPCG_VARIANTS_REC_RPT2(8)
+    out[c++] = GBDPCG_VARIANT_REC(double, double, 8, false, ST_REG, 1);
+    out[c++] = GBDPCG_VARIANT_REC(double, double, 8, false, ST_REG_S, 1);
+    GBDPCG_VARIANTS_F2(8)
+    GBDPCG_VARIANTS_F2_RPT2(8)
+    return c;
+}
+}  // namespace gbdpcg

@@ -9,8 +9,9 @@
 //   * outer step: r64 = gamma - S64 lambda64, with S64 read from global memory
 //     (FP64 FMAs, lambda halo through DSMEM), ||r64|| reduced in FP64; stop when
 //     ||r64|| <= tol ||gamma|| — the exit test is on the true FP64 residual;
-//   * inner solve: PCG in FP32 with FP64 dot accumulation on S32 d = (float)r64
-//     from d = 0, to ||r_inner|| <= inner_tol ||r64||;
+//   * inner solve: PCG in FP32 on S32 d = (float)r64 from d = 0, to
+//     ||r_inner|| <= inner_tol ||r64||, its dot products accumulated in AI:
+//     double, or f2acc (float-float, on the FP32 pipe; see accum.cuh);
 //   * lambda64 += d.
 // Result: iters = inner PCG passes summed over the outer steps, outer = outer
 // steps, rr = the final ||r64||^2.
@@ -30,12 +31,12 @@ struct SmemPlanRF {
     }
 };
 
-template <int NP, int ST, int RPT>
+template <int NP, int ST, int RPT, typename AI>
 __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>::max_threads), 1)
     pcg_refine_kernel(const LaunchParams lp) {
     using T = float;
-    using A = double;
-    using Plan = SmemPlan<T, A, NP, false, ST>;
+    static_assert(sizeof(AI) == sizeof(double), "inner and outer reductions share the slot arrays");
+    using Plan = SmemPlan<T, double, NP, false, ST>;
     constexpr bool S_REG = ST <= ST_REG_S, P_REG = ST == ST_REG;
     const cg::cluster_group cluster = cg::this_cluster();
     const uint32_t C = cluster.num_blocks();
@@ -48,8 +49,10 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
     T *vr = reinterpret_cast<T *>(sp); sp += Plan::vec(lp.kmax);
     T *uh = reinterpret_cast<T *>(sp); sp += Plan::halo();  // unused (block-diagonal Phi^-1)
     T *zh = reinterpret_cast<T *>(sp); sp += Plan::halo();
-    A *slots = reinterpret_cast<A *>(sp); sp += Plan::slots(C);
-    A *wscr = reinterpret_cast<A *>(sp); sp += Plan::wscr(nthr >> 5);
+    double *slots64 = reinterpret_cast<double *>(sp); sp += Plan::slots(C);  // FP64 reductions
+    double *wscr64 = reinterpret_cast<double *>(sp); sp += Plan::wscr(nthr >> 5);
+    AI *slots = reinterpret_cast<AI *>(slots64);  // the same bytes for the inner reductions
+    AI *wscr = reinterpret_cast<AI *>(wscr64);
     uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp); sp += Plan::mat_p(lp.kmax);
@@ -58,7 +61,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
     const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
     const uint32_t zero_d = (uint32_t)(SmemPlanRF<NP, ST>::dwin(lp.kmax) / sizeof(double));
 
-    for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
+    for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(double)); e += nthr) slots64[e] = 0.0;
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     for (uint32_t pass = 0;; ++pass) {
         uint32_t item;
@@ -158,10 +161,10 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
         int buf = 0;
         double gg;
         {
-            A v1[1] = {0.0};
+            double v1[1] = {0.0};
 #pragma unroll
             for (int q = 0; q < RPT; ++q) v1[0] = fma(gam[q], gam[q], v1[0]);
-            cluster_allreduce<A, 1>(v1, slots, wscr, buf, cluster, C, rank);
+            cluster_allreduce<double, 1>(v1, slots64, wscr64, buf, cluster, C, rank);
             buf ^= 1;
             gg = v1[0];
         }
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
         uint32_t iters = 0, outer = 0;
         int32_t status = ST_MAX_ITER;
         double rr64 = 0.0;
-        A eta_last = A(0);
+        AI eta_last = AI(0);
         for (;;) {
             // ---- r64 = gamma - S64 lambda64 (FP64, S64 from global memory)
             if (act) {
@@ -205,10 +208,10 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
                 for (int q = 0; q < RPT; ++q) r64[q] = 0.0;
             }
             {
-                A v1[1] = {0.0};
+                double v1[1] = {0.0};
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) v1[0] = fma(r64[q], r64[q], v1[0]);
-                cluster_allreduce<A, 1>(v1, slots, wscr, buf, cluster, C, rank);
+                cluster_allreduce<double, 1>(v1, slots64, wscr64, buf, cluster, C, rank);
                 buf ^= 1;
                 rr64 = v1[0];
             }
@@ -245,20 +248,20 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) dst[q] = z[q];
             }
-            A eta, rr_in0;
+            AI eta, rr_in0;
             {
-                A v2[2] = {A(0), A(0)};
+                AI v2[2] = {AI(0), AI(0)};
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
-                    v2[0] += A(r[q]) * A(z[q]);
-                    v2[1] += A(r[q]) * A(r[q]);
+                    acc_madd(v2[0], r[q], z[q]);
+                    acc_madd(v2[1], r[q], r[q]);
                 }
-                cluster_allreduce<A, 2>(v2, slots, wscr, buf, cluster, C, rank);
+                cluster_allreduce<AI, 2>(v2, slots, wscr, buf, cluster, C, rank);
                 buf ^= 1;
                 eta = v2[0];
                 rr_in0 = v2[1];
             }
-            const A thr_in = A(inner_tol2) * rr_in0;
+            const AI thr_in = AI(inner_tol2 * (double)rr_in0);
             const uint32_t budget = d.max_iter - iters;
             uint32_t it = 0;
             bool broke = false;
@@ -268,16 +271,16 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) y[q] = T(0);
                 }
-                A pap;
+                AI pap;
                 {
-                    A v1[1] = {A(0)};
+                    AI v1[1] = {AI(0)};
 #pragma unroll
-                    for (int q = 0; q < RPT; ++q) v1[0] += A(p[q]) * A(y[q]);
-                    cluster_allreduce<A, 1>(v1, slots, wscr, buf, cluster, C, rank);
+                    for (int q = 0; q < RPT; ++q) acc_madd(v1[0], p[q], y[q]);
+                    cluster_allreduce<AI, 1>(v1, slots, wscr, buf, cluster, C, rank);
                     buf ^= 1;
                     pap = v1[0];
                 }
-                const T alpha = (pap == A(0)) ? T(0) : T(eta / pap);
+                const T alpha = (pap == AI(0)) ? T(0) : acc_ratio<T>(eta, pap);
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
                     x[q] = fma_rn(alpha, p[q], x[q]);
@@ -300,24 +303,24 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) dst[q] = z[q];
                 }
-                A eta_new, rr;
+                AI eta_new, rr;
                 {
-                    A v2[2] = {A(0), A(0)};
+                    AI v2[2] = {AI(0), AI(0)};
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) {
-                        v2[0] += A(r[q]) * A(z[q]);
-                        v2[1] += A(r[q]) * A(r[q]);
+                        acc_madd(v2[0], r[q], z[q]);
+                        acc_madd(v2[1], r[q], r[q]);
                     }
-                    cluster_allreduce<A, 2>(v2, slots, wscr, buf, cluster, C, rank);
+                    cluster_allreduce<AI, 2>(v2, slots, wscr, buf, cluster, C, rank);
                     buf ^= 1;
                     eta_new = v2[0];
                     rr = v2[1];
                 }
                 ++it;
                 eta_last = eta_new;
-                if (!isfinite(eta_new) || !isfinite(pap)) { broke = true; break; }
+                if (!acc_finite(eta_new) || !acc_finite(pap)) { broke = true; break; }
                 if (rr <= thr_in) break;
-                const T beta = T(eta_new / eta);
+                const T beta = acc_ratio<T>(eta_new, eta);
                 eta = eta_new;
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {

@@ -7,13 +7,13 @@
 
 #define GBDPCG_VARIANT(T, A, NP, PTRI, ST, RPT)                                               \
     ::gbdpcg::KernelVariant {                                                                 \
-        sizeof(T) == 8, sizeof(A) == 8, NP, PTRI, ST, RPT, 0,                                 \
+        sizeof(T) == 8, ::gbdpcg::acc_code<T, A>(), NP, PTRI, ST, RPT, 0,                     \
             (const void *)&::gbdpcg::pcg_cluster_kernel<T, A, NP, PTRI, ST, RPT, false>,      \
             &::gbdpcg::SmemPlan<T, A, NP, PTRI, ST>::bytes                                    \
     }
 #define GBDPCG_VARIANT_REC(T, A, NP, PTRI, ST, RPT)                                           \
     ::gbdpcg::KernelVariant {                                                                 \
-        sizeof(T) == 8, sizeof(A) == 8, NP, PTRI, ST, RPT, 3,                                 \
+        sizeof(T) == 8, ::gbdpcg::acc_code<T, A>(), NP, PTRI, ST, RPT, 3,                     \
             (const void *)&::gbdpcg::pcg_cluster_kernel<T, A, NP, PTRI, ST, RPT, true>,       \
             &::gbdpcg::SmemPlan<T, A, NP, PTRI, ST>::bytes                                    \
     }
@@ -28,16 +28,18 @@
 #define GBDPCG_VARIANTS_REC_RPT2(NP) out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_REG_S, 2);
 #define GBDPCG_VARIANT_SR(T, A, NP, ST, RPT)                                                  \
     ::gbdpcg::KernelVariant {                                                                 \
-        sizeof(T) == 8, sizeof(A) == 8, NP, false, ST, RPT, 1,                                \
+        sizeof(T) == 8, ::gbdpcg::acc_code<T, A>(), NP, false, ST, RPT, 1,                    \
             (const void *)&::gbdpcg::pcg_sr_kernel<T, A, NP, ST, RPT>,                        \
             &::gbdpcg::SmemPlanSR<T, A, NP, ST>::bytes                                        \
     }
 
-#define GBDPCG_VARIANT_RF(NP, ST, RPT)                                                        \
+#define GBDPCG_VARIANT_RF_ACC(NP, ST, RPT, AI)                                                \
     ::gbdpcg::KernelVariant {                                                                 \
-        0, 1, NP, false, ST, RPT, 2, (const void *)&::gbdpcg::pcg_refine_kernel<NP, ST, RPT>,   \
+        0, ::gbdpcg::acc_code<float, AI>(), NP, false, ST, RPT, 2,                            \
+            (const void *)&::gbdpcg::pcg_refine_kernel<NP, ST, RPT, AI>,                      \
             &::gbdpcg::SmemPlanRF<NP, ST>::bytes                                              \
     }
+#define GBDPCG_VARIANT_RF(NP, ST, RPT) GBDPCG_VARIANT_RF_ACC(NP, ST, RPT, double)
 // FP32 inner solve with FP64 refinement
 #define GBDPCG_VARIANTS_RF(NP)                                                                \
     out[c++] = GBDPCG_VARIANT_RF(NP, ST_REG, 1);                                              \
@@ -69,3 +71,19 @@
     out[c++] = GBDPCG_VARIANT(double, double, NP, false, ST_SMEM, 1);                         \
     out[c++] = GBDPCG_VARIANT(double, double, NP, true, ST_SMEM, 1);                          \
     out[c++] = GBDPCG_VARIANT_SR(double, double, NP, ST_SMEM, 1);
+
+// FP32 systems with float-float dot accumulation (accum.cuh), and FP32 + FP64
+// refinement whose inner dot products accumulate in float-float.
+#define GBDPCG_VARIANTS_F2(NP)                                                                \
+    out[c++] = GBDPCG_VARIANT(float, ::gbdpcg::f2acc, NP, false, ST_REG, 1);                  \
+    out[c++] = GBDPCG_VARIANT(float, ::gbdpcg::f2acc, NP, true, ST_REG, 1);                   \
+    out[c++] = GBDPCG_VARIANT(float, ::gbdpcg::f2acc, NP, false, ST_REG_S, 1);                \
+    out[c++] = GBDPCG_VARIANT(float, ::gbdpcg::f2acc, NP, false, ST_SMEM, 1);                 \
+    out[c++] = GBDPCG_VARIANT_REC(float, ::gbdpcg::f2acc, NP, false, ST_REG, 1);              \
+    out[c++] = GBDPCG_VARIANT_RF_ACC(NP, ST_REG, 1, ::gbdpcg::f2acc);                         \
+    out[c++] = GBDPCG_VARIANT_RF_ACC(NP, ST_REG_S, 1, ::gbdpcg::f2acc);                       \
+    out[c++] = GBDPCG_VARIANT_RF_ACC(NP, ST_SMEM, 1, ::gbdpcg::f2acc);
+#define GBDPCG_VARIANTS_F2_RPT2(NP)                                                           \
+    out[c++] = GBDPCG_VARIANT(float, ::gbdpcg::f2acc, NP, false, ST_REG_S, 2);                \
+    out[c++] = GBDPCG_VARIANT_REC(float, ::gbdpcg::f2acc, NP, false, ST_REG_S, 2);            \
+    out[c++] = GBDPCG_VARIANT_RF_ACC(NP, ST_REG_S, 2, ::gbdpcg::f2acc);

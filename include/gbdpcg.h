@@ -76,8 +76,15 @@ enum {
                                   barriers per iteration instead of four; iterates differ at
                                   roundoff level */
 };
-/* dot-product accumulation for float systems */
-enum { GBDPCG_DOT_NATIVE = 0, GBDPCG_DOT_FP64 = 1 };
+/* dot-product accumulation for float systems (and for the FP32 inner solve of
+ * a refined FP64 system, where NATIVE means FP64) */
+enum {
+    GBDPCG_DOT_NATIVE = 0,
+    GBDPCG_DOT_FP64 = 1,  /* double */
+    GBDPCG_DOT_FLOAT2 = 2 /* float-float: exact products, double-word sums with a 48-bit
+                             significand, on the FP32 pipe (GB300's FP64 rate is a small
+                             fraction of its FP32 rate); not with SINGLE_REDUCTION */
+};
 /* where the cluster solver keeps the matrix rows: AUTO picks; REGISTERS: S and
  * Phi^-1 rows in registers; SHARED: both staged in shared memory; SPLIT: S rows
  * in registers (two per thread for even n), Phi^-1 in shared memory */

@@ -158,6 +158,47 @@ def test_dot_fp64_accumulation(gb, oracle_mod, handle):
     assert relerr(lam.cpu().numpy(), lam_o) < F32_TOL
 
 
+@pytest.mark.parametrize("layout,storage,algo", [("compact", "registers", "cluster"), ("cbtd", "registers", "cluster"),
+                                                  ("compact", "split", "cluster"), ("compact", "shared", "cluster"),
+                                                  ("compact", "registers", "recurrence"), ("compact", "split", "recurrence")])
+@pytest.mark.parametrize("n,N,seed", [(14, 64, 4), (24, 100, 5), (6, 40, 6)])
+def test_dot_float2_accumulation(gb, oracle_mod, handle, layout, storage, algo, n, N, seed):
+    """Float-float accumulation (exact products, double-word sums) against the
+    oracle's FP64 accumulation: both are exact far beyond FP32, so the passes
+    agree to +-1 and lambda to the FP32 bar."""
+    import torch
+    O = oracle_mod
+    sy, S, P, g = system(O, n, N, seed, np.float32, layout)
+    flags = O.EXIT_RELRES | O.ACC64 | (O.PINV_BLOCKDIAG if layout == "compact" else 0)
+    lam_o, it_o, st, _, _ = O.pcg(S, P, g, np.zeros(n * N, np.float32), n, N, 300, 1e-6, flags=flags)
+    d = torch.device("cuda:0")
+    lam = torch.zeros(n * N, device=d)
+    st_code = {"registers": gb.STORAGE_REGISTERS, "split": gb.STORAGE_SPLIT, "shared": gb.STORAGE_SHARED}[storage]
+    if n % 2 and storage == "split":
+        pytest.skip("split storage pairs rows: even n")
+    cfg = gb.config(max_iter=300, exit_mode=gb.EXIT_RELRES, dot_precision=gb.DOT_FLOAT2, storage=st_code,
+                    algorithm=gb.ALGO_RECURRENCE if algo == "recurrence" else gb.ALGO_CLUSTER)
+    r = handle.solve(*(torch.from_numpy(a).to(d) for a in (S, P, g)), lam, n, N,
+                     gb.PINV_BLOCKDIAG if layout == "compact" else gb.PINV_CBTD, cfg)
+    assert r.status == gb.CONVERGED and abs(int(r.iters) - it_o) <= 1, (r.iters, it_o)
+    bar = F32_TOL if algo == "cluster" else 3 * F32_TOL
+    assert relerr(lam.cpu().numpy(), lam_o) < bar
+    # the reported residual is the FP32 recursive residual's norm, accumulated exactly enough
+    assert r.relres <= 1e-6 * (1 + 1e-6)
+
+
+def test_dot_float2_rejects_single_reduction(gb, oracle_mod, handle):
+    import torch
+    O = oracle_mod
+    n, N = 6, 20
+    _, S, P, g = system(O, n, N, 1, np.float32, "compact")
+    d = torch.device("cuda:0")
+    with pytest.raises(gb.GbdpcgError):
+        handle.solve(*(torch.from_numpy(a).to(d) for a in (S, P, g)), torch.zeros(n * N, device=d), n, N,
+                     gb.PINV_BLOCKDIAG, gb.config(dot_precision=gb.DOT_FLOAT2,
+                                                  algorithm=gb.ALGO_SINGLE_REDUCTION))
+
+
 def test_warm_start_and_zero_rhs(gb, oracle_mod, handle):
     O = oracle_mod
     n, N = 6, 20

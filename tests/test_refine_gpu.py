@@ -16,15 +16,17 @@ def _setup(O, n, N, seed, ill):
     return sy, S64, g64
 
 
+@pytest.mark.parametrize("dot", ["fp64", "float2"])
 @pytest.mark.parametrize("n,N,seed,ill", [(24, 64, 0, True), (14, 32, 1, False), (6, 100, 2, True), (24, 256, 3, True)])
-def test_refined_reaches_fp64_accuracy(gb, oracle_mod, handle, n, N, seed, ill):
+def test_refined_reaches_fp64_accuracy(gb, oracle_mod, handle, n, N, seed, ill, dot):
     import torch
     O = oracle_mod
     sy, S64, g64 = _setup(O, n, N, seed, ill)
     P32 = torch.empty(n * n * N, dtype=torch.float32, device=S64.device)
     handle.block_jacobi_f64to32(S64, P32, n, N)
     lam = torch.zeros(n * N, dtype=torch.float64, device=S64.device)
-    cfg = gb.config(exit_mode=gb.EXIT_RELRES, exit_tol=1e-10, max_iter=40000, max_outer=60, inner_tol=0.05)
+    cfg = gb.config(exit_mode=gb.EXIT_RELRES, exit_tol=1e-10, max_iter=40000, max_outer=60, inner_tol=0.05,
+                    dot_precision=gb.DOT_FLOAT2 if dot == "float2" else gb.DOT_FP64)
     r = handle.refine_solve(S64, P32, g64, lam, n, N, cfg)
     assert r.status == gb.CONVERGED, r
     lam_h = lam.cpu().numpy()
@@ -60,7 +62,8 @@ def test_refined_zero_rhs_and_warm_start(gb, oracle_mod, handle):
     assert r.status == gb.CONVERGED and r.iters == 0
 
 
-def test_refined_plan_batch(gb, oracle_mod, handle):
+@pytest.mark.parametrize("dot", ["fp64", "float2"])
+def test_refined_plan_batch(gb, oracle_mod, handle, dot):
     """Batched refinement (plan dtype 2) over ill-conditioned n=24 systems."""
     import torch
     O = oracle_mod
@@ -74,7 +77,8 @@ def test_refined_plan_batch(gb, oracle_mod, handle):
                         "gamma": torch.from_numpy(sy.gamma).to(d),
                         "lambda": torch.zeros(n * N, dtype=torch.float64, device=d), "n": n, "N": N})
         keep.append(sy)
-    cfg = gb.config(exit_mode=gb.EXIT_RELRES, exit_tol=1e-10, max_iter=40000, max_outer=60, zero_guess=1)
+    cfg = gb.config(exit_mode=gb.EXIT_RELRES, exit_tol=1e-10, max_iter=40000, max_outer=60, zero_guess=1,
+                    dot_precision=gb.DOT_FLOAT2 if dot == "float2" else gb.DOT_FP64)
     plan = gb.Plan(handle, systems, gb.PINV_BLOCKDIAG, cfg, dtype=2)
     plan.build_block_jacobi()
     plan.execute()

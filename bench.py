@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--no-extras", action="store_true", help="skip the baselines and the other configurations")
     ap.add_argument("--algorithm", default="auto", choices=["auto", "standard", "recurrence", "single-reduction"])
+    ap.add_argument("--host-pieces", type=int, default=0,
+                    help="pieces the end-to-end path pipelines copies and solves in (0: automatic)")
     ap.add_argument("--tune", default="shapes+recurrence", choices=["off", "shapes", "shapes+recurrence", "shapes+algorithms"],
                     help="autotune the plan before timing (untimed set-up, like building the plan)")
     return ap.parse_args()
@@ -163,8 +165,10 @@ def relres64(S, g, lam, n, N):
     return float(np.linalg.norm(g - y.reshape(-1)) / np.linalg.norm(g))
 
 
-def cpu_port_baseline(Sa, Pa, ga, descs, sample, threads):
-    """The oracle's C port of the PCG on `sample` systems with `threads` host threads."""
+def cpu_port_baseline(Sa, Pa, ga, descs, sample, threads, passes=1):
+    """The oracle's C port of the PCG on the first `sample` systems, `passes`
+    times over, with `threads` host threads.  Returns (systems/s, seconds,
+    threads used, iterations, status)."""
     from oracle import oracle as O
     O.lib()
     systems = []
@@ -172,10 +176,20 @@ def cpu_port_baseline(Sa, Pa, ga, descs, sample, threads):
         systems.append({"S": Sa[oS:oS + 3 * n * n * N], "Pinv": Pa[oP:oP + n * n * N],
                         "gamma": ga[oV:oV + n * N], "lambda": np.zeros(n * N, np.float32), "n": n, "N": N})
     t0 = time.perf_counter()
-    iters, status, used = O.pcg_batch(systems, flags=O.PINV_BLOCKDIAG | O.EXIT_RELRES, nthreads=threads,
-                                      max_iter=MAX_ITER, tol=TOL)
+    for _ in range(passes):
+        iters, status, used = O.pcg_batch(systems, flags=O.PINV_BLOCKDIAG | O.EXIT_RELRES, nthreads=threads,
+                                          max_iter=MAX_ITER, tol=TOL)
     dt = time.perf_counter() - t0
-    return sample / dt, dt, used, iters, status
+    return sample * passes / dt, dt, used, iters, status
+
+
+def cpu_sample_size(rate, count, seconds=10.0):
+    """(systems, passes) giving about `seconds` of host work at `rate` systems/s:
+    the first systems of the batch, or the whole batch several times over."""
+    want = max(64, int(rate * seconds))
+    if want <= count:
+        return want, 1
+    return count, max(1, int(round(want / count)))
 
 
 def single_system_latency(gbdpcg, h, dev):
@@ -369,9 +383,10 @@ def run_reference(args):
         lo, di, up = O.unpack_cbtd(Sa[oS:oS + 3 * n * n * N], n, N)
         Pa[oP:oP + n * n * N] = O.block_jacobi(di, "compact").astype(np.float32)
     threads = os.cpu_count() or 1
-    # size each step to ~10 s of host work: calibrate on 64 systems
-    rate, _, _, _, _ = cpu_port_baseline(Sa, Pa, ga, descs, min(64, len(descs)), threads)
-    sample = int(min(len(descs), max(64, rate * 10.0)))
+    # each step: about 5 s of host work (the whole batch once, or its first systems);
+    # calibrated on 256 systems
+    rate, _, _, _, _ = cpu_port_baseline(Sa, Pa, ga, descs, min(256, len(descs)), threads)
+    sample = int(min(len(descs), max(64, rate * 5.0)))
     for _ in range(args.warmup):
         cpu_port_baseline(Sa, Pa, ga, descs, min(sample, 64), threads)
     times, used = [], threads
@@ -419,7 +434,8 @@ def main():
     h = gbdpcg.Handle(local)
     algo = {"auto": gbdpcg.ALGO_AUTO, "standard": gbdpcg.ALGO_CLUSTER, "recurrence": gbdpcg.ALGO_RECURRENCE,
             "single-reduction": gbdpcg.ALGO_SINGLE_REDUCTION}[args.algorithm]
-    cfg = gbdpcg.config(max_iter=MAX_ITER, exit_tol=TOL, exit_mode=gbdpcg.EXIT_RELRES, zero_guess=1, algorithm=algo)
+    cfg = gbdpcg.config(max_iter=MAX_ITER, exit_tol=TOL, exit_mode=gbdpcg.EXIT_RELRES, zero_guess=1, algorithm=algo,
+                        host_pieces=args.host_pieces)
     plan = gbdpcg.Plan(h, layout=gbdpcg.PINV_BLOCKDIAG, cfg=cfg, packed=(descs, dS, dP, dg, dl))
     plan.build_block_jacobi()
     torch.cuda.synchronize()
@@ -570,12 +586,12 @@ def main():
         # ---- host-core port of the same PCG (the CPU baseline)
         threads = os.cpu_count() or 1
         Pn = dP.cpu().numpy()
-        rate, _, _, _, _ = cpu_port_baseline(Sa, Pn, ga, descs, min(64, count), threads)
-        csample = int(min(count, max(64, rate * 10.0)))
-        rate, dt, used, _, _ = cpu_port_baseline(Sa, Pn, ga, descs, csample, threads)
+        rate, _, _, _, _ = cpu_port_baseline(Sa, Pn, ga, descs, min(256, count), threads)
+        csample, cpasses = cpu_sample_size(rate, count)
+        rate, dt, used, _, _ = cpu_port_baseline(Sa, Pn, ga, descs, csample, threads, cpasses)
         line["cpu_baseline"] = {"value": rate, "unit": "solves/s", "cores": used, "kind": "port",
-                                "sample": f"first {csample} of the {count} systems, oracle/pcg_oracle.c, "
-                                          f"{dt:.1f} s"}
+                                "sample": f"first {csample} of the {count} systems x {cpasses} passes, "
+                                          f"oracle/pcg_oracle.c, {dt:.1f} s"}
     if not args.no_extras and world == 1:
         for key, fn in (("single_system", lambda: single_system_latency(gbdpcg, h, dev)),
                         ("adjoint", lambda: adjoint_config(gbdpcg, h, dev, tune_flags)),

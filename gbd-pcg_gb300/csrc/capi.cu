@@ -502,10 +502,28 @@ struct gbdpcg_plan_s {
     cudaGraphExec_t gexec = nullptr;
     // packed plans: the device arenas and their sizes in bytes
     bool packed = false;
+    int dtype = 0;
     const void *arena_S = nullptr, *arena_P = nullptr, *arena_g = nullptr;
     void *arena_l = nullptr;
     size_t bytes_S = 0, bytes_P = 0, bytes_vec = 0;
+    std::vector<gbdpcg_packed_system> packed_list;
+    // execute_host pipeline (built on first use): pieces of consecutive systems,
+    // each a plan of its own over the same arenas, with byte ranges [lo, hi)
+    bool pieces_built = false;
+    struct Piece {
+        gbdpcg_plan_s *plan = nullptr;
+        uint32_t first = 0, count = 0;
+        size_t S0 = 0, S1 = 0, P0 = 0, P1 = 0, V0 = 0, V1 = 0;
+    };
+    std::vector<Piece> pieces;
+    cudaStream_t copy_stream = nullptr;
+    std::vector<cudaStream_t> piece_streams;
+    std::vector<cudaEvent_t> piece_events;  // [copied i] then [solved i]
     ~gbdpcg_plan_s() {
+        for (auto &pc : pieces) delete pc.plan;
+        if (copy_stream) cudaStreamDestroy(copy_stream);
+        for (auto s : piece_streams) cudaStreamDestroy(s);
+        for (auto e : piece_events) cudaEventDestroy(e);
         if (gexec) cudaGraphExecDestroy(gexec);
         if (graph) cudaGraphDestroy(graph);
         for (auto s : streams) cudaStreamDestroy(s);
@@ -1033,6 +1051,8 @@ int gbdpcg_plan_create_packed(gbdpcg_handle_t h, int dtype, const gbdpcg_packed_
     if (rc) return rc;
     gbdpcg_plan_s *p = *plan;
     p->packed = true;
+    p->dtype = dtype;
+    p->packed_list.assign(systems, systems + count);
     p->arena_S = d_S;
     p->arena_P = d_Pinv;
     p->arena_g = d_gamma;
@@ -1043,6 +1063,84 @@ int gbdpcg_plan_create_packed(gbdpcg_handle_t h, int dtype, const gbdpcg_packed_
     return GBDPCG_SUCCESS;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Forgets the execute_host pieces (rebuilt on the next call, e.g. with the
+// shapes a new autotuning chose).
+void drop_pieces(gbdpcg_plan_s *p) {
+    for (auto &pc : p->pieces) delete pc.plan;
+    p->pieces.clear();
+    if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
+    p->copy_stream = nullptr;
+    for (auto s : p->piece_streams) cudaStreamDestroy(s);
+    p->piece_streams.clear();
+    for (auto e : p->piece_events) cudaEventDestroy(e);
+    p->piece_events.clear();
+    p->pieces_built = false;
+}
+
+// Cuts a packed plan into pieces of consecutive systems for execute_host.
+// Needs offsets that increase with the system index in all three arenas, so
+// that each piece is one contiguous byte range of each; otherwise (or with one
+// piece) execute_host copies the arenas whole.
+int build_pieces(gbdpcg_plan_s *p) {
+    p->pieces_built = true;
+    const uint32_t count = p->count;
+    uint32_t k = p->cfg.host_pieces;
+    if (k == 0) k = std::min<uint32_t>(16, std::max<uint32_t>(1, count / 256));
+    k = std::min(k, count);
+    if (k <= 1 || !p->plain_items.empty()) return GBDPCG_SUCCESS;
+    const auto &L = p->packed_list;
+    for (uint32_t i = 1; i < count; ++i)
+        if (L[i].S_off <= L[i - 1].S_off || L[i].Pinv_off <= L[i - 1].Pinv_off || L[i].vec_off <= L[i - 1].vec_off)
+            return GBDPCG_SUCCESS;
+    const size_t s = p->dtype ? 8 : 4;
+    // equal shares of S bytes
+    std::vector<uint32_t> cut = {0};
+    const double total = (double)p->bytes_S;
+    for (uint32_t i = 1; i < count && cut.size() < k; ++i)
+        if ((double)L[i].S_off * s >= total * cut.size() / k) cut.push_back(i);
+    cut.push_back(count);
+    gbdpcg_config cfg = p->cfg;
+    cfg.host_pieces = 1;
+    for (size_t j = 0; j + 1 < cut.size(); ++j) {
+        gbdpcg_plan_s::Piece pc;
+        pc.first = cut[j];
+        pc.count = cut[j + 1] - cut[j];
+        pc.S0 = L[pc.first].S_off * s;
+        pc.P0 = L[pc.first].Pinv_off * s;
+        pc.V0 = L[pc.first].vec_off * s;
+        const bool last = j + 2 == cut.size();
+        pc.S1 = last ? p->bytes_S : L[cut[j + 1]].S_off * s;
+        pc.P1 = last ? p->bytes_P : L[cut[j + 1]].Pinv_off * s;
+        pc.V1 = last ? p->bytes_vec : L[cut[j + 1]].vec_off * s;
+        gbdpcg_plan_t sub = nullptr;
+        int rc = gbdpcg_plan_create_packed(p->h, p->dtype, L.data() + pc.first, pc.count, p->arena_S,
+                                           p->arena_P, p->arena_g, p->arena_l, p->layout, &cfg, &sub);
+        if (rc) return rc;
+        pc.plan = sub;
+        p->pieces.push_back(pc);
+    }
+    GB_CUDA(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
+    for (int j = 0; j < 2; ++j) {
+        cudaStream_t st;
+        GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        p->piece_streams.push_back(st);
+    }
+    for (size_t j = 0; j < 2 * p->pieces.size() + 1; ++j) {
+        cudaEvent_t ev;
+        GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        p->piece_events.push_back(ev);
+    }
+    return GBDPCG_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
 int gbdpcg_plan_execute_host(gbdpcg_plan_t p, const void *h_S, const void *h_Pinv,
                              const void *h_gamma, void *h_lambda, gbdpcg_result *h_results,
                              gbdpcg_stream_t stream_) {
@@ -1050,6 +1148,49 @@ int gbdpcg_plan_execute_host(gbdpcg_plan_t p, const void *h_S, const void *h_Pin
     if (!p->packed) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan was not created packed");
     HandleScope scope(p->h->device);
     cudaStream_t st = (cudaStream_t)stream_;
+    if (!p->pieces_built) {
+        int rc = build_pieces(p);
+        if (rc) return rc;
+    }
+    if (!p->pieces.empty()) {
+        const size_t np = p->pieces.size();
+        cudaEvent_t start = p->piece_events[2 * np];
+        GB_CUDA(cudaEventRecord(start, st));
+        GB_CUDA(cudaStreamWaitEvent(p->copy_stream, start, 0));
+        for (auto s : p->piece_streams) GB_CUDA(cudaStreamWaitEvent(s, start, 0));
+        auto h2d = [&](const void *dst, const void *src, size_t lo, size_t hi) -> cudaError_t {
+            if (!src || hi <= lo) return cudaSuccess;
+            return cudaMemcpyAsync(static_cast<char *>(const_cast<void *>(dst)) + lo,
+                                   static_cast<const char *>(src) + lo, hi - lo, cudaMemcpyHostToDevice,
+                                   p->copy_stream);
+        };
+        for (size_t j = 0; j < np; ++j) {
+            const auto &pc = p->pieces[j];
+            GB_CUDA(h2d(p->arena_S, h_S, pc.S0, pc.S1));
+            GB_CUDA(h2d(p->arena_P, h_Pinv, pc.P0, pc.P1));
+            GB_CUDA(h2d(p->arena_g, h_gamma, pc.V0, pc.V1));
+            if (!p->cfg.zero_guess) GB_CUDA(h2d(p->arena_l, h_lambda, pc.V0, pc.V1));
+            GB_CUDA(cudaEventRecord(p->piece_events[j], p->copy_stream));
+        }
+        for (size_t j = 0; j < np; ++j) {
+            const auto &pc = p->pieces[j];
+            cudaStream_t cs = p->piece_streams[j % p->piece_streams.size()];
+            GB_CUDA(cudaStreamWaitEvent(cs, p->piece_events[j], 0));
+            int rc = gbdpcg_plan_execute(pc.plan, cs);
+            if (rc) return rc;
+            if (pc.V1 > pc.V0)
+                GB_CUDA(cudaMemcpyAsync(static_cast<char *>(h_lambda) + pc.V0,
+                                        static_cast<char *>(p->arena_l) + pc.V0, pc.V1 - pc.V0,
+                                        cudaMemcpyDeviceToHost, cs));
+            GB_CUDA(cudaMemcpyAsync(p->d_results.as<SysResult>() + pc.first, pc.plan->d_results.p,
+                                    sizeof(SysResult) * pc.count, cudaMemcpyDeviceToDevice, cs));
+            GB_CUDA(cudaEventRecord(p->piece_events[np + j], cs));
+        }
+        for (size_t j = 0; j < np; ++j) GB_CUDA(cudaStreamWaitEvent(st, p->piece_events[np + j], 0));
+        if (h_results) return gbdpcg_plan_results(p, h_results, stream_);
+        GB_CUDA(cudaStreamSynchronize(st));
+        return GBDPCG_SUCCESS;
+    }
     if (h_S) GB_CUDA(cudaMemcpyAsync(const_cast<void *>(p->arena_S), h_S, p->bytes_S,
                                      cudaMemcpyHostToDevice, st));
     if (h_Pinv) GB_CUDA(cudaMemcpyAsync(const_cast<void *>(p->arena_P), h_Pinv, p->bytes_P,
@@ -1145,6 +1286,8 @@ int gbdpcg_plan_destroy(gbdpcg_plan_t p) {
     return GBDPCG_SUCCESS;
 }
 
+}  // extern "C"
+
 // ------------------------------------------------------------------ autotuner
 namespace {
 
@@ -1215,6 +1358,8 @@ std::vector<Candidate> tune_candidates(gbdpcg_plan_s *p, const PlanClass &base,
 }
 
 }  // namespace
+
+extern "C" {
 
 int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_stream_t stream_) {
     if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
@@ -1336,6 +1481,7 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
         std::lock_guard<std::mutex> lk(p->h->tune_mu);
         for (auto &kv : learned) p->h->tune[kv.first] = kv.second;
     }
+    drop_pieces(p);
     return plan_layout(p);
 }
 

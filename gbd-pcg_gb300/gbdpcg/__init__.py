@@ -45,7 +45,7 @@ class Config(ctypes.Structure):
                 ("algorithm", ctypes.c_uint32), ("cluster_size", ctypes.c_uint32),
                 ("max_threads", ctypes.c_uint32), ("storage", ctypes.c_uint32),
                 ("use_graph", ctypes.c_uint32), ("zero_guess", ctypes.c_uint32),
-                ("max_outer", ctypes.c_uint32), ("streams", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 1),
+                ("max_outer", ctypes.c_uint32), ("streams", ctypes.c_uint32), ("host_pieces", ctypes.c_uint32),
                 ("inner_tol", ctypes.c_double)]
 
 

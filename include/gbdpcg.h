@@ -108,7 +108,8 @@ typedef struct {
     uint32_t zero_guess;     /* 1: start from lambda = 0 and do not read lambda (default 0) */
     uint32_t max_outer;      /* refinement: outer steps (default 50) */
     uint32_t streams;        /* plans: streams the launches of one execution spread over (default 8) */
-    uint32_t reserved[1];
+    uint32_t host_pieces;    /* packed plans: pieces gbdpcg_plan_execute_host pipelines (copies of
+                                piece i+1 overlap the solve of piece i); 0 = automatic, 1 = none */
     double inner_tol;        /* refinement: relative residual of each FP32 inner solve (default 0.05) */
 } gbdpcg_config;
 
@@ -274,7 +275,11 @@ GBDPCG_API int gbdpcg_plan_create_packed(gbdpcg_handle_t h, int dtype,
 /* End-to-end solve of a packed plan from host arenas: copies S, Pinv, gamma
  * (each skipped when NULL) host to device, executes, copies lambda (and, if
  * non-NULL, the per-system results) back, and waits.  Pinned host memory
- * makes the copies asynchronous DMA. */
+ * makes the copies asynchronous DMA.  When the arenas hold the systems in
+ * index order (offsets increasing), the batch is cut into pieces of
+ * consecutive systems (config host_pieces): the copy of piece i+1 overlaps
+ * the solve of piece i, and the solves of consecutive pieces overlap each
+ * other, so the step costs about the copies plus the last piece's solve. */
 GBDPCG_API int gbdpcg_plan_execute_host(gbdpcg_plan_t plan, const void *h_S, const void *h_Pinv,
                                         const void *h_gamma, void *h_lambda,
                                         gbdpcg_result *h_results, gbdpcg_stream_t stream);

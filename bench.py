@@ -177,6 +177,8 @@ def cpu_port_baseline(Sa, Pa, ga, descs, sample, threads, passes=1):
                         "gamma": ga[oV:oV + n * N], "lambda": np.zeros(n * N, np.float32), "n": n, "N": N})
     t0 = time.perf_counter()
     for _ in range(passes):
+        for sy in systems:  # every pass solves from lambda0 = 0, like the GPU path
+            sy["lambda"][:] = 0.0
         iters, status, used = O.pcg_batch(systems, flags=O.PINV_BLOCKDIAG | O.EXIT_RELRES, nthreads=threads,
                                           max_iter=MAX_ITER, tol=TOL)
     dt = time.perf_counter() - t0

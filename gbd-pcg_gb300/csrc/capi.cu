@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -200,8 +201,9 @@ std::vector<Pref> storage_prefs(bool f64, bool ptri, uint32_t storage) {
     if (storage == GBDPCG_STORAGE_REGISTERS) return {{0, 1}, {0, 2}};
     if (storage == GBDPCG_STORAGE_SHARED) return {{2, 1}};
     if (storage == GBDPCG_STORAGE_SPLIT) return ptri ? std::vector<Pref>{} : std::vector<Pref>{{1, 2}, {1, 1}};
+    if (storage == GBDPCG_STORAGE_HYBRID) return ptri ? std::vector<Pref>{} : std::vector<Pref>{{3, 2}, {3, 1}};
     if (f64) return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{0, 1}, {1, 1}, {2, 1}};
-    return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{1, 2}, {0, 1}, {1, 1}, {2, 1}};
+    return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{1, 2}, {0, 1}, {1, 1}, {2, 1}, {3, 2}, {3, 1}};
 }
 
 // A tuned shape for one system, if its variant exists and holds the system.
@@ -366,7 +368,7 @@ int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
     if (!cfg) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "config is NULL");
     if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad pinv_layout");
     if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FLOAT2 ||
-        cfg->algorithm > GBDPCG_ALGO_RECURRENCE || cfg->storage > GBDPCG_STORAGE_SPLIT ||
+        cfg->algorithm > GBDPCG_ALGO_RECURRENCE || cfg->storage > GBDPCG_STORAGE_HYBRID ||
         cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1 ||
         !(cfg->inner_tol >= 0) || cfg->inner_tol >= 1)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad config field");
@@ -1312,6 +1314,7 @@ std::vector<Candidate> tune_candidates(gbdpcg_plan_s *p, const PlanClass &base,
     const int want_st = p->cfg.storage == GBDPCG_STORAGE_REGISTERS ? 0
                         : p->cfg.storage == GBDPCG_STORAGE_SHARED  ? 2
                         : p->cfg.storage == GBDPCG_STORAGE_SPLIT   ? 1
+                        : p->cfg.storage == GBDPCG_STORAGE_HYBRID  ? 3
                                                                    : -1;
     static const uint32_t kC[] = {1, 2, 3, 4, 5, 6, 7, 8, 16};
     for (auto &vi : reg->list) {
@@ -1406,6 +1409,22 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
 
     std::vector<SysDesc> td = p->descs;
     std::vector<std::pair<TuneKey, TuneChoice>> learned;
+    // GBDPCG_TUNE_LOG=1: one line per timed shape on stderr (diagnostics)
+    const char *log_env = getenv("GBDPCG_TUNE_LOG");
+    const bool log = log_env && log_env[0] == '1';
+    auto log_shape = [&](const PlanClass &pc, const Shape &sh, uint32_t grid, float ms, const char *tag) {
+        if (!log) return;
+        const KernelVariant &v = sh.vi->v;
+        uint32_t nmin = 1u << 30, nmax = 0, Nmin = 1u << 30, Nmax = 0;
+        for (uint32_t i : pc.items) {
+            nmin = std::min(nmin, p->descs[i].n);
+            nmax = std::max(nmax, p->descs[i].n);
+            Nmin = std::min(Nmin, p->descs[i].N);
+            Nmax = std::max(Nmax, p->descs[i].N);
+        }
+        fprintf(stderr, "gbdpcg tune: systems=%zu n=%u-%u N=%u-%u | np=%d st=%d rpt=%d alg=%d acc=%d C=%u threads=%u grid=%u | %.4f ms%s\n",
+                pc.items.size(), nmin, nmax, Nmin, Nmax, v.np, v.st, v.rpt, v.alg, v.acc, sh.C, sh.threads, grid, ms, tag);
+    };
     for (auto &pc : p->classes) {
         // this class's systems solve from zero into the scratch buffers
         size_t off = 0;
@@ -1451,6 +1470,7 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
         };
         float best_ms = 0;
         if ((rc = time_shape(pc.sh, pc.kmax, pc.grid_clusters, &best_ms))) return rc;
+        log_shape(pc, pc.sh, pc.grid_clusters, best_ms, " (planned)");
         Candidate best;
         best.sh = pc.sh;
         best.kmax = pc.kmax;
@@ -1465,6 +1485,7 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
                 GB_CUDA(cudaStreamSynchronize(st));
                 continue;
             }
+            log_shape(pc, cd.sh, cd.grid, ms, "");
             if (ms < best_ms * 0.98f) {
                 best_ms = ms;
                 best = cd;
@@ -1531,7 +1552,7 @@ int gbdpcg_tune_import(gbdpcg_handle_t h, const char *text) {
         for (int i = 0; i < 5; ++i)
             if (f[i] > (i == 2 ? 2u : 1u))
                 return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno));
-        if (f[5] > GBDPCG_ALGO_RECURRENCE || f[6] > GBDPCG_STORAGE_SPLIT || f[7] == 0 || f[8] == 0 || C == 0 ||
+        if (f[5] > GBDPCG_ALGO_RECURRENCE || f[6] > GBDPCG_STORAGE_HYBRID || f[7] == 0 || f[8] == 0 || C == 0 ||
             C > 16 || thr == 0 || thr > 1024 || thr % 32)
             return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno));
         const int np = np_for(f[7]);

@@ -46,7 +46,11 @@ __device__ __forceinline__ double fma_rn(double a, double b, double c) { return 
 
 __host__ __device__ constexpr size_t round_up(size_t x, size_t m) { return (x + m - 1) / m * m; }
 
-enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2 };
+// Storage of the matrix rows: ST_REG S and Phi^-1 in registers; ST_REG_S S in
+// registers, Phi^-1 in shared memory; ST_SMEM both in shared memory; ST_HYB
+// the sub-diagonal and diagonal blocks of S in registers, the super-diagonal
+// block of S and Phi^-1 (block-diagonal) in shared memory.
+enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2, ST_HYB = 3 };
 
 // Reduction slots: [2 buffers][3 values][C ranks x 32 warps]
 constexpr int kMaxValues = 3;
@@ -61,7 +65,9 @@ struct SmemPlan {
     }
     __host__ __device__ static size_t halo() { return round_up((size_t)2 * NP * sizeof(T), 32); }
     __host__ __device__ static size_t mat_s(uint32_t kmax) {
-        return ST == ST_SMEM ? round_up((size_t)kmax * 3 * NP * NP * sizeof(T), 32) : 0;
+        return ST == ST_SMEM  ? round_up((size_t)kmax * 3 * NP * NP * sizeof(T), 32)
+               : ST == ST_HYB ? round_up((size_t)kmax * NP * NP * sizeof(T), 32)
+                              : 0;
     }
     __host__ __device__ static size_t mat_p(uint32_t kmax) {
         return ST >= ST_REG_S ? round_up((size_t)kmax * NB_P * NP * NP * sizeof(T), 32) : 0;
@@ -86,7 +92,8 @@ template <typename T, typename A, int NP, bool PTRI, int ST, int RPT>
 struct RegBudget {
     static constexpr int words = (int)(sizeof(T) / 4);
     static constexpr int matrix =
-        RPT * ((ST <= ST_REG_S ? 3 * NP : 0) + (ST == ST_REG ? (PTRI ? 3 : 1) * NP : 0)) * words;
+        RPT * ((ST <= ST_REG_S ? 3 * NP : (ST == ST_HYB ? 2 * NP : 0)) + (ST == ST_REG ? (PTRI ? 3 : 1) * NP : 0)) *
+        words;
     static constexpr int base = ((sizeof(T) == 8 || sizeof(A) == 8) ? 72 : 56) + 8 * (RPT - 1) * words;
     static constexpr int regs = matrix + base > 255 ? 255 : matrix + base;
     static constexpr int max_threads_raw = 65536 / regs / 128 * 128;
@@ -194,6 +201,55 @@ __device__ __forceinline__ void smem_matvec(const T *M, uint32_t R, uint32_t r, 
     }
 }
 
+// Block-row matvec of the hybrid storage: blocks 0 and 1 (sub-diagonal,
+// diagonal) from registers, block 2 (super-diagonal, present when b2) from the
+// staged matrix M (one n x n block per knot, column-interleaved like
+// smem_matvec's).  Same chains and summation order as reg_matvec.
+template <typename T, int NP, int RPT>
+__device__ __forceinline__ void hyb_matvec(const T (&Mr)[RPT][2 * NP], const T *M, uint32_t R, uint32_t r,
+                                           bool b2, const T *x, uint32_t n, T (&y)[RPT]) {
+    T acc[RPT][3];
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+        T xv[NP];
+        lds_row<T, NP>(xv, x + b * NP);
+#pragma unroll
+        for (int q = 0; q < RPT; ++q) {
+            acc[q][b] = T(0);
+#pragma unroll
+            for (int j = 0; j < NP; ++j) acc[q][b] = fma_rn(Mr[q][b * NP + j], xv[j], acc[q][b]);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) acc[q][2] = T(0);
+    if (b2) {
+        const T *col = M + r;
+        const T *xb = x + 2 * NP;
+#pragma unroll 4
+        for (uint32_t j = 0; j < n; ++j) {
+            const T xj = xb[j];
+            if constexpr (RPT == 2 && sizeof(T) == 4) {
+                const float2 m = *reinterpret_cast<const float2 *>(col + (size_t)j * R);
+                acc[0][2] = fma_rn(m.x, xj, acc[0][2]);
+                acc[1][2] = fma_rn(m.y, xj, acc[1][2]);
+            } else if constexpr (RPT == 2) {
+                const double2 m = *reinterpret_cast<const double2 *>(col + (size_t)j * R);
+                acc[0][2] = fma_rn(m.x, xj, acc[0][2]);
+                acc[1][2] = fma_rn(m.y, xj, acc[1][2]);
+            } else {
+                acc[0][2] = fma_rn(col[(size_t)j * R], xj, acc[0][2]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) {
+        T s = acc[q][0];
+        s += acc[q][1];
+        s += acc[q][2];
+        y[q] = s;
+    }
+}
+
 // Stage the block rows of knots [kb, kb+nk) (blk = NB n^2 elements each,
 // column-major n x NB n) into the column-interleaved layout M[c*R + k*n + i].
 template <typename TO, typename TI>
@@ -203,6 +259,19 @@ __device__ __forceinline__ void stage_rows(TO *M, uint32_t R, const TI *__restri
         const uint32_t kl = e / blk, w = e - kl * blk;
         const uint32_t c = w / n, i = w - c * n;
         M[(size_t)c * R + kl * n + i] = static_cast<TO>(__ldg(g + e));
+    }
+}
+
+// Stage block `blk_off` (n^2 elements) of each of the block rows of knots
+// [kb, kb+nk) (stride elements apart) into M[c*R + k*n + i].
+template <typename TO, typename TI>
+__device__ __forceinline__ void stage_block(TO *M, uint32_t R, const TI *__restrict__ g, uint32_t nk,
+                                            uint32_t n, uint32_t stride, uint32_t tid, uint32_t nthr) {
+    const uint32_t blk = n * n;
+    for (uint32_t e = tid; e < nk * blk; e += nthr) {
+        const uint32_t kl = e / blk, w = e - kl * blk;
+        const uint32_t c = w / n, i = w - c * n;
+        M[(size_t)c * R + kl * n + i] = static_cast<TO>(__ldg(g + (size_t)kl * stride + w));
     }
 }
 
@@ -333,7 +402,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     pcg_cluster_kernel(const LaunchParams lp) {
     using Plan = SmemPlan<T, A, NP, PTRI, ST>;
     constexpr int NBP = PTRI ? 3 : 1;
-    constexpr bool S_REG = ST <= ST_REG_S, P_REG = ST == ST_REG;
+    constexpr bool S_REG = ST <= ST_REG_S, P_REG = ST == ST_REG, S_HYB = ST == ST_HYB;
+    static_assert(!S_HYB || !PTRI, "the hybrid storage keeps a block-diagonal Phi^-1");
     const cg::cluster_group cluster = cg::this_cluster();
     const uint32_t C = cluster.num_blocks();
     const uint32_t rank = cluster.block_rank();
@@ -401,12 +471,12 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         for (uint32_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
 
         // ---- matrices: registers or shared memory
-        T Sr[S_REG ? RPT : 1][S_REG ? 3 * NP : 1];
+        T Sr[S_REG || S_HYB ? RPT : 1][S_REG ? 3 * NP : (S_HYB ? 2 * NP : 1)];
         T Pr[P_REG ? RPT : 1][P_REG ? NBP * NP : 1];
-        if constexpr (S_REG) {
+        if constexpr (S_REG || S_HYB) {
             const T *Sk = S + (size_t)k * blkS;
 #pragma unroll
-            for (int b = 0; b < 3; ++b) {
+            for (int b = 0; b < (S_HYB ? 2 : 3); ++b) {
                 const bool present = act && (b != 0 || k > 0) && (b != 2 || k + 1 < N);
 #pragma unroll
                 for (int j = 0; j < NP; ++j)
@@ -416,6 +486,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                                                 ? __ldg(Sk + (b * n + j) * n + i + q)
                                                 : T(0);
             }
+            if constexpr (S_HYB) stage_block(ms, R, S + (size_t)kb * blkS + 2 * n * n, nk, n, blkS, tid, nthr);
         } else {
             const T *Sg = S + (size_t)kb * blkS;
             stage_rows(ms, R, Sg, nk, n, blkS, tid, nthr);
@@ -441,6 +512,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
         auto matS = [&](const T *x, T(&y)[RPT]) {
             if constexpr (S_REG) reg_matvec<T, NP, 3, RPT>(Sr, x, y);
+            else if constexpr (S_HYB) hyb_matvec<T, NP, RPT>(Sr, ms, R, lk * n + i, sb1 == 3, x, n, y);
             else smem_matvec<T, NP, 3, RPT>(ms, R, lk * n + i, sb0, sb1, x, n, y);
         };
         auto matP = [&](const T *x, T(&y)[RPT]) {

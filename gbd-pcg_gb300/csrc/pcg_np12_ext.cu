@@ -14,6 +14,8 @@ int variants_np12_ext(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT_REC(double, double, 12, false, ST_REG_S, 1);
     GBDPCG_VARIANTS_F2(12)
     GBDPCG_VARIANTS_F2_RPT2(12)
+    GBDPCG_VARIANTS_HYB(12)
+    GBDPCG_VARIANTS_HYB_RPT2(12)
     return c;
 }
 }  // namespace gbdpcg

@@ -14,6 +14,8 @@ int variants_np14_ext(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT_REC(double, double, 14, false, ST_REG_S, 1);
     GBDPCG_VARIANTS_F2(14)
     GBDPCG_VARIANTS_F2_RPT2(14)
+    GBDPCG_VARIANTS_HYB(14)
+    GBDPCG_VARIANTS_HYB_RPT2(14)
     return c;
 }
 }  // namespace gbdpcg

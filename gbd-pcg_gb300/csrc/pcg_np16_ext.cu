@@ -14,6 +14,8 @@ int variants_np16_ext(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT_REC(double, double, 16, false, ST_REG_S, 1);
     GBDPCG_VARIANTS_F2(16)
     GBDPCG_VARIANTS_F2_RPT2(16)
+    GBDPCG_VARIANTS_HYB(16)
+    GBDPCG_VARIANTS_HYB_RPT2(16)
     return c;
 }
 }  // namespace gbdpcg

@@ -13,6 +13,8 @@ int variants_np24_ext(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT_REC(double, double, 24, false, ST_REG_S, 1);
     GBDPCG_VARIANTS_F2(24)
     GBDPCG_VARIANTS_F2_RPT2(24)
+    GBDPCG_VARIANTS_HYB(24)
+    GBDPCG_VARIANTS_HYB_RPT2(24)
     return c;
 }
 }  // namespace gbdpcg

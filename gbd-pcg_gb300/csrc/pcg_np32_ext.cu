@@ -9,6 +9,7 @@ int variants_np32_ext(KernelVariant *out) {
     GBDPCG_VARIANTS_RF(32)
     GBDPCG_VARIANTS_REC(32)
     GBDPCG_VARIANTS_F2(32)
+    GBDPCG_VARIANTS_HYB(32)
     return c;
 }
 }  // namespace gbdpcg

@@ -14,6 +14,8 @@ int variants_np6_ext(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT_REC(double, double, 6, false, ST_REG_S, 1);
     GBDPCG_VARIANTS_F2(6)
     GBDPCG_VARIANTS_F2_RPT2(6)
+    GBDPCG_VARIANTS_HYB(6)
+    GBDPCG_VARIANTS_HYB_RPT2(6)
     return c;
 }
 }  // namespace gbdpcg

@@ -14,6 +14,8 @@ int variants_np8_ext(KernelVariant *out) {
     out[c++] = GBDPCG_VARIANT_REC(double, double, 8, false, ST_REG_S, 1);
     GBDPCG_VARIANTS_F2(8)
     GBDPCG_VARIANTS_F2_RPT2(8)
+    GBDPCG_VARIANTS_HYB(8)
+    GBDPCG_VARIANTS_HYB_RPT2(8)
     return c;
 }
 }  // namespace gbdpcg

@@ -17,7 +17,7 @@
             (const void *)&::gbdpcg::pcg_cluster_kernel<T, A, NP, PTRI, ST, RPT, true>,       \
             &::gbdpcg::SmemPlan<T, A, NP, PTRI, ST>::bytes                                    \
     }
-// recurrence form (two barriers per iteration)
+// recurrence form (three barriers per iteration)
 #define GBDPCG_VARIANTS_REC(NP)                                                               \
     out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_REG, 1);                        \
     out[c++] = GBDPCG_VARIANT_REC(float, float, NP, true, ST_REG, 1);                         \
@@ -87,3 +87,11 @@
     out[c++] = GBDPCG_VARIANT(float, ::gbdpcg::f2acc, NP, false, ST_REG_S, 2);                \
     out[c++] = GBDPCG_VARIANT_REC(float, ::gbdpcg::f2acc, NP, false, ST_REG_S, 2);            \
     out[c++] = GBDPCG_VARIANT_RF_ACC(NP, ST_REG_S, 2, ::gbdpcg::f2acc);
+// Hybrid storage (sub-diagonal and diagonal S blocks in registers, the
+// super-diagonal block and Phi^-1 in shared memory), standard and recurrence forms.
+#define GBDPCG_VARIANTS_HYB(NP)                                                               \
+    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_HYB, 1);                            \
+    out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_HYB, 1);
+#define GBDPCG_VARIANTS_HYB_RPT2(NP)                                                          \
+    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_HYB, 2);                            \
+    out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_HYB, 2);

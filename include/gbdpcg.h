@@ -87,12 +87,16 @@ enum {
 };
 /* where the cluster solver keeps the matrix rows: AUTO picks; REGISTERS: S and
  * Phi^-1 rows in registers; SHARED: both staged in shared memory; SPLIT: S rows
- * in registers (two per thread for even n), Phi^-1 in shared memory */
+ * in registers (two per thread for even n), Phi^-1 in shared memory; HYBRID:
+ * the sub-diagonal and diagonal blocks of S in registers, its super-diagonal
+ * block and Phi^-1 in shared memory (more rows per SM; FP32, block-diagonal
+ * Phi^-1) */
 enum {
     GBDPCG_STORAGE_AUTO = 0,
     GBDPCG_STORAGE_REGISTERS = 1,
     GBDPCG_STORAGE_SHARED = 2,
-    GBDPCG_STORAGE_SPLIT = 3
+    GBDPCG_STORAGE_SPLIT = 3,
+    GBDPCG_STORAGE_HYBRID = 4
 };
 
 typedef struct {
@@ -293,7 +297,7 @@ GBDPCG_API int gbdpcg_plan_launch_count(gbdpcg_plan_t plan, uint32_t *launches);
 GBDPCG_API int gbdpcg_plan_launch_info(gbdpcg_plan_t plan, uint32_t i, uint32_t *cluster, uint32_t *threads,
                             uint32_t *kmax, uint32_t *systems, uint32_t *ctas);
 /* Kernel of launch i: storage (0 S and Phi^-1 in registers, 1 S in registers
- * and Phi^-1 in shared memory, 2 both in shared memory), matrix rows per
+ * and Phi^-1 in shared memory, 2 both in shared memory, 3 hybrid), matrix rows per
  * thread, and algorithm (GBDPCG_ALGO_CLUSTER, _SINGLE_REDUCTION, _RECURRENCE,
  * or _PLAIN for a one-system plain launch; refinement launches report 0). */
 GBDPCG_API int gbdpcg_plan_launch_kernel(gbdpcg_plan_t plan, uint32_t i, uint32_t *storage,

@@ -154,6 +154,58 @@ __device__ __forceinline__ void reg_matvec(const T (&M)[RPT][NB * NP], const T *
     }
 }
 
+// One block of a shared-memory block-row matvec: acc[q][b] = sum_{j<n}
+// col[j*R + q] * x[j] for the RPT adjacent rows at col, one FMA chain per row
+// in ascending j.  The window x (NP-aligned) is read VW elements at a time
+// with vector loads (4 floats when NP is a multiple of 4, else 2); a column
+// costs one matrix load (two rows at once when RPT = 2).  Columns j >= n of
+// the staged matrix hold no data and are never read.
+template <typename T, int NP, int RPT>
+__device__ __forceinline__ void smem_col(const T *col, uint32_t R, uint32_t j, T xj, T (&a)[RPT]) {
+    if constexpr (RPT == 2 && sizeof(T) == 4) {
+        const float2 m = *reinterpret_cast<const float2 *>(col + (size_t)j * R);
+        a[0] = fma_rn(m.x, xj, a[0]);
+        a[1] = fma_rn(m.y, xj, a[1]);
+    } else if constexpr (RPT == 2) {
+        const double2 m = *reinterpret_cast<const double2 *>(col + (size_t)j * R);
+        a[0] = fma_rn(m.x, xj, a[0]);
+        a[1] = fma_rn(m.y, xj, a[1]);
+    } else {
+        a[0] = fma_rn(col[(size_t)j * R], xj, a[0]);
+    }
+}
+
+template <typename T, int NP, int RPT, int NBA>
+__device__ __forceinline__ void smem_block(const T *col, uint32_t R, const T *x, uint32_t n, T (&acc)[RPT][NBA],
+                                           int b) {
+    constexpr int VW = (sizeof(T) == 4 && NP % 4 == 0) ? 4 : (NP % 2 == 0 ? 2 : 1);
+    T a[RPT];
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) a[q] = acc[q][b];
+    uint32_t j = 0;
+#pragma unroll 2
+    for (; j + VW <= n; j += VW) {
+        T xv[VW];
+        if constexpr (VW == 4) {
+            const float4 t = *reinterpret_cast<const float4 *>(x + j);
+            xv[0] = t.x; xv[1] = t.y; xv[2] = t.z; xv[3] = t.w;
+        } else if constexpr (VW == 2 && sizeof(T) == 4) {
+            const float2 t = *reinterpret_cast<const float2 *>(x + j);
+            xv[0] = t.x; xv[1] = t.y;
+        } else if constexpr (VW == 2) {
+            const double2 t = *reinterpret_cast<const double2 *>(x + j);
+            xv[0] = t.x; xv[1] = t.y;
+        } else {
+            xv[0] = x[j];
+        }
+#pragma unroll
+        for (int u = 0; u < VW; ++u) smem_col<T, NP, RPT>(col, R, j + u, xv[u], a);
+    }
+    for (; j < n; ++j) smem_col<T, NP, RPT>(col, R, j, x[j], a);
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) acc[q][b] = a[q];
+}
+
 // Shared-memory matrices are staged column-interleaved across the CTA's rows:
 // element (row r of the CTA, column c of the block row) at M[c*R + r], R the
 // row stride (even).  A warp then reads consecutive addresses for every column
@@ -172,25 +224,7 @@ __device__ __forceinline__ void smem_matvec(const T *M, uint32_t R, uint32_t r, 
     for (int b = 0; b < NB; ++b) {
 #pragma unroll
         for (int q = 0; q < RPT; ++q) acc[q][b] = T(0);
-        if (b >= b0 && b < b1) {
-            const T *col = M + (size_t)b * n * R + r;
-            const T *xb = x + b * NP;
-#pragma unroll 4
-            for (uint32_t j = 0; j < n; ++j) {
-                const T xj = xb[j];
-                if constexpr (RPT == 2 && sizeof(T) == 4) {
-                    const float2 m = *reinterpret_cast<const float2 *>(col + (size_t)j * R);
-                    acc[0][b] = fma_rn(m.x, xj, acc[0][b]);
-                    acc[1][b] = fma_rn(m.y, xj, acc[1][b]);
-                } else if constexpr (RPT == 2) {
-                    const double2 m = *reinterpret_cast<const double2 *>(col + (size_t)j * R);
-                    acc[0][b] = fma_rn(m.x, xj, acc[0][b]);
-                    acc[1][b] = fma_rn(m.y, xj, acc[1][b]);
-                } else {
-                    acc[0][b] = fma_rn(col[(size_t)j * R], xj, acc[0][b]);
-                }
-            }
-        }
+        if (b >= b0 && b < b1) smem_block<T, NP, RPT>(M + (size_t)b * n * R + r, R, x + b * NP, n, acc, b);
     }
 #pragma unroll
     for (int q = 0; q < RPT; ++q) {
@@ -222,25 +256,7 @@ __device__ __forceinline__ void hyb_matvec(const T (&Mr)[RPT][2 * NP], const T *
     }
 #pragma unroll
     for (int q = 0; q < RPT; ++q) acc[q][2] = T(0);
-    if (b2) {
-        const T *col = M + r;
-        const T *xb = x + 2 * NP;
-#pragma unroll 4
-        for (uint32_t j = 0; j < n; ++j) {
-            const T xj = xb[j];
-            if constexpr (RPT == 2 && sizeof(T) == 4) {
-                const float2 m = *reinterpret_cast<const float2 *>(col + (size_t)j * R);
-                acc[0][2] = fma_rn(m.x, xj, acc[0][2]);
-                acc[1][2] = fma_rn(m.y, xj, acc[1][2]);
-            } else if constexpr (RPT == 2) {
-                const double2 m = *reinterpret_cast<const double2 *>(col + (size_t)j * R);
-                acc[0][2] = fma_rn(m.x, xj, acc[0][2]);
-                acc[1][2] = fma_rn(m.y, xj, acc[1][2]);
-            } else {
-                acc[0][2] = fma_rn(col[(size_t)j * R], xj, acc[0][2]);
-            }
-        }
-    }
+    if (b2) smem_block<T, NP, RPT>(M + r, R, x + 2 * NP, n, acc, 2);
 #pragma unroll
     for (int q = 0; q < RPT; ++q) {
         T s = acc[q][0];

@@ -202,6 +202,7 @@ std::vector<Pref> storage_prefs(bool f64, bool ptri, uint32_t storage) {
     if (storage == GBDPCG_STORAGE_SHARED) return {{2, 1}};
     if (storage == GBDPCG_STORAGE_SPLIT) return ptri ? std::vector<Pref>{} : std::vector<Pref>{{1, 2}, {1, 1}};
     if (storage == GBDPCG_STORAGE_HYBRID) return ptri ? std::vector<Pref>{} : std::vector<Pref>{{3, 2}, {3, 1}};
+    if (storage == GBDPCG_STORAGE_TMEM) return ptri || f64 ? std::vector<Pref>{} : std::vector<Pref>{{4, 2}};
     if (f64) return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{0, 1}, {1, 1}, {2, 1}};
     return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{1, 2}, {0, 1}, {1, 1}, {2, 1}, {3, 2}, {3, 1}};
 }
@@ -368,7 +369,7 @@ int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
     if (!cfg) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "config is NULL");
     if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad pinv_layout");
     if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FLOAT2 ||
-        cfg->algorithm > GBDPCG_ALGO_RECURRENCE || cfg->storage > GBDPCG_STORAGE_HYBRID ||
+        cfg->algorithm > GBDPCG_ALGO_RECURRENCE || cfg->storage > GBDPCG_STORAGE_TMEM ||
         cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1 ||
         !(cfg->inner_tol >= 0) || cfg->inner_tol >= 1)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad config field");
@@ -1315,6 +1316,7 @@ std::vector<Candidate> tune_candidates(gbdpcg_plan_s *p, const PlanClass &base,
                         : p->cfg.storage == GBDPCG_STORAGE_SHARED  ? 2
                         : p->cfg.storage == GBDPCG_STORAGE_SPLIT   ? 1
                         : p->cfg.storage == GBDPCG_STORAGE_HYBRID  ? 3
+                        : p->cfg.storage == GBDPCG_STORAGE_TMEM    ? 4
                                                                    : -1;
     static const uint32_t kC[] = {1, 2, 3, 4, 5, 6, 7, 8, 16};
     for (auto &vi : reg->list) {
@@ -1552,7 +1554,7 @@ int gbdpcg_tune_import(gbdpcg_handle_t h, const char *text) {
         for (int i = 0; i < 5; ++i)
             if (f[i] > (i == 2 ? 2u : 1u))
                 return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno));
-        if (f[5] > GBDPCG_ALGO_RECURRENCE || f[6] > GBDPCG_STORAGE_HYBRID || f[7] == 0 || f[8] == 0 || C == 0 ||
+        if (f[5] > GBDPCG_ALGO_RECURRENCE || f[6] > GBDPCG_STORAGE_TMEM || f[7] == 0 || f[8] == 0 || C == 0 ||
             C > 16 || thr == 0 || thr > 1024 || thr % 32)
             return fail(GBDPCG_ERR_INVALID_ARGUMENT, "tuning table line " + std::to_string(lineno));
         const int np = np_for(f[7]);

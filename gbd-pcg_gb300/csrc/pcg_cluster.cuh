@@ -36,6 +36,7 @@
 #include <stdint.h>
 
 #include "accum.cuh"
+#include "tmem.cuh"
 #include "pcg_types.h"
 
 namespace gbdpcg {
@@ -49,8 +50,15 @@ __host__ __device__ constexpr size_t round_up(size_t x, size_t m) { return (x + 
 // Storage of the matrix rows: ST_REG S and Phi^-1 in registers; ST_REG_S S in
 // registers, Phi^-1 in shared memory; ST_SMEM both in shared memory; ST_HYB
 // the sub-diagonal and diagonal blocks of S in registers, the super-diagonal
-// block of S and Phi^-1 (block-diagonal) in shared memory.
-enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2, ST_HYB = 3 };
+// block of S and Phi^-1 (block-diagonal) in shared memory; ST_TMEM the
+// diagonal block of S in registers, its two off-diagonal blocks in tensor
+// memory, Phi^-1 (block-diagonal) in shared memory.
+enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2, ST_HYB = 3, ST_TMEM = 4 };
+
+// A CTA of the tensor-memory storage allocates all of its SM's tensor memory;
+// it asks for more than half an SM's shared memory so that no second such CTA
+// can share the SM (an allocation would otherwise wait on the first one).
+constexpr size_t kTmemExclusiveSmem = 120 * 1024;
 
 // Reduction slots: [2 buffers][3 values][C ranks x 32 warps]
 constexpr int kMaxValues = 3;
@@ -80,7 +88,8 @@ struct SmemPlan {
         return round_up((size_t)nwarps * kMaxValues * 32 * sizeof(A), 32);
     }
     __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C, uint32_t nwarps) {
-        return 2 * vec(kmax) + 2 * halo() + slots(C) + wscr(nwarps) + 32 + mat_s(kmax) + mat_p(kmax);
+        const size_t b = 2 * vec(kmax) + 2 * halo() + slots(C) + wscr(nwarps) + 32 + mat_s(kmax) + mat_p(kmax);
+        return (ST == ST_TMEM && b < kTmemExclusiveSmem) ? kTmemExclusiveSmem : b;
     }
 };
 
@@ -92,9 +101,13 @@ template <typename T, typename A, int NP, bool PTRI, int ST, int RPT>
 struct RegBudget {
     static constexpr int words = (int)(sizeof(T) / 4);
     static constexpr int matrix =
-        RPT * ((ST <= ST_REG_S ? 3 * NP : (ST == ST_HYB ? 2 * NP : 0)) + (ST == ST_REG ? (PTRI ? 3 : 1) * NP : 0)) *
+        RPT *
+        ((ST <= ST_REG_S ? 3 * NP : (ST == ST_HYB ? 2 * NP : (ST == ST_TMEM ? NP : 0))) +
+         (ST == ST_REG ? (PTRI ? 3 : 1) * NP : 0)) *
         words;
-    static constexpr int base = ((sizeof(T) == 8 || sizeof(A) == 8) ? 72 : 56) + 8 * (RPT - 1) * words;
+    // the tensor-memory storage also holds TMEM addresses and the 16 values of a load pair
+    static constexpr int base =
+        ((sizeof(T) == 8 || sizeof(A) == 8) ? 72 : 56) + 8 * (RPT - 1) * words + (ST == ST_TMEM ? 24 : 0);
     static constexpr int regs = matrix + base > 255 ? 255 : matrix + base;
     static constexpr int max_threads_raw = 65536 / regs / 128 * 128;
     static constexpr int max_threads = max_threads_raw > 1024 ? 1024 : max_threads_raw;
@@ -266,6 +279,84 @@ __device__ __forceinline__ void hyb_matvec(const T (&Mr)[RPT][2 * NP], const T *
     }
 }
 
+// Columns of one row's block in tensor memory (a multiple of 8: x8 moves).
+template <int NP>
+__host__ __device__ constexpr int tmem_cols() { return (NP + 7) / 8 * 8; }
+
+// Block-row matvec of the tensor-memory storage, two rows per thread: blocks
+// 0 and 2 (sub- and super-diagonal) from this thread's TMEM lane at trow
+// (row q, block bi at columns (2q + bi) * NPT), block 1 (diagonal) from
+// registers.  Same chains and summation order as reg_matvec.  Warp-wide: every
+// thread of the warp calls it (inactive rows read a valid window and discard
+// the result).
+// Elements [8c, 8c+8) of an NP-element window (those below NP), loaded with
+// the widest aligned vectors.
+template <int NP>
+__device__ __forceinline__ void lds_chunk8(float (&xv)[8], const float *x, int c) {
+    constexpr int VW = NP % 4 == 0 ? 4 : (NP % 2 == 0 ? 2 : 1);
+#pragma unroll
+    for (int u = 0; u < 8; u += VW) {
+        if (8 * c + u < NP) {
+            if constexpr (VW == 4) {
+                const float4 t = *reinterpret_cast<const float4 *>(x + 8 * c + u);
+                xv[u] = t.x; xv[u + 1] = t.y; xv[u + 2] = t.z; xv[u + 3] = t.w;
+            } else if constexpr (VW == 2) {
+                const float2 t = *reinterpret_cast<const float2 *>(x + 8 * c + u);
+                xv[u] = t.x; xv[u + 1] = t.y;
+            } else {
+                xv[u] = x[8 * c + u];
+            }
+        }
+    }
+}
+
+template <int NP>
+__device__ __forceinline__ void tmem_matvec(const float (&Md)[2][NP], uint32_t trow, const float *x, float (&y)[2]) {
+    constexpr int NPT = tmem_cols<NP>();
+    __syncwarp();  // tcgen05 loads are warp-wide: the warp is converged here
+    float acc[2][3];
+#pragma unroll
+    for (int bi = 0; bi < 2; ++bi) {
+        const int b = 2 * bi;
+        acc[0][b] = 0.f;
+        acc[1][b] = 0.f;
+#pragma unroll
+        for (int c = 0; c < NPT / 8; ++c) {
+            float m0[8], m1[8], xv[8];
+            tmem_ld8x2(trow + (0 * 2 + bi) * NPT + 8 * c, trow + (1 * 2 + bi) * NPT + 8 * c, m0, m1);
+            lds_chunk8<NP>(xv, x + b * NP, c);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (8 * c + u < NP) {
+                    acc[0][b] = fma_rn(m0[u], xv[u], acc[0][b]);
+                    acc[1][b] = fma_rn(m1[u], xv[u], acc[1][b]);
+                }
+            }
+        }
+    }
+    acc[0][1] = 0.f;
+    acc[1][1] = 0.f;
+#pragma unroll
+    for (int c = 0; c < NPT / 8; ++c) {
+        float xv[8];
+        lds_chunk8<NP>(xv, x + NP, c);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (8 * c + u < NP) {
+                acc[0][1] = fma_rn(Md[0][8 * c + u], xv[u], acc[0][1]);
+                acc[1][1] = fma_rn(Md[1][8 * c + u], xv[u], acc[1][1]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        float s = acc[q][0];
+        s += acc[q][1];
+        s += acc[q][2];
+        y[q] = s;
+    }
+}
+
 // Stage the block rows of knots [kb, kb+nk) (blk = NB n^2 elements each,
 // column-major n x NB n) into the column-interleaved layout M[c*R + k*n + i].
 template <typename TO, typename TI>
@@ -418,8 +509,13 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     pcg_cluster_kernel(const LaunchParams lp) {
     using Plan = SmemPlan<T, A, NP, PTRI, ST>;
     constexpr int NBP = PTRI ? 3 : 1;
-    constexpr bool S_REG = ST <= ST_REG_S, P_REG = ST == ST_REG, S_HYB = ST == ST_HYB;
+    constexpr bool S_REG = ST <= ST_REG_S, P_REG = ST == ST_REG, S_HYB = ST == ST_HYB, S_TM = ST == ST_TMEM;
     static_assert(!S_HYB || !PTRI, "the hybrid storage keeps a block-diagonal Phi^-1");
+    static_assert(!S_TM || (!PTRI && RPT == 2 && sizeof(T) == 4), "tensor-memory storage: FP32, two rows per thread");
+    constexpr int NPT = tmem_cols<NP>();
+    static_assert(!S_TM || (RegBudget<T, A, NP, PTRI, ST, RPT>::max_threads + 127) / 128 * RPT * 2 * NPT <=
+                               (int)kTmemColumns,
+                  "the warps of a CTA fit the tensor memory's columns");
     const cg::cluster_group cluster = cg::this_cluster();
     const uint32_t C = cluster.num_blocks();
     const uint32_t rank = cluster.block_rank();
@@ -439,6 +535,17 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
 
     for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
+    // tensor memory: warp 0 allocates every column (the CTA is alone on its SM);
+    // warp w reaches lanes (w % 4) * 32 + lane, its rows at columns (w / 4) * 2 RPT NPT
+    uint32_t tbase = 0, trow = 0;
+    if constexpr (S_TM) {
+        if ((tid >> 5) == 0) tmem_alloc(s_item + 1, kTmemColumns);
+        tmem_fence_before_sync();
+        __syncthreads();
+        tmem_fence_after_sync();
+        tbase = *reinterpret_cast<volatile uint32_t *>(s_item + 1);
+        trow = tbase + ((((tid >> 5) & 3u) * 32u) << 16) + (tid >> 7) * (uint32_t)(RPT * 2 * NPT);
+    }
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     for (uint32_t pass = 0;; ++pass) {
         // ---- pull the next system (cluster leader pops, broadcasts by DSMEM)
@@ -487,7 +594,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         for (uint32_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
 
         // ---- matrices: registers or shared memory
-        T Sr[S_REG || S_HYB ? RPT : 1][S_REG ? 3 * NP : (S_HYB ? 2 * NP : 1)];
+        T Sr[S_REG || S_HYB || S_TM ? RPT : 1][S_REG ? 3 * NP : (S_HYB ? 2 * NP : (S_TM ? NP : 1))];
         T Pr[P_REG ? RPT : 1][P_REG ? NBP * NP : 1];
         if constexpr (S_REG || S_HYB) {
             const T *Sk = S + (size_t)k * blkS;
@@ -503,6 +610,34 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                                                 : T(0);
             }
             if constexpr (S_HYB) stage_block(ms, R, S + (size_t)kb * blkS + 2 * n * n, nk, n, blkS, tid, nthr);
+        } else if constexpr (S_TM) {
+            const T *Sk = S + (size_t)k * blkS;
+#pragma unroll
+            for (int j = 0; j < NP; ++j)
+#pragma unroll
+                for (int q = 0; q < RPT; ++q)
+                    Sr[q][j] = (act && (uint32_t)j < n) ? __ldg(Sk + (n + j) * n + i + q) : T(0);
+            __syncwarp();  // tcgen05 stores are warp-wide
+            // one 8-column piece at a time (the loads of a piece are in flight together)
+#pragma unroll 1
+            for (int bi = 0; bi < 2; ++bi) {
+                const int b = 2 * bi;
+                const bool present = act && (b != 0 || k > 0) && (b != 2 || k + 1 < N);
+#pragma unroll 1
+                for (int q = 0; q < RPT; ++q) {
+#pragma unroll 1
+                    for (int cc = 0; cc < NPT / 8; ++cc) {
+                        float v[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            const uint32_t j = 8 * cc + u;
+                            v[u] = (present && j < n) ? __ldg(Sk + (b * n + j) * n + i + q) : 0.f;
+                        }
+                        tmem_st8(trow + (q * 2 + bi) * NPT + 8 * cc, v);
+                    }
+                }
+            }
+            tmem_wait_st();
         } else {
             const T *Sg = S + (size_t)kb * blkS;
             stage_rows(ms, R, Sg, nk, n, blkS, tid, nthr);
@@ -528,6 +663,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
         auto matS = [&](const T *x, T(&y)[RPT]) {
             if constexpr (S_REG) reg_matvec<T, NP, 3, RPT>(Sr, x, y);
+            else if constexpr (S_TM) tmem_matvec<NP>(Sr, trow, x, y);
             else if constexpr (S_HYB) hyb_matvec<T, NP, RPT>(Sr, ms, R, lk * n + i, sb1 == 3, x, n, y);
             else smem_matvec<T, NP, 3, RPT>(ms, R, lk * n + i, sb0, sb1, x, n, y);
         };
@@ -538,6 +674,23 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             } else {
                 if constexpr (PTRI) smem_matvec<T, NP, 3, RPT>(mp, R, lk * n + i, sb0, sb1, x, n, y);
                 else smem_matvec<T, NP, 1, RPT>(mp, R, lk * n + i, 0, 1, x + NP, n, y);
+            }
+        };
+        // y = S p over this thread's rows (zero for a thread without rows); with
+        // tensor memory every thread of a warp takes part in the loads
+        auto matS_rows = [&](T(&y)[RPT]) {
+            if constexpr (S_TM) {
+                matS(vp + (act ? lk : 0u) * NP, y);
+                if (!act) {
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) y[q] = T(0);
+                }
+            } else {
+                if (act) matS(vp + lk * NP, y);
+                else {
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) y[q] = T(0);
+                }
             }
         };
         T *my_p = vp + (lk + 1) * NP + i;  // this thread's rows in the windows
@@ -559,7 +712,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             }
         }
         __syncthreads();
-        if (act) matS(vp + lk * NP, y);
+        matS_rows(y);
 #pragma unroll
         for (int q = 0; q < RPT; ++q) r[q] = act ? gam[q] - y[q] : T(0);
         group_sync(cluster, C);  // all windows read before any neighbour writes into them
@@ -623,11 +776,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         const uint32_t max_iter = d.max_iter;
         if constexpr (REC) {
             // y = S p0 (p0 = z0 and its halos are in vp after the barrier above)
-            if (act) matS(vp + lk * NP, y);
-            else {
-#pragma unroll
-                for (int q = 0; q < RPT; ++q) y[q] = T(0);
-            }
+            matS_rows(y);
             for (; iter < max_iter;) {
                 if constexpr (PTRI) {  // neighbours need this CTA's boundary y for their r halo
                     if (first_knot) {
@@ -703,11 +852,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 const T beta = acc_ratio<T>(eta_new, eta);
                 eta = eta_new;
                 T w[RPT];
-                if (act) matS(vp + lk * NP, w);
-                else {
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) w[q] = T(0);
-                }
+                matS_rows(w);
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
                     p[q] = fma_rn(beta, p[q], z[q]);
@@ -716,11 +861,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             }
         } else {
             for (; iter < max_iter;) {
-                if (act) matS(vp + lk * NP, y);
-                else {
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) y[q] = T(0);
-                }
+                matS_rows(y);
                 if constexpr (PTRI) {  // neighbours need this CTA's boundary upsilon for their r halo
                     if (first_knot) {
                         T *dst = cluster.map_shared_rank(uh, rank - 1) + NP + i;
@@ -867,6 +1008,12 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 }
             }
         }
+    }
+    if constexpr (S_TM) {  // every TMEM access of the CTA is done
+        tmem_fence_before_sync();
+        __syncthreads();
+        tmem_fence_after_sync();
+        if ((tid >> 5) == 0) tmem_dealloc(tbase, kTmemColumns);
     }
 }
 

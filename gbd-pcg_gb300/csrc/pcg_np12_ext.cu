@@ -16,6 +16,7 @@ int variants_np12_ext(KernelVariant *out) {
     GBDPCG_VARIANTS_F2_RPT2(12)
     GBDPCG_VARIANTS_HYB(12)
     GBDPCG_VARIANTS_HYB_RPT2(12)
+    GBDPCG_VARIANTS_TMEM(12)
     return c;
 }
 }  // namespace gbdpcg

@@ -16,6 +16,7 @@ int variants_np14_ext(KernelVariant *out) {
     GBDPCG_VARIANTS_F2_RPT2(14)
     GBDPCG_VARIANTS_HYB(14)
     GBDPCG_VARIANTS_HYB_RPT2(14)
+    GBDPCG_VARIANTS_TMEM(14)
     return c;
 }
 }  // namespace gbdpcg

@@ -16,6 +16,7 @@ int variants_np16_ext(KernelVariant *out) {
     GBDPCG_VARIANTS_F2_RPT2(16)
     GBDPCG_VARIANTS_HYB(16)
     GBDPCG_VARIANTS_HYB_RPT2(16)
+    GBDPCG_VARIANTS_TMEM(16)
     return c;
 }
 }  // namespace gbdpcg

@@ -15,6 +15,7 @@ int variants_np24_ext(KernelVariant *out) {
     GBDPCG_VARIANTS_F2_RPT2(24)
     GBDPCG_VARIANTS_HYB(24)
     GBDPCG_VARIANTS_HYB_RPT2(24)
+    GBDPCG_VARIANTS_TMEM(24)
     return c;
 }
 }  // namespace gbdpcg

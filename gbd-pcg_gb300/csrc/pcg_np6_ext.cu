@@ -16,6 +16,7 @@ int variants_np6_ext(KernelVariant *out) {
     GBDPCG_VARIANTS_F2_RPT2(6)
     GBDPCG_VARIANTS_HYB(6)
     GBDPCG_VARIANTS_HYB_RPT2(6)
+    GBDPCG_VARIANTS_TMEM(6)
     return c;
 }
 }  // namespace gbdpcg

@@ -16,6 +16,7 @@ int variants_np8_ext(KernelVariant *out) {
     GBDPCG_VARIANTS_F2_RPT2(8)
     GBDPCG_VARIANTS_HYB(8)
     GBDPCG_VARIANTS_HYB_RPT2(8)
+    GBDPCG_VARIANTS_TMEM(8)
     return c;
 }
 }  // namespace gbdpcg

@@ -95,3 +95,8 @@
 #define GBDPCG_VARIANTS_HYB_RPT2(NP)                                                          \
     out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_HYB, 2);                            \
     out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_HYB, 2);
+// Tensor-memory storage (diagonal S block in registers, off-diagonal blocks in
+// TMEM, Phi^-1 in shared memory), two rows per thread, standard and recurrence forms.
+#define GBDPCG_VARIANTS_TMEM(NP)                                                              \
+    out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_TMEM, 2);                           \
+    out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_TMEM, 2);

@@ -30,7 +30,7 @@ PINV_CBTD, PINV_BLOCKDIAG = 0, 1
 ALGO_AUTO, ALGO_CLUSTER, ALGO_PLAIN, ALGO_SINGLE_REDUCTION, ALGO_RECURRENCE = 0, 1, 2, 3, 4
 TUNE_RECURRENCE, TUNE_SINGLE_REDUCTION = 1, 2
 DOT_NATIVE, DOT_FP64, DOT_FLOAT2 = 0, 1, 2
-STORAGE_AUTO, STORAGE_REGISTERS, STORAGE_SHARED, STORAGE_SPLIT, STORAGE_HYBRID = 0, 1, 2, 3, 4
+STORAGE_AUTO, STORAGE_REGISTERS, STORAGE_SHARED, STORAGE_SPLIT, STORAGE_HYBRID, STORAGE_TMEM = 0, 1, 2, 3, 4, 5
 
 
 class GbdpcgError(RuntimeError):

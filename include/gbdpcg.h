@@ -90,13 +90,16 @@ enum {
  * in registers (two per thread for even n), Phi^-1 in shared memory; HYBRID:
  * the sub-diagonal and diagonal blocks of S in registers, its super-diagonal
  * block and Phi^-1 in shared memory (more rows per SM; FP32, block-diagonal
- * Phi^-1) */
+ * Phi^-1); TMEM: the diagonal block of S in registers, its off-diagonal
+ * blocks in the SM's tensor memory, Phi^-1 in shared memory (the most rows
+ * per SM; FP32, block-diagonal Phi^-1, even n; one CTA per SM) */
 enum {
     GBDPCG_STORAGE_AUTO = 0,
     GBDPCG_STORAGE_REGISTERS = 1,
     GBDPCG_STORAGE_SHARED = 2,
     GBDPCG_STORAGE_SPLIT = 3,
-    GBDPCG_STORAGE_HYBRID = 4
+    GBDPCG_STORAGE_HYBRID = 4,
+    GBDPCG_STORAGE_TMEM = 5
 };
 
 typedef struct {
@@ -297,7 +300,7 @@ GBDPCG_API int gbdpcg_plan_launch_count(gbdpcg_plan_t plan, uint32_t *launches);
 GBDPCG_API int gbdpcg_plan_launch_info(gbdpcg_plan_t plan, uint32_t i, uint32_t *cluster, uint32_t *threads,
                             uint32_t *kmax, uint32_t *systems, uint32_t *ctas);
 /* Kernel of launch i: storage (0 S and Phi^-1 in registers, 1 S in registers
- * and Phi^-1 in shared memory, 2 both in shared memory, 3 hybrid), matrix rows per
+ * and Phi^-1 in shared memory, 2 both in shared memory, 3 hybrid, 4 tensor memory), matrix rows per
  * thread, and algorithm (GBDPCG_ALGO_CLUSTER, _SINGLE_REDUCTION, _RECURRENCE,
  * or _PLAIN for a one-system plain launch; refinement launches report 0). */
 GBDPCG_API int gbdpcg_plan_launch_kernel(gbdpcg_plan_t plan, uint32_t i, uint32_t *storage,

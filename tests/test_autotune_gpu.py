@@ -52,7 +52,7 @@ def test_autotuned_plan_matches_oracle(gb, oracle_mod, handle):
     assert sum(l["systems"] for l in after) == len(systems)
     assert len(after) <= len(before)
     for l in after:
-        assert 1 <= l["cluster"] <= 16 and l["threads"] % 32 == 0 and l["storage"] in (0, 1, 2)
+        assert 1 <= l["cluster"] <= 16 and l["threads"] % 32 == 0 and l["storage"] in (0, 1, 2, 3, 4)
     for s in systems:
         assert bool((s["lambda"] == 7.0).all())
         s["lambda"].zero_()

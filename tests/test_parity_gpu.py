@@ -127,8 +127,9 @@ def test_cluster_sizes_agree(gb, oracle_mod, handle, C):
 def test_storage_and_layout_bitwise(gb, oracle_mod, handle):
     """Registers vs shared-memory rows, and compact vs cbtd block-diagonal Phi^-1,
     give identical bits (same summation order; padded entries are exact zeros).
-    With two rows per thread (even n), S in registers and the hybrid storage
-    (two blocks of S in registers, one in shared memory) agree bit for bit too."""
+    With two rows per thread (even n), S in registers, the hybrid storage (two
+    blocks of S in registers, one in shared memory) and the tensor-memory
+    storage (off-diagonal blocks in TMEM) agree bit for bit too."""
     import torch
     O = oracle_mod
     n, N = 12, 50
@@ -145,8 +146,9 @@ def test_storage_and_layout_bitwise(gb, oracle_mod, handle):
     one_row = [run(layout, P, storage) for layout, P in ((gb.PINV_BLOCKDIAG, Pc), (gb.PINV_CBTD, Pt))
                for storage in (gb.STORAGE_REGISTERS, gb.STORAGE_SHARED)]
     assert all(o == one_row[0] for o in one_row), [o[0] for o in one_row]
-    two_rows = [run(gb.PINV_BLOCKDIAG, Pc, storage) for storage in (gb.STORAGE_SPLIT, gb.STORAGE_HYBRID)]
-    assert two_rows[0] == two_rows[1], [o[0] for o in two_rows]
+    two_rows = [run(gb.PINV_BLOCKDIAG, Pc, storage)
+                for storage in (gb.STORAGE_SPLIT, gb.STORAGE_HYBRID, gb.STORAGE_TMEM)]
+    assert all(o == two_rows[0] for o in two_rows), [o[0] for o in two_rows]
 
 
 def test_dot_fp64_accumulation(gb, oracle_mod, handle):
@@ -268,7 +270,7 @@ def test_batched_plan_matches_single(gb, oracle_mod, handle):
 
 
 @pytest.mark.parametrize("dts", ["f32", "f64"])
-@pytest.mark.parametrize("storage", ["registers", "shared", "split", "hybrid"])
+@pytest.mark.parametrize("storage", ["registers", "shared", "split", "hybrid", "tmem"])
 @pytest.mark.parametrize("n,N", [(6, 70), (14, 128), (24, 100), (7, 33)])
 def test_every_storage_variant(gb, oracle_mod, handle, dts, storage, n, N):
     """Each way of holding the rows (registers; shared memory; S in registers
@@ -284,7 +286,7 @@ def test_every_storage_variant(gb, oracle_mod, handle, dts, storage, n, N):
     d = torch.device("cuda:0")
     lam = torch.zeros(n * N, dtype=torch.float64 if dts == "f64" else torch.float32, device=d)
     st = {"registers": gb.STORAGE_REGISTERS, "shared": gb.STORAGE_SHARED, "split": gb.STORAGE_SPLIT,
-          "hybrid": gb.STORAGE_HYBRID}[storage]
+          "hybrid": gb.STORAGE_HYBRID, "tmem": gb.STORAGE_TMEM}[storage]
     try:
         r = handle.solve(*(torch.from_numpy(a).to(d) for a in (S, P, g)), lam, n, N, gb.PINV_BLOCKDIAG,
                          gb.config(max_iter=500, exit_tol=tol, exit_mode=gb.EXIT_RELRES, storage=st))
@@ -352,7 +354,7 @@ def test_single_reduction_rejects_tridiagonal_pinv(gb, oracle_mod, handle):
 
 
 @pytest.mark.parametrize("dts", ["f32", "f64"])
-@pytest.mark.parametrize("storage", ["auto", "registers", "shared", "split", "hybrid"])
+@pytest.mark.parametrize("storage", ["auto", "registers", "shared", "split", "hybrid", "tmem"])
 @pytest.mark.parametrize("n,N,C,layout", [(14, 128, 0, "compact"), (6, 64, 1, "compact"), (24, 100, 0, "compact"),
                                           (12, 40, 3, "compact"), (7, 19, 2, "compact"), (14, 1, 0, "compact"),
                                           (14, 64, 4, "cbtd"), (5, 30, 2, "cbtd")])
@@ -370,7 +372,7 @@ def test_recurrence_vs_oracle(gb, oracle_mod, handle, dts, storage, n, N, C, lay
     d = torch.device("cuda:0")
     lam = torch.zeros(n * N, dtype=torch.float64 if dts == "f64" else torch.float32, device=d)
     st = {"auto": gb.STORAGE_AUTO, "registers": gb.STORAGE_REGISTERS, "shared": gb.STORAGE_SHARED,
-          "split": gb.STORAGE_SPLIT, "hybrid": gb.STORAGE_HYBRID}[storage]
+          "split": gb.STORAGE_SPLIT, "hybrid": gb.STORAGE_HYBRID, "tmem": gb.STORAGE_TMEM}[storage]
     lay = gb.PINV_BLOCKDIAG if layout == "compact" else gb.PINV_CBTD
     try:
         r = handle.solve(*(torch.from_numpy(a).to(d) for a in (S, P, g)), lam, n, N, lay,

@@ -51,8 +51,8 @@ __host__ __device__ constexpr size_t round_up(size_t x, size_t m) { return (x + 
 // registers, Phi^-1 in shared memory; ST_SMEM both in shared memory; ST_HYB
 // the sub-diagonal and diagonal blocks of S in registers, the super-diagonal
 // block of S and Phi^-1 (block-diagonal) in shared memory; ST_TMEM the
-// diagonal block of S in registers, its two off-diagonal blocks in tensor
-// memory, Phi^-1 (block-diagonal) in shared memory.
+// diagonal block of S in registers, its two off-diagonal blocks and Phi^-1
+// (block-diagonal) in tensor memory.
 enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2, ST_HYB = 3, ST_TMEM = 4 };
 
 // A CTA of the tensor-memory storage allocates all of its SM's tensor memory;
@@ -78,7 +78,7 @@ struct SmemPlan {
                               : 0;
     }
     __host__ __device__ static size_t mat_p(uint32_t kmax) {
-        return ST >= ST_REG_S ? round_up((size_t)kmax * NB_P * NP * NP * sizeof(T), 32) : 0;
+        return (ST >= ST_REG_S && ST != ST_TMEM) ? round_up((size_t)kmax * NB_P * NP * NP * sizeof(T), 32) : 0;
     }
     __host__ __device__ static size_t slots(uint32_t C) {
         return round_up(2 * kMaxValues * slot_stride(C) * sizeof(A), 32);
@@ -285,8 +285,8 @@ __host__ __device__ constexpr int tmem_cols() { return (NP + 7) / 8 * 8; }
 
 // Block-row matvec of the tensor-memory storage, two rows per thread: blocks
 // 0 and 2 (sub- and super-diagonal) from this thread's TMEM lane at trow
-// (row q, block bi at columns (2q + bi) * NPT), block 1 (diagonal) from
-// registers.  Same chains and summation order as reg_matvec.  Warp-wide: every
+// (row q: S block 0 at columns 3q NPT, S block 2 at (3q + 1) NPT, Phi^-1 at
+// (3q + 2) NPT), block 1 (diagonal) from registers.  Same chains and summation order as reg_matvec.  Warp-wide: every
 // thread of the warp calls it (inactive rows read a valid window and discard
 // the result).
 // Elements [8c, 8c+8) of an NP-element window (those below NP), loaded with
@@ -323,7 +323,7 @@ __device__ __forceinline__ void tmem_matvec(const float (&Md)[2][NP], uint32_t t
 #pragma unroll
         for (int c = 0; c < NPT / 8; ++c) {
             float m0[8], m1[8], xv[8];
-            tmem_ld8x2(trow + (0 * 2 + bi) * NPT + 8 * c, trow + (1 * 2 + bi) * NPT + 8 * c, m0, m1);
+            tmem_ld8x2(trow + (0 * 3 + bi) * NPT + 8 * c, trow + (1 * 3 + bi) * NPT + 8 * c, m0, m1);
             lds_chunk8<NP>(xv, x + b * NP, c);
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
@@ -355,6 +355,31 @@ __device__ __forceinline__ void tmem_matvec(const float (&Md)[2][NP], uint32_t t
         s += acc[q][2];
         y[q] = s;
     }
+}
+
+// Phi^-1 (block-diagonal) times the centre block of the window, two rows per
+// thread, from TMEM columns (3q + 2) NPT.  Same chain as smem_matvec's.
+// Warp-wide, like tmem_matvec.
+template <int NP>
+__device__ __forceinline__ void tmem_pmatvec(uint32_t trow, const float *x, float (&y)[2]) {
+    constexpr int NPT = tmem_cols<NP>();
+    __syncwarp();
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int c = 0; c < NPT / 8; ++c) {
+        float m0[8], m1[8], xv[8];
+        tmem_ld8x2(trow + 2 * NPT + 8 * c, trow + 5 * NPT + 8 * c, m0, m1);
+        lds_chunk8<NP>(xv, x + NP, c);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (8 * c + u < NP) {
+                a0 = fma_rn(m0[u], xv[u], a0);
+                a1 = fma_rn(m1[u], xv[u], a1);
+            }
+        }
+    }
+    y[0] = a0;
+    y[1] = a1;
 }
 
 // Stage the block rows of knots [kb, kb+nk) (blk = NB n^2 elements each,
@@ -513,7 +538,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     static_assert(!S_HYB || !PTRI, "the hybrid storage keeps a block-diagonal Phi^-1");
     static_assert(!S_TM || (!PTRI && RPT == 2 && sizeof(T) == 4), "tensor-memory storage: FP32, two rows per thread");
     constexpr int NPT = tmem_cols<NP>();
-    static_assert(!S_TM || (RegBudget<T, A, NP, PTRI, ST, RPT>::max_threads + 127) / 128 * RPT * 2 * NPT <=
+    static_assert(!S_TM || (RegBudget<T, A, NP, PTRI, ST, RPT>::max_threads + 127) / 128 * RPT * 3 * NPT <=
                                (int)kTmemColumns,
                   "the warps of a CTA fit the tensor memory's columns");
     const cg::cluster_group cluster = cg::this_cluster();
@@ -536,7 +561,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
 
     for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
     // tensor memory: warp 0 allocates every column (the CTA is alone on its SM);
-    // warp w reaches lanes (w % 4) * 32 + lane, its rows at columns (w / 4) * 2 RPT NPT
+    // warp w reaches lanes (w % 4) * 32 + lane, its rows at columns (w / 4) * 3 RPT NPT
     uint32_t tbase = 0, trow = 0;
     if constexpr (S_TM) {
         if ((tid >> 5) == 0) tmem_alloc(s_item + 1, kTmemColumns);
@@ -544,7 +569,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         __syncthreads();
         tmem_fence_after_sync();
         tbase = *reinterpret_cast<volatile uint32_t *>(s_item + 1);
-        trow = tbase + ((((tid >> 5) & 3u) * 32u) << 16) + (tid >> 7) * (uint32_t)(RPT * 2 * NPT);
+        trow = tbase + ((((tid >> 5) & 3u) * 32u) << 16) + (tid >> 7) * (uint32_t)(RPT * 3 * NPT);
     }
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     for (uint32_t pass = 0;; ++pass) {
@@ -633,8 +658,23 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                             const uint32_t j = 8 * cc + u;
                             v[u] = (present && j < n) ? __ldg(Sk + (b * n + j) * n + i + q) : 0.f;
                         }
-                        tmem_st8(trow + (q * 2 + bi) * NPT + 8 * cc, v);
+                        tmem_st8(trow + (q * 3 + bi) * NPT + 8 * cc, v);
                     }
+                }
+            }
+            // Phi^-1 (compact, n^2 per knot) at columns (3q + 2) NPT
+            const T *Pk = P + (size_t)k * n * n;
+#pragma unroll 1
+            for (int q = 0; q < RPT; ++q) {
+#pragma unroll 1
+                for (int cc = 0; cc < NPT / 8; ++cc) {
+                    float v[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const uint32_t j = 8 * cc + u;
+                        v[u] = (act && j < n) ? __ldg(Pk + j * n + i + q) : 0.f;
+                    }
+                    tmem_st8(trow + (q * 3 + 2) * NPT + 8 * cc, v);
                 }
             }
             tmem_wait_st();
@@ -642,7 +682,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             const T *Sg = S + (size_t)kb * blkS;
             stage_rows(ms, R, Sg, nk, n, blkS, tid, nthr);
         }
-        if constexpr (P_REG) {
+        if constexpr (S_TM) {
+            // Phi^-1 went to tensor memory with the off-diagonal S blocks
+        } else if constexpr (P_REG) {
             const T *Pk = P + (size_t)k * blkP;
 #pragma unroll
             for (int b = 0; b < NBP; ++b) {
@@ -668,7 +710,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             else smem_matvec<T, NP, 3, RPT>(ms, R, lk * n + i, sb0, sb1, x, n, y);
         };
         auto matP = [&](const T *x, T(&y)[RPT]) {
-            if constexpr (P_REG) {
+            if constexpr (S_TM) {
+                tmem_pmatvec<NP>(trow, x, y);
+            } else if constexpr (P_REG) {
                 if constexpr (PTRI) reg_matvec<T, NP, 3, RPT>(Pr, x, y);
                 else reg_matvec<T, NP, 1, RPT>(Pr, x + NP, y);
             } else {
@@ -690,6 +734,22 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 else {
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) y[q] = T(0);
+                }
+            }
+        };
+        // z = Phi^-1 r over this thread's rows, the same way
+        auto matP_rows = [&](T(&z)[RPT]) {
+            if constexpr (S_TM) {
+                matP(vr + (act ? lk : 0u) * NP, z);
+                if (!act) {
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) z[q] = T(0);
+                }
+            } else {
+                if (act) matP(vr + lk * NP, z);
+                else {
+#pragma unroll
+                    for (int q = 0; q < RPT; ++q) z[q] = T(0);
                 }
             }
         };
@@ -737,7 +797,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         } else {
             __syncthreads();
         }
-        if (act) matP(vr + lk * NP, z);
+        matP_rows(z);
 #pragma unroll
         for (int q = 0; q < RPT; ++q) {
             if (!act) z[q] = T(0);
@@ -815,11 +875,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                     }
                 }
                 __syncthreads();
-                if (act) matP(vr + lk * NP, z);
-                else {
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) z[q] = T(0);
-                }
+                matP_rows(z);
                 // z into the vp window (own rows; boundary into the neighbours' halos)
                 if (act) {
 #pragma unroll
@@ -899,11 +955,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                     }
                 }
                 __syncthreads();
-                if (act) matP(vr + lk * NP, z);
-                else {
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) z[q] = T(0);
-                }
+                matP_rows(z);
                 if (first_knot) {
                     T *dst = cluster.map_shared_rank(zh, rank - 1) + NP + i;
 #pragma unroll

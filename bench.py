@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--no-extras", action="store_true", help="skip the baselines and the other configurations")
     ap.add_argument("--algorithm", default="auto", choices=["auto", "standard", "recurrence", "single-reduction"])
+    ap.add_argument("--storage", default="auto", choices=["auto", "registers", "shared", "split", "hybrid", "tmem"],
+                    help="pin where the cluster solver keeps the matrix rows (profiling; default: the tuner's choice)")
+    ap.add_argument("--cluster-size", type=int, default=0, help="pin the CTAs per system (profiling; 0: chosen)")
     ap.add_argument("--host-pieces", type=int, default=0,
                     help="pieces the end-to-end path pipelines copies and solves in (0: automatic)")
     ap.add_argument("--tune", default="shapes+recurrence", choices=["off", "shapes", "shapes+recurrence", "shapes+algorithms"],
@@ -436,8 +439,10 @@ def main():
     h = gbdpcg.Handle(local)
     algo = {"auto": gbdpcg.ALGO_AUTO, "standard": gbdpcg.ALGO_CLUSTER, "recurrence": gbdpcg.ALGO_RECURRENCE,
             "single-reduction": gbdpcg.ALGO_SINGLE_REDUCTION}[args.algorithm]
+    storage = {"auto": gbdpcg.STORAGE_AUTO, "registers": gbdpcg.STORAGE_REGISTERS, "shared": gbdpcg.STORAGE_SHARED,
+               "split": gbdpcg.STORAGE_SPLIT, "hybrid": gbdpcg.STORAGE_HYBRID, "tmem": gbdpcg.STORAGE_TMEM}[args.storage]
     cfg = gbdpcg.config(max_iter=MAX_ITER, exit_tol=TOL, exit_mode=gbdpcg.EXIT_RELRES, zero_guess=1, algorithm=algo,
-                        host_pieces=args.host_pieces)
+                        host_pieces=args.host_pieces, storage=storage, cluster_size=args.cluster_size)
     plan = gbdpcg.Plan(h, layout=gbdpcg.PINV_BLOCKDIAG, cfg=cfg, packed=(descs, dS, dP, dg, dl))
     plan.build_block_jacobi()
     torch.cuda.synchronize()
@@ -526,7 +531,8 @@ def main():
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, see config)",
-        "config": {"workload": WORKLOAD, "algorithm": args.algorithm, "systems_per_gpu": count,
+        "config": {"workload": WORKLOAD, "algorithm": args.algorithm, "storage": args.storage,
+                   "cluster_size": args.cluster_size, "systems_per_gpu": count,
                    "global_batch": count * world,
                    "seeds": f"rank*{count} + [0, {count})", "l2": "inputs (1.1 GB/GPU) larger than L2",
                    "parallelism": f"replicas{world} (independent systems per GPU)",

@@ -9,8 +9,9 @@ are solved by one CUDA-graph replay of the persistent cluster launches.
 
 Printed JSON line (rank 0):
   value      solves/s with inputs resident in HBM (inputs, 1.1 GB, exceed L2)
-  e2e        solves/s through gbdpcg_plan_execute_host from pinned host
-             buffers, host<->device copies inside the timed region
+  e2e        solves/s through gbdpcg_plan_solve_host (the batched pcg_solve:
+             S and gamma in, Phi^-1 built on the GPU, lambda out) from pinned
+             host buffers, host<->device copies inside the timed region
   roofline   bytes model: sizeof(T)*[(3N-2)n^2 + N n^2 + 6nN] per PCG
              iteration per system (S and Phi^-1 block rows once, vectors
              p, r, lambda read and written), summed over the iterations each
@@ -484,20 +485,29 @@ def main():
     ms_step = ms / args.steps
     value = whole_job_rate(world, count, args.steps, ms / 1e3)
 
-    # ---- end to end from pinned host buffers through the C ABI
+    # ---- end to end from pinned host buffers through the C ABI: the batched
+    # pcg_solve (S and gamma in, Phi^-1 built on the device, lambda and the
+    # results out), every copy inside the timed region
     hS = torch.from_numpy(Sa).pin_memory()
     hP = dP.cpu().pin_memory()
     hg = torch.from_numpy(ga).pin_memory()
     hl = torch.zeros(ga.size, dtype=torch.float32).pin_memory()
-    plan.execute_host(hS, hP, hg, hl)  # warm
+    plan.solve_host(hS, hg, hl)  # warm
     barrier()
     t0 = time.perf_counter()
     e2e_steps = max(3, args.steps // 4)
     for _ in range(e2e_steps):
-        plan.execute_host(hS, hP, hg, hl, with_results=True)
+        plan.solve_host(hS, hg, hl, with_results=True)
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
-    h2d = (hS.numel() + hP.numel() + hg.numel()) * 4
+    h2d = (hS.numel() + hg.numel()) * 4
     d2h = hl.numel() * 4 + count * 24
+    # the same with a host-built Phi^-1 copied in as well (solvePCG with Pinv)
+    plan.execute_host(hS, hP, hg, hl)  # warm
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        plan.execute_host(hS, hP, hg, hl, with_results=True)
+    e2e_p_s = max_over_ranks(time.perf_counter() - t0, world, dev)
 
     if rank != 0:
         if world > 1:
@@ -552,7 +562,12 @@ def main():
                                     "frac": compulsory / (ms_step / 1e3) / 1e9 / hbm},
                      "fp32_flops_per_step": flops, "fp32_tflops": flops / (ms_step / 1e3) / 1e12},
         "e2e": {"value": whole_job_rate(world, count, e2e_steps, e2e_s), "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h,
+                "path": "gbdpcg_plan_solve_host (batched pcg_solve): S, gamma in; Phi^-1 built on the GPU; "
+                        "lambda and results out; pinned host memory",
+                "with_pinv_copied": {"value": whole_job_rate(world, count, e2e_steps, e2e_p_s), "unit": "solves/s",
+                                     "h2d_bytes_per_step": h2d + hP.numel() * 4,
+                                     "path": "gbdpcg_plan_execute_host (solvePCG with Pinv)"}},
         "gpu_launches": len(launches) * args.steps,
         "clocks": clocks,
     }

@@ -1144,11 +1144,20 @@ int build_pieces(gbdpcg_plan_s *p) {
 
 extern "C" {
 
-int gbdpcg_plan_execute_host(gbdpcg_plan_t p, const void *h_S, const void *h_Pinv,
-                             const void *h_gamma, void *h_lambda, gbdpcg_result *h_results,
-                             gbdpcg_stream_t stream_) {
+}  // extern "C"
+
+namespace {
+
+// End-to-end execution of a packed plan from host arenas; with build_pinv the
+// block-Jacobi Phi^-1 is built on the device from the copied S (per piece,
+// right before that piece's solve) instead of being copied.
+int host_run(gbdpcg_plan_s *p, const void *h_S, const void *h_Pinv, const void *h_gamma, void *h_lambda,
+             gbdpcg_result *h_results, gbdpcg_stream_t stream_, bool build_pinv) {
     if (!p || !h_lambda) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
     if (!p->packed) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan was not created packed");
+    if (build_pinv)
+        for (auto &d : p->descs)
+            if (d.n > 32) return fail(GBDPCG_ERR_UNSUPPORTED, "block-Jacobi builder needs n <= 32");
     HandleScope scope(p->h->device);
     cudaStream_t st = (cudaStream_t)stream_;
     if (!p->pieces_built) {
@@ -1179,7 +1188,9 @@ int gbdpcg_plan_execute_host(gbdpcg_plan_t p, const void *h_S, const void *h_Pin
             const auto &pc = p->pieces[j];
             cudaStream_t cs = p->piece_streams[j % p->piece_streams.size()];
             GB_CUDA(cudaStreamWaitEvent(cs, p->piece_events[j], 0));
-            int rc = gbdpcg_plan_execute(pc.plan, cs);
+            int rc;
+            if (build_pinv && (rc = gbdpcg_plan_build_block_jacobi(pc.plan, cs))) return rc;
+            rc = gbdpcg_plan_execute(pc.plan, cs);
             if (rc) return rc;
             if (pc.V1 > pc.V0)
                 GB_CUDA(cudaMemcpyAsync(static_cast<char *>(h_lambda) + pc.V0,
@@ -1202,12 +1213,30 @@ int gbdpcg_plan_execute_host(gbdpcg_plan_t p, const void *h_S, const void *h_Pin
                                          cudaMemcpyHostToDevice, st));
     if (!p->cfg.zero_guess)
         GB_CUDA(cudaMemcpyAsync(p->arena_l, h_lambda, p->bytes_vec, cudaMemcpyHostToDevice, st));
-    int rc = gbdpcg_plan_execute(p, stream_);
+    int rc;
+    if (build_pinv && (rc = gbdpcg_plan_build_block_jacobi(p, stream_))) return rc;
+    rc = gbdpcg_plan_execute(p, stream_);
     if (rc) return rc;
     GB_CUDA(cudaMemcpyAsync(h_lambda, p->arena_l, p->bytes_vec, cudaMemcpyDeviceToHost, st));
     if (h_results) return gbdpcg_plan_results(p, h_results, stream_);
     GB_CUDA(cudaStreamSynchronize(st));
     return GBDPCG_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbdpcg_plan_execute_host(gbdpcg_plan_t p, const void *h_S, const void *h_Pinv,
+                             const void *h_gamma, void *h_lambda, gbdpcg_result *h_results,
+                             gbdpcg_stream_t stream) {
+    return host_run(p, h_S, h_Pinv, h_gamma, h_lambda, h_results, stream, false);
+}
+
+int gbdpcg_plan_solve_host(gbdpcg_plan_t p, const void *h_S, const void *h_gamma, void *h_lambda,
+                           gbdpcg_result *h_results, gbdpcg_stream_t stream) {
+    if (!h_S || !h_gamma) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    return host_run(p, h_S, nullptr, h_gamma, h_lambda, h_results, stream, true);
 }
 
 int gbdpcg_plan_build_block_jacobi(gbdpcg_plan_t p, gbdpcg_stream_t stream) {

@@ -93,6 +93,7 @@ _SIGS = {
     "gbdpcg_plan_execute": ([_P, _P], _I),
     "gbdpcg_plan_create_packed": ([_P, _I, _P, _U, _P, _P, _P, _P, _U, _P, _P], _I),
     "gbdpcg_plan_execute_host": ([_P, _P, _P, _P, _P, _P, _P], _I),
+    "gbdpcg_plan_solve_host": ([_P, _P, _P, _P, _P, _P], _I),
     "gbdpcg_plan_build_block_jacobi": ([_P, _P], _I),
     "gbdpcg_plan_results": ([_P, _P, _P], _I),
     "gbdpcg_plan_launch_count": ([_P, _P], _I),
@@ -314,6 +315,17 @@ class Plan:
         _check(lib().gbdpcg_plan_execute_host(self.p, ptr(h_S), ptr(h_P), ptr(h_g), ptr(h_l),
                                               ctypes.cast(res, ctypes.c_void_p) if res is not None else None,
                                               _stream(stream)), "gbdpcg_plan_execute_host")
+        return list(res) if res is not None else None
+
+    def solve_host(self, h_S, h_g, h_l, with_results=False, stream=None):
+        """pcg_solve over the batch from host arrays: S and gamma in, Phi^-1 built
+        on the device, lambda out."""
+        def ptr(a):
+            return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data_as(ctypes.c_void_p)
+        res = (Result * self.count)() if with_results else None
+        _check(lib().gbdpcg_plan_solve_host(self.p, ptr(h_S), ptr(h_g), ptr(h_l),
+                                            ctypes.cast(res, ctypes.c_void_p) if res is not None else None,
+                                            _stream(stream)), "gbdpcg_plan_solve_host")
         return list(res) if res is not None else None
 
     def build_block_jacobi(self, stream=None):

@@ -290,6 +290,15 @@ GBDPCG_API int gbdpcg_plan_create_packed(gbdpcg_handle_t h, int dtype,
 GBDPCG_API int gbdpcg_plan_execute_host(gbdpcg_plan_t plan, const void *h_S, const void *h_Pinv,
                                         const void *h_gamma, void *h_lambda,
                                         gbdpcg_result *h_results, gbdpcg_stream_t stream);
+/* Batched counterpart of the reference's documented pcg_solve(S, gamma,
+ * lambda, stateSize, knotPoints, config) (README.md:42), which takes no Phi^-1:
+ * copies S and gamma of a packed plan from the host, builds each system's
+ * block-Jacobi Phi^-1 on the device into the plan's Pinv arena, solves, copies
+ * lambda (and, if non-NULL, the results) back, and waits.  Pipelined in pieces
+ * like gbdpcg_plan_execute_host (each piece's Phi^-1 is built right after its
+ * copy).  n <= 32. */
+GBDPCG_API int gbdpcg_plan_solve_host(gbdpcg_plan_t plan, const void *h_S, const void *h_gamma, void *h_lambda,
+                                      gbdpcg_result *h_results, gbdpcg_stream_t stream);
 /* Builds every system's block-Jacobi Phi^-1 into its Pinv pointer (stream-ordered). */
 GBDPCG_API int gbdpcg_plan_build_block_jacobi(gbdpcg_plan_t plan, gbdpcg_stream_t stream);
 /* Waits for the stream and copies `count` results out. */

@@ -221,12 +221,15 @@ def test_warm_start_and_zero_rhs(gb, oracle_mod, handle):
     assert r.iters == 1 and r.status == gb.CONVERGED and not lam0.any()
 
 
-def test_pcg_solve_builds_block_jacobi(gb, oracle_mod, handle):
-    """pcg_solve without Pinv: the GPU builds blockdiag(S_kk^-1)."""
+@pytest.mark.parametrize("n", [6, 14, 24, 32, 5])
+def test_pcg_solve_builds_block_jacobi(gb, oracle_mod, handle, n):
+    """pcg_solve without Pinv: the GPU builds blockdiag(S_kk^-1) (warp
+    Gauss-Jordan inverse) to within FP32 / FP64 rounding of the FP64
+    Cholesky-based oracle."""
     import torch
     O = oracle_mod
     for dt, tol in ((np.float32, 2e-5), (np.float64, 1e-12)):
-        n, N = 14, 40
+        N = 40
         sy = O.generate(n, N, 5)
         S = sy.cbtd(dt)
         d = torch.device("cuda:0")

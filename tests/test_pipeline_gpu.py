@@ -85,3 +85,35 @@ def test_out_of_order_arenas_fall_back(gb, oracle_mod, handle):
     l_fwd, r_fwd, _, _ = _run_host(gb, handle, descs, Sa, Pa, ga, pieces=4)
     assert r_rev == list(reversed(r_fwd))
     assert l_rev.tobytes() == l_fwd.tobytes()
+
+
+@pytest.mark.parametrize("pieces", [1, 4])
+def test_solve_host_builds_pinv_on_device(gb, oracle_mod, handle, pieces):
+    """The batched pcg_solve (S and gamma from the host, block-Jacobi Phi^-1
+    built on the device) gives the bits of building Phi^-1 on the device and
+    executing the plan there."""
+    import torch
+    O = oracle_mod
+    descs, Sa, ga, nP = _packed(gb, 120, 4700)
+    d = torch.device("cuda:0")
+    handle.tune_clear()
+    cfg = gb.config(max_iter=300, exit_tol=1e-6, exit_mode=gb.EXIT_RELRES, zero_guess=1, host_pieces=pieces)
+    dS = torch.zeros(Sa.size, device=d)
+    dP = torch.full((nP,), float("nan"), device=d)  # nothing may read a Phi^-1 the call did not build
+    dg = torch.zeros(ga.size, device=d)
+    dl = torch.zeros(ga.size, device=d)
+    plan = gb.Plan(handle, layout=gb.PINV_BLOCKDIAG, cfg=cfg, packed=(descs, dS, dP, dg, dl))
+    hS = torch.from_numpy(Sa).pin_memory()
+    hg = torch.from_numpy(ga).pin_memory()
+    hl = torch.full((ga.size,), 9.0).pin_memory()
+    res = plan.solve_host(hS, hg, hl, with_results=True)
+    out = hl.numpy().copy()
+    assert all(r.status == gb.CONVERGED for r in res)
+    dl.zero_()
+    plan.build_block_jacobi()
+    plan.execute()
+    torch.cuda.synchronize()
+    assert dl.cpu().numpy().tobytes() == out.tobytes()
+    for (n, N, oS, oP, oV) in descs[::13]:
+        assert O.relres(Sa[oS:oS + 3 * n * n * N], out[oV:oV + n * N], ga[oV:oV + n * N], n, N) < 1e-3
+    plan.close()

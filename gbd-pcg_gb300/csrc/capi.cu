@@ -1092,7 +1092,7 @@ int build_pieces(gbdpcg_plan_s *p) {
     p->pieces_built = true;
     const uint32_t count = p->count;
     uint32_t k = p->cfg.host_pieces;
-    if (k == 0) k = std::min<uint32_t>(16, std::max<uint32_t>(1, count / 256));
+    if (k == 0) k = std::min<uint32_t>(8, std::max<uint32_t>(1, count / 512));
     k = std::min(k, count);
     if (k <= 1 || !p->plain_items.empty()) return GBDPCG_SUCCESS;
     const auto &L = p->packed_list;
@@ -1127,7 +1127,7 @@ int build_pieces(gbdpcg_plan_s *p) {
         p->pieces.push_back(pc);
     }
     GB_CUDA(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
-    for (int j = 0; j < 2; ++j) {
+    for (int j = 0; j < 2; ++j) {  // consecutive pieces overlap
         cudaStream_t st;
         GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         p->piece_streams.push_back(st);

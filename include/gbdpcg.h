@@ -116,7 +116,8 @@ typedef struct {
     uint32_t max_outer;      /* refinement: outer steps (default 50) */
     uint32_t streams;        /* plans: streams the launches of one execution spread over (default 8) */
     uint32_t host_pieces;    /* packed plans: pieces gbdpcg_plan_execute_host pipelines (copies of
-                                piece i+1 overlap the solve of piece i); 0 = automatic, 1 = none */
+                                piece i+1 overlap the solve of piece i); 0 = automatic (about 512
+                                systems a piece, at most 8), 1 = none */
     double inner_tol;        /* refinement: relative residual of each FP32 inner solve (default 0.05) */
 } gbdpcg_config;
 

@@ -100,6 +100,8 @@ _SIGS = {
     "gbdpcg_plan_launch_info": ([_P, _U, _P, _P, _P, _P, _P], _I),
     "gbdpcg_plan_launch_kernel": ([_P, _U, _P, _P, _P], _I),
     "gbdpcg_plan_destroy": ([_P], _I),
+    "gbdpcg_csr_to_cbtd_f32": ([_P, _P, _P, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_csr_to_cbtd_f64": ([_P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_plan_autotune": ([_P, _U, _U, _P], _I),
     "gbdpcg_tune_export": ([_P, _P, ctypes.c_size_t, _P], _I),
     "gbdpcg_tune_import": ([_P, ctypes.c_char_p], _I),
@@ -422,3 +424,10 @@ def pcg_solve_autograd(S, Pinv, gamma, n, N, layout=PINV_BLOCKDIAG, **cfg_kw):
     if _fn is None:
         _fn = _make_fn()
     return _fn.apply(S, Pinv, gamma, n, N, layout, cfg_kw)
+
+
+def csr_to_cbtd(row_ptr, col_ind, val, n, N, out, err, stream=None):
+    """CSR (device tensors: uint32-compatible int32 row_ptr / col_ind, values)
+    -> cbtd `out` (3 n^2 N); `err` is a one-element int32 device tensor."""
+    fn = lib().gbdpcg_csr_to_cbtd_f64 if val.dtype.itemsize == 8 else lib().gbdpcg_csr_to_cbtd_f32
+    _check(fn(_tp(row_ptr), _tp(col_ind), _tp(val), n, N, _tp(out), _tp(err), _stream(stream)), "gbdpcg_csr_to_cbtd")

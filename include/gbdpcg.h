@@ -309,6 +309,19 @@ GBDPCG_API int gbdpcg_plan_launch_count(gbdpcg_plan_t plan, uint32_t *launches);
 /* Describes launch i: cluster size, threads per CTA, knots per CTA, systems, CTAs in the grid. */
 GBDPCG_API int gbdpcg_plan_launch_info(gbdpcg_plan_t plan, uint32_t i, uint32_t *cluster, uint32_t *threads,
                             uint32_t *kmax, uint32_t *systems, uint32_t *ctas);
+/* CSR -> cbtd on the device: the adapter behind the reference's solvePCG
+ * overload for csr_t matrices (include/interface.cuh:8-20, whose body exits
+ * with "NOT IMPLEMENTED"; csr_t at include/types.cuh:7-15).  A CSR matrix with
+ * n N rows and columns (row_ptr: n N + 1 entries) whose entries lie in the
+ * three diagonal blocks of their block row is scattered into d_out (3 n^2 N
+ * elements, zeroed first; duplicates add).  d_err is one device word the call
+ * uses as scratch.  Synchronous; an entry outside the band returns
+ * GBDPCG_ERR_INVALID_ARGUMENT (the other entries are written). */
+GBDPCG_API int gbdpcg_csr_to_cbtd_f32(const uint32_t *d_row_ptr, const uint32_t *d_col_ind, const float *d_val,
+                                      uint32_t n, uint32_t N, float *d_out, uint32_t *d_err, gbdpcg_stream_t stream);
+GBDPCG_API int gbdpcg_csr_to_cbtd_f64(const uint32_t *d_row_ptr, const uint32_t *d_col_ind, const double *d_val,
+                                      uint32_t n, uint32_t N, double *d_out, uint32_t *d_err, gbdpcg_stream_t stream);
+
 /* Kernel of launch i: storage (0 S and Phi^-1 in registers, 1 S in registers
  * and Phi^-1 in shared memory, 2 both in shared memory, 3 hybrid, 4 tensor memory), matrix rows per
  * thread, and algorithm (GBDPCG_ALGO_CLUSTER, _SINGLE_REDUCTION, _RECURRENCE,

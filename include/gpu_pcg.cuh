@@ -15,7 +15,8 @@
 //                      README.md:42 (documented there, not implemented in the
 //                      reference; here Phi^-1 = blockdiag(S_kk^-1) is built on
 //                      the GPU)
-//   csr_t<T>           include/types.cuh:7-15
+//   csr_t<T>           include/types.cuh:7-15 (and the CSR overload of solvePCG,
+//                      include/interface.cuh:8-20, implemented here)
 //   gpuErrchk / gpuAssert  include/gpuassert.cuh:5-14
 // Differences a caller can observe, all deliberate:
 //   * sizes are runtime arguments only; the STATE_SIZE / KNOT_POINTS macros
@@ -168,6 +169,69 @@ uint32_t solvePCG(const uint32_t state_size, const uint32_t knot_points, T *d_S,
                                   knot_points, &cfg, &res, nullptr);
     gpuErrchk(rc);
     return res.iters;
+}
+
+// CSR overload (include/interface.cuh:8-20, which exits "NOT IMPLEMENTED" in
+// the reference).  h_S and, if non-null, h_Pinv are csr_t with host arrays
+// describing n N x n N block-tridiagonal matrices (row r in knot r / n); they
+// are copied to the device and scattered into the cbtd layout there
+// (gbdpcg_csr_to_cbtd_*).  A null h_Pinv builds the block-Jacobi Phi^-1 on the
+// GPU.  Returns the iteration count; h_lambda is the initial guess on entry.
+template <typename T>
+uint32_t solvePCG(csr_t<T> *h_S, csr_t<T> *h_Pinv, T *h_gamma, T *h_lambda, unsigned stateSize,
+                  unsigned knotPoints, struct pcg_config<T> *config) {
+    static_assert(std::is_same<T, float>::value || std::is_same<T, double>::value, "float or double");
+    const uint32_t n = stateSize, N = knotPoints, rows = n * N;
+    if (!h_S || h_S->rows != rows || h_S->cols != rows || (h_Pinv && (h_Pinv->rows != rows || h_Pinv->cols != rows)))
+        gpuErrchk(GBDPCG_ERR_INVALID_ARGUMENT);
+    const size_t mat = (size_t)3 * n * n * N;
+    gbdpcg_handle_t h = gbdpcg_detail::thread_handle();
+    T *d_S = nullptr, *d_P = nullptr, *d_g = nullptr, *d_l = nullptr;
+    uint32_t *d_err = nullptr;
+    gpuErrchk(cudaMalloc(&d_S, sizeof(T) * mat) == cudaSuccess ? GBDPCG_SUCCESS : GBDPCG_ERR_NO_MEMORY);
+    gpuErrchk(cudaMalloc(&d_P, sizeof(T) * mat) == cudaSuccess ? GBDPCG_SUCCESS : GBDPCG_ERR_NO_MEMORY);
+    gpuErrchk(cudaMalloc(&d_g, sizeof(T) * rows) == cudaSuccess ? GBDPCG_SUCCESS : GBDPCG_ERR_NO_MEMORY);
+    gpuErrchk(cudaMalloc(&d_l, sizeof(T) * rows) == cudaSuccess ? GBDPCG_SUCCESS : GBDPCG_ERR_NO_MEMORY);
+    gpuErrchk(cudaMalloc(&d_err, sizeof(uint32_t)) == cudaSuccess ? GBDPCG_SUCCESS : GBDPCG_ERR_NO_MEMORY);
+    auto upload_csr = [&](const csr_t<T> *m, T *d_out) {
+        uint32_t *d_rp = nullptr, *d_ci = nullptr;
+        T *d_v = nullptr;
+        const size_t nnz = m->nnz;
+        gpuErrchk(cudaMalloc(&d_rp, sizeof(uint32_t) * (rows + 1)) == cudaSuccess ? GBDPCG_SUCCESS : GBDPCG_ERR_NO_MEMORY);
+        gpuErrchk(cudaMalloc(&d_ci, sizeof(uint32_t) * (nnz ? nnz : 1)) == cudaSuccess ? GBDPCG_SUCCESS : GBDPCG_ERR_NO_MEMORY);
+        gpuErrchk(cudaMalloc(&d_v, sizeof(T) * (nnz ? nnz : 1)) == cudaSuccess ? GBDPCG_SUCCESS : GBDPCG_ERR_NO_MEMORY);
+        cudaMemcpy(d_rp, m->row_ptr, sizeof(uint32_t) * (rows + 1), cudaMemcpyHostToDevice);
+        if (nnz) {
+            cudaMemcpy(d_ci, m->col_ind, sizeof(uint32_t) * nnz, cudaMemcpyHostToDevice);
+            cudaMemcpy(d_v, m->val, sizeof(T) * nnz, cudaMemcpyHostToDevice);
+        }
+        int rc;
+        if constexpr (std::is_same<T, float>::value) rc = gbdpcg_csr_to_cbtd_f32(d_rp, d_ci, d_v, n, N, d_out, d_err, nullptr);
+        else rc = gbdpcg_csr_to_cbtd_f64(d_rp, d_ci, d_v, n, N, d_out, d_err, nullptr);
+        cudaFree(d_rp);
+        cudaFree(d_ci);
+        cudaFree(d_v);
+        gpuErrchk(rc);
+    };
+    upload_csr(h_S, d_S);
+    if (h_Pinv) {
+        upload_csr(h_Pinv, d_P);
+    } else {
+        int rc;
+        if constexpr (std::is_same<T, float>::value) rc = gbdpcg_block_jacobi_f32(h, d_S, d_P, GBDPCG_PINV_CBTD, n, N, nullptr);
+        else rc = gbdpcg_block_jacobi_f64(h, d_S, d_P, GBDPCG_PINV_CBTD, n, N, nullptr);
+        gpuErrchk(rc);
+    }
+    cudaMemcpy(d_g, h_gamma, sizeof(T) * rows, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_l, h_lambda, sizeof(T) * rows, cudaMemcpyHostToDevice);
+    const uint32_t iters = solvePCG<T>(n, N, d_S, d_P, d_g, d_l, nullptr, nullptr, nullptr, nullptr, config);
+    cudaMemcpy(h_lambda, d_l, sizeof(T) * rows, cudaMemcpyDeviceToHost);
+    cudaFree(d_S);
+    cudaFree(d_P);
+    cudaFree(d_g);
+    cudaFree(d_l);
+    cudaFree(d_err);
+    return iters;
 }
 
 // The documented API (README.md:42): Phi^-1 is built on the GPU.

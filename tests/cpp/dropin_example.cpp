@@ -3,7 +3,8 @@
 // examples/pcg_solve.cu of the reference does.  Inputs come from a binary file
 // written by tests/test_cpp_dropin_gpu.py:
 //   uint32 n, N, dtype(4|8), with_pinv; then S (3n^2N), Pinv (3n^2N, if any),
-//   gamma (nN), lambda0 (nN).
+//   gamma (nN), lambda0 (nN).  with_pinv = 2 passes S and Pinv as csr_t (the
+//   reference's CSR overload of solvePCG), built here from the cbtd arrays.
 // Output (stdout): "iters <k>" then the solution as hex of its bytes.
 #include <stdio.h>
 #include <stdlib.h>
@@ -11,6 +12,36 @@
 #include <vector>
 
 #include "gpu_pcg.cuh"
+
+// cbtd (n x 3n column-major block row per knot) -> CSR of the n N x n N matrix
+template <typename T>
+struct HostCsr {
+    std::vector<uint32_t> row_ptr, col_ind;
+    std::vector<T> val;
+    csr_t<T> csr;
+};
+
+template <typename T>
+void to_csr(const std::vector<T> &M, uint32_t n, uint32_t N, HostCsr<T> &out) {
+    out.row_ptr.assign(1, 0);
+    for (uint32_t r = 0; r < n * N; ++r) {
+        const uint32_t k = r / n, i = r % n;
+        for (uint32_t b = 0; b < 3; ++b) {
+            if ((b == 0 && k == 0) || (b == 2 && k + 1 == N)) continue;
+            const uint32_t kc = k + b - 1;
+            for (uint32_t j = 0; j < n; ++j) {
+                const T v = M[(size_t)k * 3 * n * n + (size_t)(b * n + j) * n + i];
+                if (v != T(0)) {
+                    out.col_ind.push_back(kc * n + j);
+                    out.val.push_back(v);
+                }
+            }
+        }
+        out.row_ptr.push_back((uint32_t)out.col_ind.size());
+    }
+    out.csr = csr_t<T>{out.row_ptr.data(), out.col_ind.data(), out.val.data(), n * N, n * N,
+                       (uint32_t)out.val.size()};
+}
 
 template <typename T>
 int run(FILE *f, uint32_t n, uint32_t N, uint32_t with_pinv, uint32_t max_iter, double tol) {
@@ -22,7 +53,12 @@ int run(FILE *f, uint32_t n, uint32_t N, uint32_t with_pinv, uint32_t max_iter, 
     if (fread(lam.data(), sizeof(T), vec, f) != vec) return 2;
     pcg_config<T> config((T)tol, max_iter);
     uint32_t iters;
-    if (with_pinv)
+    if (with_pinv == 2) {
+        HostCsr<T> cS, cP;
+        to_csr(S, n, N, cS);
+        to_csr(P, n, N, cP);
+        iters = solvePCG<T>(&cS.csr, &cP.csr, g.data(), lam.data(), n, N, &config);
+    } else if (with_pinv)
         iters = solvePCG<T>(S.data(), P.data(), g.data(), lam.data(), n, N, &config);
     else
         iters = (uint32_t)pcg_solve<T>(S.data(), g.data(), lam.data(), n, N, &config);

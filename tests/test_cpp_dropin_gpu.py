@@ -34,11 +34,11 @@ def exe_plain(gb, tmp_path_factory):
                     ["-DGBDPCG_DROPIN_ALGORITHM=GBDPCG_ALGO_PLAIN"])
 
 
-def _run(exe, tmp_path, n, N, S, P, g, max_iter, tol):
+def _run(exe, tmp_path, n, N, S, P, g, max_iter, tol, csr=False):
     dt = S.dtype
     path = str(tmp_path / "in.bin")
     with open(path, "wb") as f:
-        f.write(np.array([n, N, dt.itemsize, P is not None], np.uint32).tobytes())
+        f.write(np.array([n, N, dt.itemsize, 2 if csr else int(P is not None)], np.uint32).tobytes())
         for a in (S, P, g, np.zeros(n * N, dt)):
             if a is not None:
                 f.write(np.ascontiguousarray(a, dt).tobytes())
@@ -80,3 +80,19 @@ def test_generated_through_cpp_interface(exe, oracle_mod, handle, tmp_path, dt):
     it2, lam2 = _run(exe, tmp_path, n, N, S, None, g, 200, tol)
     assert abs(it2 - it_o) <= 1
     assert O.relres(sy.cbtd(), lam2, sy.gamma, n, N) < (1e-3 if dt == np.float32 else 1e-7)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_csr_overload_through_cpp_interface(exe, oracle_mod, handle, tmp_path, dt):
+    """The reference's CSR overload of solvePCG (a stub that exits in the
+    reference): S and Phi^-1 as csr_t give the bits of the same matrices passed
+    in the cbtd layout."""
+    O = oracle_mod
+    n, N = 12, 40
+    sy = O.generate(n, N, 3)
+    S, P, g = sy.cbtd(dt), O.block_jacobi(sy.D).astype(dt), sy.gamma.astype(dt)
+    tol = 1e-6 if dt == np.float32 else 1e-12
+    it_c, lam_c = _run(exe, tmp_path, n, N, S, P, g, 200, tol)
+    it_r, lam_r = _run(exe, tmp_path, n, N, S, P, g, 200, tol, csr=True)
+    assert it_r == it_c and lam_r.tobytes() == lam_c.tobytes()

@@ -1,0 +1,227 @@
+// The steps on either side of the PCG in a trajectory-optimisation solver
+// (the callers of solvePCG in MPCGPU / GATO, outside the reference repo):
+// forming the Schur complement S and its right-hand side gamma from the
+// problem data, and recovering the primal step from the multipliers lambda.
+//
+// Problem (one system): states x_0..x_N (n each), controls u_0..u_{N-1}
+// (m each), z = (x, u); cost 1/2 z^T Theta z + g^T z with Theta =
+// blockdiag(Q_0..Q_N, R_0..R_{N-1}), Q_k = diag(Qd_k), R_k = diag(Rd_k),
+// g = (q_0..q_N, r_0..r_{N-1}); constraints C z = c with one block row
+// [A_k  B_k  -I] per knot acting on (x_k, u_k, x_{k+1}), k = 0..N-1.  The KKT
+// system [Theta C^T; C 0] [z; lambda] = [-g; c] reduces to
+//     S lambda = gamma,  S = C Theta^-1 C^T,  gamma = -(c + C Theta^-1 g),
+//     z = -Theta^-1 (g + C^T lambda):
+//   S_kk      = A_k Q_k^-1 A_k^T + B_k R_k^-1 B_k^T + Q_{k+1}^-1
+//   S_{k,k+1} = -Q_{k+1}^-1 A_{k+1}^T,  S_{k+1,k} = S_{k,k+1}^T
+//   gamma_k   = -(c_k + A_k Q_k^-1 q_k + B_k R_k^-1 r_k - Q_{k+1}^-1 q_{k+1})
+//   x_k = -Q_k^-1 (q_k + A_k^T lambda_k - lambda_{k-1})   (terms present for k < N, k > 0)
+//   u_k = -R_k^-1 (r_k + B_k^T lambda_k)
+// Inputs A_k (n x n) and B_k (n x m) are column-major blocks, knot-major:
+// element (r, c) of A_k at k n^2 + c n + r, of B_k at k n m + c n + r.  S is
+// written in the cbtd layout (padding blocks of knots 0 and N-1 zero), gamma
+// and lambda are n N, x is n (N+1), u is m N.
+//
+// Both kernels run one warp per knot (lane i owns row i of the knot's
+// blocks); they read each input once and write each output once, so HBM
+// bandwidth bounds them.  S_kk is symmetrised through shared memory
+// (0.5 (S + S^T), exactly symmetric).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/gbdpcg.h"
+
+namespace gbdpcg {
+void set_last_error(const std::string &msg);
+}
+
+namespace {
+
+constexpr int kKktMaxN = 32;  // n, m <= 32
+// knots per CTA (4 float, 2 double: 36 KB of static shared memory either way)
+template <typename T>
+constexpr int kkt_warps() { return sizeof(T) == 8 ? 2 : 4; }
+
+template <typename T, int kKktWarps = kkt_warps<T>()>
+__global__ void __launch_bounds__(kKktWarps * 32)
+    form_schur_kernel(const T *__restrict__ A, const T *__restrict__ B, const T *__restrict__ Qd,
+                      const T *__restrict__ Rd, const T *__restrict__ q, const T *__restrict__ r,
+                      const T *__restrict__ c, uint32_t n, uint32_t m, uint32_t N, T *__restrict__ S,
+                      T *__restrict__ gamma) {
+    __shared__ T sA[kKktWarps][kKktMaxN * (kKktMaxN + 1)];  // A_k, then S_kk
+    __shared__ T sB[kKktWarps][kKktMaxN * (kKktMaxN + 1)];
+    __shared__ T sv[kKktWarps][4][kKktMaxN];                 // Qi_k, Ri_k, Qi_{k+1}, scratch
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t k = blockIdx.x * kKktWarps + warp;
+    if (k >= N) return;  // warp-uniform; no CTA barrier below
+    const uint32_t ld = kKktMaxN + 1;
+    T *Ak = sA[warp], *Bk = sB[warp];
+    T *qi = sv[warp][0], *ri = sv[warp][1], *qn = sv[warp][2];
+    const T *Ag = A + (size_t)k * n * n, *Bg = B + (size_t)k * n * m;
+    for (uint32_t e = lane; e < n * n; e += 32) Ak[(e % n) * ld + e / n] = Ag[e];  // Ak[row][col]
+    for (uint32_t e = lane; e < n * m; e += 32) Bk[(e % n) * ld + e / n] = Bg[e];
+    if (lane < n) {
+        qi[lane] = T(1) / Qd[(size_t)k * n + lane];
+        qn[lane] = T(1) / Qd[(size_t)(k + 1) * n + lane];
+    }
+    if (lane < m) ri[lane] = T(1) / Rd[(size_t)k * m + lane];
+    __syncwarp();
+    // row i of S_kk (unsymmetrised) and gamma_k
+    T srow[kKktMaxN];
+    T g = T(0);
+    if (lane < n) {
+        const uint32_t i = lane;
+#pragma unroll
+        for (int j = 0; j < kKktMaxN; ++j) srow[j] = T(0);
+        for (uint32_t l = 0; l < n; ++l) {
+            const T a = Ak[i * ld + l] * qi[l];
+            g += a * q[(size_t)k * n + l];
+#pragma unroll
+            for (int j = 0; j < kKktMaxN; ++j)
+                if ((uint32_t)j < n) srow[j] += a * Ak[j * ld + l];
+        }
+        for (uint32_t l = 0; l < m; ++l) {
+            const T b = Bk[i * ld + l] * ri[l];
+            g += b * r[(size_t)k * m + l];
+#pragma unroll
+            for (int j = 0; j < kKktMaxN; ++j)
+                if ((uint32_t)j < n) srow[j] += b * Bk[j * ld + l];
+        }
+#pragma unroll
+        for (int j = 0; j < kKktMaxN; ++j)
+            if ((uint32_t)j == i) srow[j] += qn[i];
+        gamma[(size_t)k * n + i] = -(c[(size_t)k * n + i] + g - qn[i] * q[(size_t)(k + 1) * n + i]);
+    }
+    T *Sk = S + (size_t)k * 3 * n * n;
+    // block 0: S_{k,k-1} = S_{k-1,k}^T, element (i, j) = -Qi_k[j] A_k[i][j]
+    for (uint32_t e = lane; e < n * n; e += 32) {
+        const uint32_t col = e / n, row = e - col * n;
+        Sk[e] = (k > 0) ? -qi[col] * Ak[row * ld + col] : T(0);
+    }
+    // block 2: S_{k,k+1}, element (i, j) = -Qi_{k+1}[i] A_{k+1}[j][i]
+    const T *An = A + (size_t)(k + 1) * n * n;
+    for (uint32_t e = lane; e < n * n; e += 32) {
+        const uint32_t col = e / n, row = e - col * n;
+        Sk[2 * n * n + e] = (k + 1 < N) ? -qn[row] * An[(size_t)row * n + col] : T(0);
+    }
+    __syncwarp();  // every lane is done with Ak
+    if (lane < n) {
+#pragma unroll
+        for (int j = 0; j < kKktMaxN; ++j)
+            if ((uint32_t)j < n) Ak[lane * ld + j] = srow[j];
+    }
+    __syncwarp();
+    // block 1: S_kk symmetrised
+    for (uint32_t e = lane; e < n * n; e += 32) {
+        const uint32_t col = e / n, row = e - col * n;
+        Sk[n * n + e] = T(0.5) * (Ak[row * ld + col] + Ak[col * ld + row]);
+    }
+}
+
+template <typename T, int kKktWarps = kkt_warps<T>()>
+__global__ void __launch_bounds__(kKktWarps * 32)
+    kkt_backsub_kernel(const T *__restrict__ A, const T *__restrict__ B, const T *__restrict__ Qd,
+                       const T *__restrict__ Rd, const T *__restrict__ q, const T *__restrict__ r,
+                       const T *__restrict__ lambda, uint32_t n, uint32_t m, uint32_t N, T *__restrict__ x,
+                       T *__restrict__ u) {
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t k = blockIdx.x * kKktWarps + warp;  // knots 0..N (x) and 0..N-1 (u)
+    if (k > N) return;
+    if (lane < n) {
+        const uint32_t i = lane;
+        T s = q[(size_t)k * n + i];
+        if (k < N) {  // + (A_k^T lambda_k)_i = sum_j A_k[j][i] lambda_k[j]; column i of A_k is contiguous
+            const T *Acol = A + (size_t)k * n * n + (size_t)i * n;
+            const T *lk = lambda + (size_t)k * n;
+            for (uint32_t j = 0; j < n; ++j) s += Acol[j] * lk[j];
+        }
+        if (k > 0) s -= lambda[(size_t)(k - 1) * n + i];
+        x[(size_t)k * n + i] = -s / Qd[(size_t)k * n + i];
+    }
+    if (k < N && lane < m) {
+        const uint32_t i = lane;
+        T s = r[(size_t)k * m + i];
+        const T *Bcol = B + (size_t)k * n * m + (size_t)i * n;
+        const T *lk = lambda + (size_t)k * n;
+        for (uint32_t j = 0; j < n; ++j) s += Bcol[j] * lk[j];
+        u[(size_t)k * m + i] = -s / Rd[(size_t)k * m + i];
+    }
+}
+
+int check(const void *const *ptrs, int np, uint32_t n, uint32_t m, uint32_t N) {
+    for (int i = 0; i < np; ++i)
+        if (!ptrs[i]) {
+            gbdpcg::set_last_error("NULL pointer");
+            return GBDPCG_ERR_INVALID_ARGUMENT;
+        }
+    if (n == 0 || m == 0 || N == 0) {
+        gbdpcg::set_last_error("n, m and N must be positive");
+        return GBDPCG_ERR_INVALID_ARGUMENT;
+    }
+    if (n > (uint32_t)kKktMaxN || m > (uint32_t)kKktMaxN) {
+        gbdpcg::set_last_error("n and m must be <= 32");
+        return GBDPCG_ERR_UNSUPPORTED;
+    }
+    return GBDPCG_SUCCESS;
+}
+
+int launched(const char *what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        gbdpcg::set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+        return GBDPCG_ERR_CUDA;
+    }
+    return GBDPCG_SUCCESS;
+}
+
+template <typename T>
+int form_schur(const T *A, const T *B, const T *Qd, const T *Rd, const T *q, const T *r, const T *c, uint32_t n,
+               uint32_t m, uint32_t N, T *S, T *gamma, cudaStream_t st) {
+    const void *p[] = {A, B, Qd, Rd, q, r, c, S, gamma};
+    int rc = check(p, 9, n, m, N);
+    if (rc) return rc;
+    constexpr int W = kkt_warps<T>();
+    form_schur_kernel<T><<<(N + W - 1) / W, W * 32, 0, st>>>(A, B, Qd, Rd, q, r, c, n, m,
+                                                                                       N, S, gamma);
+    return launched("form_schur");
+}
+
+template <typename T>
+int kkt_backsub(const T *A, const T *B, const T *Qd, const T *Rd, const T *q, const T *r, const T *lambda,
+                uint32_t n, uint32_t m, uint32_t N, T *x, T *u, cudaStream_t st) {
+    const void *p[] = {A, B, Qd, Rd, q, r, lambda, x, u};
+    int rc = check(p, 9, n, m, N);
+    if (rc) return rc;
+    constexpr int W = kkt_warps<T>();
+    kkt_backsub_kernel<T><<<(N + 1 + W - 1) / W, W * 32, 0, st>>>(A, B, Qd, Rd, q, r,
+                                                                                           lambda, n, m, N, x, u);
+    return launched("kkt_backsub");
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbdpcg_form_schur_f32(const float *d_A, const float *d_B, const float *d_Qd, const float *d_Rd,
+                          const float *d_q, const float *d_r, const float *d_c, uint32_t n, uint32_t m, uint32_t N,
+                          float *d_S, float *d_gamma, gbdpcg_stream_t stream) {
+    return form_schur<float>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_c, n, m, N, d_S, d_gamma, (cudaStream_t)stream);
+}
+int gbdpcg_form_schur_f64(const double *d_A, const double *d_B, const double *d_Qd, const double *d_Rd,
+                          const double *d_q, const double *d_r, const double *d_c, uint32_t n, uint32_t m,
+                          uint32_t N, double *d_S, double *d_gamma, gbdpcg_stream_t stream) {
+    return form_schur<double>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_c, n, m, N, d_S, d_gamma, (cudaStream_t)stream);
+}
+int gbdpcg_kkt_backsub_f32(const float *d_A, const float *d_B, const float *d_Qd, const float *d_Rd,
+                           const float *d_q, const float *d_r, const float *d_lambda, uint32_t n, uint32_t m,
+                           uint32_t N, float *d_x, float *d_u, gbdpcg_stream_t stream) {
+    return kkt_backsub<float>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_lambda, n, m, N, d_x, d_u, (cudaStream_t)stream);
+}
+int gbdpcg_kkt_backsub_f64(const double *d_A, const double *d_B, const double *d_Qd, const double *d_Rd,
+                           const double *d_q, const double *d_r, const double *d_lambda, uint32_t n, uint32_t m,
+                           uint32_t N, double *d_x, double *d_u, gbdpcg_stream_t stream) {
+    return kkt_backsub<double>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_lambda, n, m, N, d_x, d_u, (cudaStream_t)stream);
+}
+
+}  // extern "C"

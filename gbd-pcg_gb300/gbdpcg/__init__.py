@@ -100,6 +100,10 @@ _SIGS = {
     "gbdpcg_plan_launch_info": ([_P, _U, _P, _P, _P, _P, _P], _I),
     "gbdpcg_plan_launch_kernel": ([_P, _U, _P, _P, _P], _I),
     "gbdpcg_plan_destroy": ([_P], _I),
+    "gbdpcg_form_schur_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_form_schur_f64": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_kkt_backsub_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_kkt_backsub_f64": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
     "gbdpcg_csr_to_cbtd_f32": ([_P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_csr_to_cbtd_f64": ([_P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_plan_autotune": ([_P, _U, _U, _P], _I),
@@ -431,3 +435,18 @@ def csr_to_cbtd(row_ptr, col_ind, val, n, N, out, err, stream=None):
     -> cbtd `out` (3 n^2 N); `err` is a one-element int32 device tensor."""
     fn = lib().gbdpcg_csr_to_cbtd_f64 if val.dtype.itemsize == 8 else lib().gbdpcg_csr_to_cbtd_f32
     _check(fn(_tp(row_ptr), _tp(col_ind), _tp(val), n, N, _tp(out), _tp(err), _stream(stream)), "gbdpcg_csr_to_cbtd")
+
+
+def form_schur(A, B, Qd, Rd, q, r, c, n, m, N, S_out, gamma_out, stream=None):
+    """S = C Theta^-1 C^T (cbtd) and gamma = -(c + C Theta^-1 g) from the
+    trajectory-optimisation data (device tensors; A_k, B_k column-major)."""
+    fn = lib().gbdpcg_form_schur_f64 if A.dtype.itemsize == 8 else lib().gbdpcg_form_schur_f32
+    _check(fn(*[_tp(t) for t in (A, B, Qd, Rd, q, r, c)], n, m, N, _tp(S_out), _tp(gamma_out), _stream(stream)),
+           "gbdpcg_form_schur")
+
+
+def kkt_backsub(A, B, Qd, Rd, q, r, lam, n, m, N, x_out, u_out, stream=None):
+    """z = -Theta^-1 (g + C^T lambda): states x (n (N+1)) and controls u (m N)."""
+    fn = lib().gbdpcg_kkt_backsub_f64 if A.dtype.itemsize == 8 else lib().gbdpcg_kkt_backsub_f32
+    _check(fn(*[_tp(t) for t in (A, B, Qd, Rd, q, r, lam)], n, m, N, _tp(x_out), _tp(u_out), _stream(stream)),
+           "gbdpcg_kkt_backsub")

@@ -322,6 +322,28 @@ GBDPCG_API int gbdpcg_csr_to_cbtd_f32(const uint32_t *d_row_ptr, const uint32_t 
 GBDPCG_API int gbdpcg_csr_to_cbtd_f64(const uint32_t *d_row_ptr, const uint32_t *d_col_ind, const double *d_val,
                                       uint32_t n, uint32_t N, double *d_out, uint32_t *d_err, gbdpcg_stream_t stream);
 
+/* The steps either side of the solve in a trajectory optimiser (no reference
+ * counterpart: the callers of solvePCG in MPCGPU / GATO).  Problem: states
+ * x_0..x_N (n), controls u_0..u_{N-1} (m), cost 1/2 z^T Theta z + g^T z with
+ * Theta = blockdiag(diag(Qd_0)..diag(Qd_N), diag(Rd_0)..diag(Rd_{N-1})), g =
+ * (q_0..q_N, r_0..r_{N-1}), constraints [A_k  B_k  -I] (x_k, u_k, x_{k+1}) = c_k,
+ * KKT [Theta C^T; C 0][z; lambda] = [-g; c].  A_k (n x n) and B_k (n x m) are
+ * column-major, knot-major.  n, m <= 32.  Stream-ordered.
+ * form_schur: S = C Theta^-1 C^T (cbtd, N block rows) and gamma = -(c + C Theta^-1 g). */
+GBDPCG_API int gbdpcg_form_schur_f32(const float *d_A, const float *d_B, const float *d_Qd, const float *d_Rd,
+                                     const float *d_q, const float *d_r, const float *d_c, uint32_t n, uint32_t m,
+                                     uint32_t N, float *d_S, float *d_gamma, gbdpcg_stream_t stream);
+GBDPCG_API int gbdpcg_form_schur_f64(const double *d_A, const double *d_B, const double *d_Qd, const double *d_Rd,
+                                     const double *d_q, const double *d_r, const double *d_c, uint32_t n, uint32_t m,
+                                     uint32_t N, double *d_S, double *d_gamma, gbdpcg_stream_t stream);
+/* kkt_backsub: z = -Theta^-1 (g + C^T lambda): x (n (N+1)) and u (m N). */
+GBDPCG_API int gbdpcg_kkt_backsub_f32(const float *d_A, const float *d_B, const float *d_Qd, const float *d_Rd,
+                                      const float *d_q, const float *d_r, const float *d_lambda, uint32_t n,
+                                      uint32_t m, uint32_t N, float *d_x, float *d_u, gbdpcg_stream_t stream);
+GBDPCG_API int gbdpcg_kkt_backsub_f64(const double *d_A, const double *d_B, const double *d_Qd, const double *d_Rd,
+                                      const double *d_q, const double *d_r, const double *d_lambda, uint32_t n,
+                                      uint32_t m, uint32_t N, double *d_x, double *d_u, gbdpcg_stream_t stream);
+
 /* Kernel of launch i: storage (0 S and Phi^-1 in registers, 1 S in registers
  * and Phi^-1 in shared memory, 2 both in shared memory, 3 hybrid, 4 tensor memory), matrix rows per
  * thread, and algorithm (GBDPCG_ALGO_CLUSTER, _SINGLE_REDUCTION, _RECURRENCE,

@@ -144,6 +144,79 @@ def relres(S, lam, gamma, n, N) -> float:
 
 
 # ------------------------------------------------------------------ reference example data
+# ---- trajectory-optimisation problem around the solve (FP64 numpy references
+# of csrc/kkt.cu's formation and back-substitution)
+
+def generate_problem(n: int, N: int, seed: int, ill: bool = False):
+    """The data behind generate(n, N, seed): A, B, Q, R drawn exactly as there
+    (same generator, same order), plus cost gradients q, r and constraint
+    right-hand side c from a second stream.  Blocks as (N, rows, cols) arrays."""
+    rng = np.random.default_rng(seed)
+    m = max(1, n // 2)
+    A = rng.standard_normal((N, n, n)) / np.sqrt(n)
+    rho = np.max(np.abs(np.linalg.eigvals(A)), axis=1)
+    A *= (0.98 / rho)[:, None, None]
+    B = rng.standard_normal((N, n, m))
+    if ill:
+        Qd = np.exp(rng.uniform(np.log(1e-2), np.log(1e4), (N + 1, n)))
+        Rd = np.exp(rng.uniform(np.log(1e-3), 0.0, (N, m)))
+    else:
+        Qd = rng.uniform(1.0, 10.0, (N + 1, n))
+        Rd = rng.uniform(0.1, 1.0, (N, m))
+    r2 = np.random.default_rng(seed + 1_000_003)
+    return {"n": n, "m": m, "N": N, "A": A, "B": B, "Qd": Qd, "Rd": Rd,
+            "q": r2.standard_normal((N + 1, n)), "r": r2.standard_normal((N, m)), "c": r2.standard_normal((N, n))}
+
+
+def problem_device_layout(P, dtype=np.float64):
+    """Flat arrays in the layout gbdpcg_form_schur / gbdpcg_kkt_backsub read
+    (A_k, B_k column-major, knot-major)."""
+    col = lambda M: np.ascontiguousarray(M.transpose(0, 2, 1)).reshape(-1).astype(dtype)
+    return {"A": col(P["A"]), "B": col(P["B"]), "Qd": P["Qd"].reshape(-1).astype(dtype),
+            "Rd": P["Rd"].reshape(-1).astype(dtype), "q": P["q"].reshape(-1).astype(dtype),
+            "r": P["r"].reshape(-1).astype(dtype), "c": P["c"].reshape(-1).astype(dtype)}
+
+
+def form_schur(P):
+    """S = C Theta^-1 C^T (flat cbtd) and gamma = -(c + C Theta^-1 g), FP64."""
+    A, B, n, N = P["A"], P["B"], P["n"], P["N"]
+    Qi, Ri = 1.0 / P["Qd"], 1.0 / P["Rd"]
+    D = np.einsum("kij,kj,klj->kil", A, Qi[:N], A) + np.einsum("kij,kj,klj->kil", B, Ri, B)
+    D[:, np.arange(n), np.arange(n)] += Qi[1:]
+    D = 0.5 * (D + D.transpose(0, 2, 1))
+    O = -(Qi[1:N][:, :, None] * A[1:].transpose(0, 2, 1))
+    gamma = -(P["c"] + np.einsum("kij,kj->ki", A, Qi[:N] * P["q"][:N])
+              + np.einsum("kij,kj->ki", B, Ri * P["r"]) - Qi[1:] * P["q"][1:])
+    return pack_cbtd(D, O), gamma.reshape(-1)
+
+
+def kkt_backsub(P, lam):
+    """z = -Theta^-1 (g + C^T lambda): x (N+1, n), u (N, m), FP64."""
+    A, B, N = P["A"], P["B"], P["N"]
+    L = np.asarray(lam, np.float64).reshape(N, -1)
+    sx = P["q"].copy()
+    sx[:N] += np.einsum("kji,kj->ki", A, L)
+    sx[1:] -= L
+    su = P["r"] + np.einsum("kji,kj->ki", B, L)
+    return -sx / P["Qd"], -su / P["Rd"]
+
+
+def kkt_dense(P):
+    """The full KKT matrix [Theta C^T; C 0] and right-hand side [-g; c] (dense,
+    FP64), variables ordered (x_0..x_N, u_0..u_{N-1}, lambda_0..lambda_{N-1})."""
+    n, m, N = P["n"], P["m"], P["N"]
+    nz = n * (N + 1) + m * N
+    C = np.zeros((n * N, nz))
+    for k in range(N):
+        C[k * n:(k + 1) * n, k * n:(k + 1) * n] = P["A"][k]
+        C[k * n:(k + 1) * n, n * (N + 1) + k * m:n * (N + 1) + (k + 1) * m] = P["B"][k]
+        C[k * n:(k + 1) * n, (k + 1) * n:(k + 2) * n] = -np.eye(n)
+    Th = np.diag(np.concatenate([P["Qd"].reshape(-1), P["Rd"].reshape(-1)]))
+    K = np.block([[Th, C.T], [C, np.zeros((n * N, n * N))]])
+    g = np.concatenate([P["q"].reshape(-1), P["r"].reshape(-1)])
+    return K, np.concatenate([-g, P["c"].reshape(-1)])
+
+
 def example_system(path: str | None = None):
     """The reference example's n=2, N=3 data (examples/pcg_solve.cu:14-31), read from
     the committed fixture tests/golden/example_n2_N3.json."""

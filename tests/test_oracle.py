@@ -146,3 +146,19 @@ def test_ref_kernel_mangled_names(oracle_mod):
     """The launcher looks the rebuilt kernel up by its Itanium-mangled name."""
     assert oracle_mod.ref_kernel_name("f32", 14, 32) == "_Z3pcgIfLj14ELj32EEvPT_S1_S1_S1_S1_S1_S1_S1_PjPbjS0_"
     assert oracle_mod.ref_kernel_name("f64", 2, 3) == "_Z3pcgIdLj2ELj3EEvPT_S1_S1_S1_S1_S1_S1_S1_PjPbjS0_"
+
+
+@pytest.mark.parametrize("n,N", [(6, 5), (14, 8), (7, 1)])
+def test_kkt_formation_and_backsub_solve_the_kkt_system(oracle_mod, n, N):
+    """The FP64 references of the steps around the solve: the Schur complement
+    equals the generator's S for the same seed, and form -> solve -> back-
+    substitute satisfies the dense KKT system."""
+    O = oracle_mod
+    P = O.generate_problem(n, N, 4)
+    S, gamma = O.form_schur(P)
+    assert np.allclose(S, O.generate(n, N, 4).cbtd(), rtol=0, atol=1e-12)
+    lam = np.linalg.solve(O.dense_from_cbtd(S, n, N), gamma)
+    x, u = O.kkt_backsub(P, lam)
+    K, rhs = O.kkt_dense(P)
+    sol = np.concatenate([x.reshape(-1), u.reshape(-1), lam])
+    assert np.linalg.norm(K @ sol - rhs) <= 1e-10 * np.linalg.norm(rhs)

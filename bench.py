@@ -366,6 +366,70 @@ def precision_config(gbdpcg, h, dev, count=256, n=24, N=256, workers=8):
     return out
 
 
+def around_solve_kernels(gbdpcg, dev, hbm_gbs, n=24, N=65536, reps=5):
+    """The steps either side of the solve on one long horizon (n = 24, m = 12,
+    N = 65536 knots, FP32, random data): Schur-complement formation, KKT
+    back-substitution and the CSR -> cbtd adapter.  HBM-bound kernels: GB/s of
+    their compulsory bytes (each input read once, each output written once)
+    against the measured copy bandwidth."""
+    import torch
+    m = n // 2
+    f = dict(dtype=torch.float32, device=dev)
+    A = torch.randn(N * n * n, **f) / n ** 0.5
+    B = torch.randn(N * n * m, **f)
+    Qd = torch.rand((N + 1) * n, **f) + 1.0
+    Rd = torch.rand(N * m, **f) + 0.1
+    q = torch.randn((N + 1) * n, **f)
+    r = torch.randn(N * m, **f)
+    c = torch.randn(N * n, **f)
+    S = torch.empty(3 * n * n * N, **f)
+    g = torch.empty(n * N, **f)
+    x = torch.empty((N + 1) * n, **f)
+    u = torch.empty(N * m, **f)
+    lam = torch.randn(N * n, **f)
+    # CSR of a full block-tridiagonal band: row r of knot k holds columns of knots k-1..k+1
+    rows = n * N
+    k = torch.arange(rows, device=dev) // n
+    lo = torch.clamp(k - 1, min=0) * n
+    hi = torch.clamp(k + 2, max=N) * n
+    cnt = (hi - lo).to(torch.int64)
+    rp = torch.zeros(rows + 1, dtype=torch.int64, device=dev)
+    rp[1:] = torch.cumsum(cnt, 0)
+    nnz = int(rp[-1].item())
+    rid = torch.repeat_interleave(torch.arange(rows, device=dev), cnt)
+    ci = (lo[rid] + torch.arange(nnz, device=dev) - rp[:-1][rid]).to(torch.int32)
+    rp32 = rp.to(torch.int32)
+    val = torch.randn(nnz, **f)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            fn()
+        b.record()
+        b.synchronize()
+        return a.elapsed_time(b) / reps
+
+    s = 4
+    out = {"n": n, "m": m, "N": N, "dtype": "f32"}
+    rows_b = [("form_schur", lambda: gbdpcg.form_schur(A, B, Qd, Rd, q, r, c, n, m, N, S, g),
+               s * (N * n * n + N * n * m + 2 * (N + 1) * n + N * m + N * n + 3 * n * n * N + n * N)),
+              ("kkt_backsub", lambda: gbdpcg.kkt_backsub(A, B, Qd, Rd, q, r, lam, n, m, N, x, u),
+               s * (N * n * n + N * n * m + 2 * (N + 1) * n + 2 * N * m + N * n + (N + 1) * n)),
+              ("csr_to_cbtd", lambda: gbdpcg.csr_to_cbtd(rp32, ci, val, n, N, S, err),
+               4 * (rows + 1) + 4 * nnz + s * nnz + 2 * s * 3 * n * n * N)]
+    for name, fn, nbytes in rows_b:
+        ms = timed(fn)
+        out[name] = {"ms": ms, "bytes": nbytes, "gbs": nbytes / (ms / 1e3) / 1e9,
+                     "frac_of_hbm": nbytes / (ms / 1e3) / 1e9 / hbm_gbs}
+    out["note"] = ("csr_to_cbtd is synchronous (it reads back its error word); its bytes count the zeroing of the "
+                   "output as a write")
+    return out
+
+
 def _gen_ill(n, N, seed):
     from gbdpcg.workload import generate
     sy = generate(n, N, seed, ill=True)
@@ -618,7 +682,8 @@ def main():
     if not args.no_extras and world == 1:
         for key, fn in (("single_system", lambda: single_system_latency(gbdpcg, h, dev)),
                         ("adjoint", lambda: adjoint_config(gbdpcg, h, dev, tune_flags)),
-                        ("precision", lambda: precision_config(gbdpcg, h, dev))):
+                        ("precision", lambda: precision_config(gbdpcg, h, dev)),
+                        ("around_solve", lambda: around_solve_kernels(gbdpcg, dev, hbm))):
             try:
                 line[key] = fn()
             except Exception as e:  # report, do not lose the headline line

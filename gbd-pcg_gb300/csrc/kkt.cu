@@ -43,30 +43,118 @@ constexpr int kKktMaxN = 32;  // n, m <= 32
 template <typename T>
 constexpr int kkt_warps() { return sizeof(T) == 8 ? 2 : 4; }
 
+// Shared-memory rows of a knot's blocks: kKktMaxN columns padded to a 16-byte
+// multiple, so that 16-byte vectors of consecutive columns can be loaded.
+template <typename T>
+__host__ __device__ constexpr int kkt_vw() { return 16 / (int)sizeof(T); }
+template <typename T>
+__host__ __device__ constexpr uint32_t kkt_ld() { return kKktMaxN + kkt_vw<T>(); }
+
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    using type = float4;
+    __device__ static void get(const float *p, float (&v)[4]) {
+        const float4 t = *reinterpret_cast<const float4 *>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    }
+};
+template <>
+struct Vec16<double> {
+    __device__ static void get(const double *p, double (&v)[2]) {
+        const double2 t = *reinterpret_cast<const double2 *>(p);
+        v[0] = t.x; v[1] = t.y;
+    }
+};
+
+// Lane r (< rows) loads row r of a column-major rows x cols block into sM[r][*]
+// (one coalesced column per load, all loads in flight together); columns from
+// cols up to the next vector boundary are zero.
+template <typename T>
+__device__ __forceinline__ void load_block(T *sM, uint32_t ld, const T *g, uint32_t rows, uint32_t cols,
+                                           uint32_t lane) {
+    constexpr int VW = kkt_vw<T>();
+    T t[kKktMaxN];
+#pragma unroll
+    for (int cc = 0; cc < kKktMaxN; ++cc) t[cc] = ((uint32_t)cc < cols && lane < rows) ? g[(size_t)cc * rows + lane] : T(0);
+    const uint32_t cpad = (cols + VW - 1) / VW * VW;
+#pragma unroll
+    for (int cc = 0; cc < kKktMaxN; ++cc)
+        if ((uint32_t)cc < cpad && lane < rows) sM[lane * ld + cc] = t[cc];
+}
+
+// acc[j] += sum_l a[l] * M[j][l] over l < cols (VW columns per load), and
+// g += sum_l a[l] * w[l], with a[l] = M[i][l] * d[l]: lane i's row of
+// M diag(d) M^T and of M diag(d) w.
+template <typename T>
+__device__ __forceinline__ void row_gram(const T *M, uint32_t ld, const T *d, const T *w, uint32_t i, uint32_t rows,
+                                         uint32_t cols, T (&acc)[kKktMaxN], T &g) {
+    constexpr int VW = kkt_vw<T>();
+    for (uint32_t l = 0; l < cols; l += VW) {
+        T mi[VW], dv[VW], wv[VW], a[VW];
+        Vec16<T>::get(M + i * ld + l, mi);
+#pragma unroll
+        for (int u = 0; u < VW; ++u) {
+            const bool in = l + u < cols;
+            dv[u] = in ? d[l + u] : T(0);
+            wv[u] = in ? w[l + u] : T(0);
+            a[u] = mi[u] * dv[u];
+            g += mi[u] * (dv[u] * wv[u]);
+        }
+#pragma unroll
+        for (int j = 0; j < kKktMaxN; ++j) {
+            if ((uint32_t)j < rows) {
+                T mj[VW];
+                Vec16<T>::get(M + j * ld + l, mj);
+#pragma unroll
+                for (int u = 0; u < VW; ++u) acc[j] += a[u] * mj[u];
+            }
+        }
+    }
+}
+
 template <typename T, int kKktWarps = kkt_warps<T>()>
 __global__ void __launch_bounds__(kKktWarps * 32)
     form_schur_kernel(const T *__restrict__ A, const T *__restrict__ B, const T *__restrict__ Qd,
                       const T *__restrict__ Rd, const T *__restrict__ q, const T *__restrict__ r,
                       const T *__restrict__ c, uint32_t n, uint32_t m, uint32_t N, T *__restrict__ S,
                       T *__restrict__ gamma) {
-    __shared__ T sA[kKktWarps][kKktMaxN * (kKktMaxN + 1)];  // A_k, then S_kk
-    __shared__ T sB[kKktWarps][kKktMaxN * (kKktMaxN + 1)];
-    __shared__ T sv[kKktWarps][4][kKktMaxN];                 // Qi_k, Ri_k, Qi_{k+1}, scratch
+    constexpr uint32_t ld = kkt_ld<T>();
+    __shared__ __align__(16) T sA[kKktWarps][kKktMaxN * ld];  // A_k, then S_kk
+    __shared__ __align__(16) T sB[kKktWarps][kKktMaxN * ld];
+    __shared__ T sv[kKktWarps][5][kKktMaxN];  // Qi_k, Ri_k, Qi_{k+1}, q_k, r_k
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t k = blockIdx.x * kKktWarps + warp;
     if (k >= N) return;  // warp-uniform; no CTA barrier below
-    const uint32_t ld = kKktMaxN + 1;
     T *Ak = sA[warp], *Bk = sB[warp];
-    T *qi = sv[warp][0], *ri = sv[warp][1], *qn = sv[warp][2];
-    const T *Ag = A + (size_t)k * n * n, *Bg = B + (size_t)k * n * m;
-    for (uint32_t e = lane; e < n * n; e += 32) Ak[(e % n) * ld + e / n] = Ag[e];  // Ak[row][col]
-    for (uint32_t e = lane; e < n * m; e += 32) Bk[(e % n) * ld + e / n] = Bg[e];
+    T *qi = sv[warp][0], *ri = sv[warp][1], *qn = sv[warp][2], *qk = sv[warp][3], *rk = sv[warp][4];
+    load_block(Ak, ld, A + (size_t)k * n * n, n, n, lane);  // Ak[row][col]
+    load_block(Bk, ld, B + (size_t)k * n * m, n, m, lane);
     if (lane < n) {
         qi[lane] = T(1) / Qd[(size_t)k * n + lane];
         qn[lane] = T(1) / Qd[(size_t)(k + 1) * n + lane];
+        qk[lane] = q[(size_t)k * n + lane];
     }
-    if (lane < m) ri[lane] = T(1) / Rd[(size_t)k * m + lane];
+    if (lane < m) {
+        ri[lane] = T(1) / Rd[(size_t)k * m + lane];
+        rk[lane] = r[(size_t)k * m + lane];
+    }
     __syncwarp();
+    T *Sk = S + (size_t)k * 3 * n * n;
+    // block 0 of row k: S_{k,k-1}, element (i, j) = -Qi_k[j] A_k[i][j]; block 2
+    // of row k-1: S_{k-1,k}, element (i, j) = -Qi_k[i] A_k[j][i] (this warp holds
+    // A_k, so each A_k is read once); the last row's block 2 is padding
+    T *Sup = (k > 0) ? S + (size_t)(k - 1) * 3 * n * n + 2 * (size_t)n * n : nullptr;
+    if (lane < n) {  // column by column, lane = row: coalesced, no index division
+        const uint32_t row = lane;
+        for (uint32_t col = 0; col < n; ++col) {
+            const uint32_t e = col * n + row;
+            Sk[e] = (k > 0) ? -qi[col] * Ak[row * ld + col] : T(0);
+            if (k > 0) Sup[e] = -qi[row] * Ak[col * ld + row];
+            if (k + 1 == N) Sk[2 * (size_t)n * n + e] = T(0);
+        }
+    }
     // row i of S_kk (unsymmetrised) and gamma_k
     T srow[kKktMaxN];
     T g = T(0);
@@ -74,36 +162,12 @@ __global__ void __launch_bounds__(kKktWarps * 32)
         const uint32_t i = lane;
 #pragma unroll
         for (int j = 0; j < kKktMaxN; ++j) srow[j] = T(0);
-        for (uint32_t l = 0; l < n; ++l) {
-            const T a = Ak[i * ld + l] * qi[l];
-            g += a * q[(size_t)k * n + l];
-#pragma unroll
-            for (int j = 0; j < kKktMaxN; ++j)
-                if ((uint32_t)j < n) srow[j] += a * Ak[j * ld + l];
-        }
-        for (uint32_t l = 0; l < m; ++l) {
-            const T b = Bk[i * ld + l] * ri[l];
-            g += b * r[(size_t)k * m + l];
-#pragma unroll
-            for (int j = 0; j < kKktMaxN; ++j)
-                if ((uint32_t)j < n) srow[j] += b * Bk[j * ld + l];
-        }
+        row_gram(Ak, ld, qi, qk, i, n, n, srow, g);  // A Q^-1 A^T, A Q^-1 q
+        row_gram(Bk, ld, ri, rk, i, n, m, srow, g);  // B R^-1 B^T, B R^-1 r
 #pragma unroll
         for (int j = 0; j < kKktMaxN; ++j)
             if ((uint32_t)j == i) srow[j] += qn[i];
         gamma[(size_t)k * n + i] = -(c[(size_t)k * n + i] + g - qn[i] * q[(size_t)(k + 1) * n + i]);
-    }
-    T *Sk = S + (size_t)k * 3 * n * n;
-    // block 0: S_{k,k-1} = S_{k-1,k}^T, element (i, j) = -Qi_k[j] A_k[i][j]
-    for (uint32_t e = lane; e < n * n; e += 32) {
-        const uint32_t col = e / n, row = e - col * n;
-        Sk[e] = (k > 0) ? -qi[col] * Ak[row * ld + col] : T(0);
-    }
-    // block 2: S_{k,k+1}, element (i, j) = -Qi_{k+1}[i] A_{k+1}[j][i]
-    const T *An = A + (size_t)(k + 1) * n * n;
-    for (uint32_t e = lane; e < n * n; e += 32) {
-        const uint32_t col = e / n, row = e - col * n;
-        Sk[2 * n * n + e] = (k + 1 < N) ? -qn[row] * An[(size_t)row * n + col] : T(0);
     }
     __syncwarp();  // every lane is done with Ak
     if (lane < n) {
@@ -113,9 +177,10 @@ __global__ void __launch_bounds__(kKktWarps * 32)
     }
     __syncwarp();
     // block 1: S_kk symmetrised
-    for (uint32_t e = lane; e < n * n; e += 32) {
-        const uint32_t col = e / n, row = e - col * n;
-        Sk[n * n + e] = T(0.5) * (Ak[row * ld + col] + Ak[col * ld + row]);
+    if (lane < n) {
+        const uint32_t row = lane;
+        for (uint32_t col = 0; col < n; ++col)
+            Sk[n * n + col * n + row] = T(0.5) * (Ak[row * ld + col] + Ak[col * ld + row]);
     }
 }
 

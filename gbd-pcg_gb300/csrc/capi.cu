@@ -520,11 +520,13 @@ struct gbdpcg_plan_s {
     };
     std::vector<Piece> pieces;
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t build_stream = nullptr;  // highest priority: the Phi^-1 builds of solve_host
     std::vector<cudaStream_t> piece_streams;
-    std::vector<cudaEvent_t> piece_events;  // [copied i] then [solved i]
+    std::vector<cudaEvent_t> piece_events;  // [copied i], [solved i], start, [built i]
     ~gbdpcg_plan_s() {
         for (auto &pc : pieces) delete pc.plan;
         if (copy_stream) cudaStreamDestroy(copy_stream);
+        if (build_stream) cudaStreamDestroy(build_stream);
         for (auto s : piece_streams) cudaStreamDestroy(s);
         for (auto e : piece_events) cudaEventDestroy(e);
         if (gexec) cudaGraphExecDestroy(gexec);
@@ -1077,6 +1079,8 @@ void drop_pieces(gbdpcg_plan_s *p) {
     p->pieces.clear();
     if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
     p->copy_stream = nullptr;
+    if (p->build_stream) cudaStreamDestroy(p->build_stream);
+    p->build_stream = nullptr;
     for (auto s : p->piece_streams) cudaStreamDestroy(s);
     p->piece_streams.clear();
     for (auto e : p->piece_events) cudaEventDestroy(e);
@@ -1127,12 +1131,17 @@ int build_pieces(gbdpcg_plan_s *p) {
         p->pieces.push_back(pc);
     }
     GB_CUDA(cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
+    // A Phi^-1 build waits for SMs that the previous piece's persistent solver
+    // grids hold; at the highest priority it gets the first SMs they free.
+    int lo_prio = 0, hi_prio = 0;
+    GB_CUDA(cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio));
+    GB_CUDA(cudaStreamCreateWithPriority(&p->build_stream, cudaStreamNonBlocking, hi_prio));
     for (int j = 0; j < 2; ++j) {  // consecutive pieces overlap
         cudaStream_t st;
         GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         p->piece_streams.push_back(st);
     }
-    for (size_t j = 0; j < 2 * p->pieces.size() + 1; ++j) {
+    for (size_t j = 0; j < 3 * p->pieces.size() + 1; ++j) {
         cudaEvent_t ev;
         GB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
         p->piece_events.push_back(ev);
@@ -1169,6 +1178,7 @@ int host_run(gbdpcg_plan_s *p, const void *h_S, const void *h_Pinv, const void *
         cudaEvent_t start = p->piece_events[2 * np];
         GB_CUDA(cudaEventRecord(start, st));
         GB_CUDA(cudaStreamWaitEvent(p->copy_stream, start, 0));
+        GB_CUDA(cudaStreamWaitEvent(p->build_stream, start, 0));
         for (auto s : p->piece_streams) GB_CUDA(cudaStreamWaitEvent(s, start, 0));
         auto h2d = [&](const void *dst, const void *src, size_t lo, size_t hi) -> cudaError_t {
             if (!src || hi <= lo) return cudaSuccess;
@@ -1176,6 +1186,15 @@ int host_run(gbdpcg_plan_s *p, const void *h_S, const void *h_Pinv, const void *
                                    static_cast<const char *>(src) + lo, hi - lo, cudaMemcpyHostToDevice,
                                    p->copy_stream);
         };
+        // GBDPCG_PIPE_LOG=1: when each piece's copies, Phi^-1 build and solve
+        // end, on stderr (diagnostics)
+        const char *log_env = getenv("GBDPCG_PIPE_LOG");
+        std::vector<cudaEvent_t> tl;
+        if (log_env && log_env[0] == '1') {
+            tl.resize(3 * np + 1);
+            for (auto &e : tl) GB_CUDA(cudaEventCreate(&e));
+            GB_CUDA(cudaEventRecord(tl[3 * np], p->copy_stream));
+        }
         for (size_t j = 0; j < np; ++j) {
             const auto &pc = p->pieces[j];
             GB_CUDA(h2d(p->arena_S, h_S, pc.S0, pc.S1));
@@ -1183,15 +1202,24 @@ int host_run(gbdpcg_plan_s *p, const void *h_S, const void *h_Pinv, const void *
             GB_CUDA(h2d(p->arena_g, h_gamma, pc.V0, pc.V1));
             if (!p->cfg.zero_guess) GB_CUDA(h2d(p->arena_l, h_lambda, pc.V0, pc.V1));
             GB_CUDA(cudaEventRecord(p->piece_events[j], p->copy_stream));
+            if (!tl.empty()) GB_CUDA(cudaEventRecord(tl[j], p->copy_stream));
         }
         for (size_t j = 0; j < np; ++j) {
             const auto &pc = p->pieces[j];
             cudaStream_t cs = p->piece_streams[j % p->piece_streams.size()];
-            GB_CUDA(cudaStreamWaitEvent(cs, p->piece_events[j], 0));
             int rc;
-            if (build_pinv && (rc = gbdpcg_plan_build_block_jacobi(pc.plan, cs))) return rc;
+            if (build_pinv) {
+                GB_CUDA(cudaStreamWaitEvent(p->build_stream, p->piece_events[j], 0));
+                if ((rc = gbdpcg_plan_build_block_jacobi(pc.plan, p->build_stream))) return rc;
+                GB_CUDA(cudaEventRecord(p->piece_events[2 * np + 1 + j], p->build_stream));
+                GB_CUDA(cudaStreamWaitEvent(cs, p->piece_events[2 * np + 1 + j], 0));
+            } else {
+                GB_CUDA(cudaStreamWaitEvent(cs, p->piece_events[j], 0));
+            }
+            if (!tl.empty()) GB_CUDA(cudaEventRecord(tl[np + j], cs));
             rc = gbdpcg_plan_execute(pc.plan, cs);
             if (rc) return rc;
+            if (!tl.empty()) GB_CUDA(cudaEventRecord(tl[2 * np + j], cs));
             if (pc.V1 > pc.V0)
                 GB_CUDA(cudaMemcpyAsync(static_cast<char *>(h_lambda) + pc.V0,
                                         static_cast<char *>(p->arena_l) + pc.V0, pc.V1 - pc.V0,
@@ -1201,6 +1229,16 @@ int host_run(gbdpcg_plan_s *p, const void *h_S, const void *h_Pinv, const void *
             GB_CUDA(cudaEventRecord(p->piece_events[np + j], cs));
         }
         for (size_t j = 0; j < np; ++j) GB_CUDA(cudaStreamWaitEvent(st, p->piece_events[np + j], 0));
+        if (!tl.empty()) {
+            GB_CUDA(cudaStreamSynchronize(st));
+            for (size_t j = 0; j < np; ++j) {
+                float t[3];
+                for (int q = 0; q < 3; ++q) GB_CUDA(cudaEventElapsedTime(&t[q], tl[3 * np], tl[q * np + j]));
+                fprintf(stderr, "gbdpcg pipe: piece %zu systems %u copied %.3f ms built %.3f ms solved %.3f ms\n", j,
+                        p->pieces[j].count, t[0], t[1], t[2]);
+            }
+            for (auto e : tl) cudaEventDestroy(e);
+        }
         if (h_results) return gbdpcg_plan_results(p, h_results, stream_);
         GB_CUDA(cudaStreamSynchronize(st));
         return GBDPCG_SUCCESS;

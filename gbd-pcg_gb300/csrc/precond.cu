@@ -4,16 +4,21 @@
 // its documented pcg_solve(S, gamma, lambda, ...) (README.md:42) has no Phi^-1
 // argument; this kernel supplies it.  One warp per knot: lane r holds row r of
 // the diagonal block S_kk (the middle block of the cbtd block row) in
-// registers, and the warp inverts the block in place by Gauss-Jordan
-// elimination without pivoting (S_kk is symmetric positive definite): at step
-// j lane j's row is the pivot row, broadcast element by element with warp
-// shuffles, and every lane updates its own row.  No shared-memory round trip
-// is on the critical path; a final shared-memory transpose symmetrises the
-// inverse, which is written either as a cbtd block row [0 | S_kk^-1 | 0] or
-// compactly (n^2 per knot, column-major).  Work item = (system, knot) over a
-// batch; the knot-prefix array maps a warp to its system.  TI: element type
-// of S, TO: of Phi^-1, CT: arithmetic (double S with float Phi^-1 serves the
-// FP32-inner refinement).
+// registers, padded with the identity to NP x NP (NP in {8, 12, 16, 24, 32},
+// the smallest that holds n), and the warp inverts it by Gauss-Jordan
+// elimination without pivoting (S_kk is symmetric positive definite) in the
+// rotating form: step j pivots on row j and on the row's first register; every
+// row then shifts one column to the left and the column of the inverse being
+// formed enters at the right, so all register indices are compile-time
+// constants while the step loop stays rolled, and after NP steps the columns
+// are back in order.  The pivot row goes through shared memory: lane j stores
+// it, lane c scales its element c, and every lane reads the scaled row back
+// with 16-byte broadcast loads.  A shared-memory transpose symmetrises the
+// inverse, written either as a cbtd block row [0 | S_kk^-1 | 0] or compactly
+// (n^2 per knot, column-major), column by column.  Work item = (system, knot)
+// over a batch; the knot-prefix array maps a warp to its system.  TI: element
+// type of S, TO: of Phi^-1, CT: arithmetic (double S with float Phi^-1 serves
+// the FP32-inner refinement).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -24,11 +29,99 @@ namespace gbdpcg {
 constexpr int kPrecWarps = 4;  // knots per CTA
 constexpr int kPrecMaxN = 32;
 
+template <typename CT>
+struct PrecVec;  // 16-byte shared-memory loads
+template <>
+struct PrecVec<float> {
+    static constexpr int W = 4;
+    __device__ static void get(const float *p, float *v) {
+        const float4 t = *reinterpret_cast<const float4 *>(p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    }
+};
+template <>
+struct PrecVec<double> {
+    static constexpr int W = 2;
+    __device__ static void get(const double *p, double *v) {
+        const double2 t = *reinterpret_cast<const double2 *>(p);
+        v[0] = t.x; v[1] = t.y;
+    }
+};
+
+// Rotating Gauss-Jordan inverse of the NP x NP block whose row `lane` is a
+// (lanes >= NP hold nothing).  s_raw, s_t: NP-element, 16-byte aligned rows.
+template <typename CT, int NP>
+__device__ __forceinline__ void gj_rotate(CT (&a)[NP], CT *s_raw, CT *s_t, uint32_t lane) {
+    constexpr int W = PrecVec<CT>::W;
+#pragma unroll 1
+    for (uint32_t j = 0; j < (uint32_t)NP; ++j) {
+        const bool pivot = lane == j;
+        if (pivot) {
+#pragma unroll
+            for (int c = 0; c < NP; ++c) s_raw[c] = a[c];
+        }
+        __syncwarp();
+        CT piv = s_raw[0];
+        if (piv == CT(0)) piv = CT(1);  // singular block: leave that column unscaled
+        const CT inv = CT(1) / piv;
+        // scaled pivot row, shifted one column left; the new last column is inv
+        if (lane + 1 < (uint32_t)NP) s_t[lane] = s_raw[lane + 1] * inv;
+        else if (lane + 1 == (uint32_t)NP) s_t[lane] = inv;
+        __syncwarp();
+        const CT m = a[0];
+#pragma unroll
+        for (int c = 0; c < NP; c += W) {
+            CT t[W];
+            PrecVec<CT>::get(s_t + c, t);
+#pragma unroll
+            for (int u = 0; u < W; ++u) {
+                const int e = c + u;
+                if (e + 1 < NP) a[e] = pivot ? t[u] : a[e + 1] - m * t[u];
+                else a[e] = pivot ? t[u] : -(m * inv);
+            }
+        }
+        __syncwarp();  // the rows are read before the next step overwrites them
+    }
+}
+
+template <typename TI, typename TO, typename CT, int NP>
+__device__ __forceinline__ void invert_knot(const TI *Sk, TO *row, uint32_t n, int tri_layout, CT *s_raw, CT *s_t,
+                                            CT *X, uint32_t lane) {
+    // lane r: row r of S_kk (column-major: (r, c) at c*n + r; coalesced over
+    // lanes), identity beyond n
+    CT a[NP];
+#pragma unroll
+    for (int c = 0; c < NP; ++c)
+        a[c] = (lane < n && (uint32_t)c < n) ? CT(Sk[(size_t)c * n + lane]) : ((uint32_t)c == lane ? CT(1) : CT(0));
+    gj_rotate<CT, NP>(a, s_raw, s_t, lane);
+    // symmetrise through a shared-memory transpose: X[r][c] = inverse (r, c)
+    const uint32_t ld = kPrecMaxN + 1;
+    if (lane < n) {
+#pragma unroll
+        for (int c = 0; c < NP; ++c)
+            if ((uint32_t)c < n) X[lane * ld + c] = a[c];
+    }
+    __syncwarp();
+    // column by column, lane = row: coalesced stores, no index division
+    const uint32_t nn = n * n, mid = tri_layout ? nn : 0;
+    if (lane < n) {
+        const uint32_t r = lane;
+        for (uint32_t c = 0; c < n; ++c) {
+            row[mid + c * n + r] = TO(CT(0.5) * (X[r * ld + c] + X[c * ld + r]));
+            if (tri_layout) {
+                row[c * n + r] = TO(0);
+                row[2 * nn + c * n + r] = TO(0);
+            }
+        }
+    }
+}
+
 template <typename TI, typename TO, typename CT>
 __global__ void __launch_bounds__(kPrecWarps * 32)
     block_jacobi_kernel(const SysDesc *__restrict__ descs, const uint64_t *__restrict__ knot_prefix,
                         uint32_t nsys, uint64_t total_knots, int tri_layout) {
     __shared__ CT sX[kPrecWarps][kPrecMaxN * (kPrecMaxN + 1)];
+    __shared__ __align__(16) CT sR[kPrecWarps][2][kPrecMaxN];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint64_t gk = (uint64_t)blockIdx.x * kPrecWarps + warp;
     if (gk >= total_knots) return;  // warp-uniform; no CTA-wide barrier below
@@ -42,52 +135,13 @@ __global__ void __launch_bounds__(kPrecWarps * 32)
     const uint32_t n = d.n, k = (uint32_t)(gk - knot_prefix[lo]);
     if (n == 0 || n > (uint32_t)kPrecMaxN) return;
     const TI *Sk = static_cast<const TI *>(d.S) + (size_t)k * 3 * n * n + (size_t)n * n;
-    // lane r: row r of S_kk (column-major: (r, c) at c*n + r; coalesced over lanes)
-    CT a[kPrecMaxN];
-#pragma unroll
-    for (int c = 0; c < kPrecMaxN; ++c) a[c] = (lane < n && (uint32_t)c < n) ? CT(Sk[(size_t)c * n + lane]) : CT(0);
-    // in-place Gauss-Jordan: after step j, column j holds the inverse's column
-#pragma unroll
-    for (int j = 0; j < kPrecMaxN; ++j) {
-        if ((uint32_t)j < n) {  // warp-uniform
-            CT piv = __shfl_sync(0xffffffffu, a[j], j);
-            if (piv == CT(0)) piv = CT(1);  // singular block: leave that column unscaled
-            const CT inv = CT(1) / piv;
-            const CT g = a[j] * inv;  // lane j: 1
-#pragma unroll
-            for (int c = 0; c < kPrecMaxN; ++c) {
-                if ((uint32_t)c < n) {
-                    const CT rj = __shfl_sync(0xffffffffu, a[c], j);  // pivot row, before this step
-                    if (c == j) a[c] = ((int)lane == j) ? inv : -g;
-                    else a[c] = ((int)lane == j) ? rj * inv : a[c] - g * rj;
-                }
-            }
-        }
-    }
-    // symmetrise through a shared-memory transpose: X[r][c] = inverse (r, c)
-    CT *X = sX[warp];
-    const uint32_t ld = kPrecMaxN + 1;
-    if (lane < n) {
-#pragma unroll
-        for (int c = 0; c < kPrecMaxN; ++c)
-            if ((uint32_t)c < n) X[lane * ld + c] = a[c];
-    }
-    __syncwarp();
-    TO *out = static_cast<TO *>(const_cast<void *>(d.P));
-    if (tri_layout) {
-        TO *row = out + (size_t)k * 3 * n * n;
-        for (uint32_t e = lane; e < 3 * n * n; e += 32) {
-            const uint32_t b = e / (n * n), w = e - b * n * n;
-            const uint32_t c = w / n, r = w - c * n;
-            row[e] = (b == 1) ? TO(CT(0.5) * (X[r * ld + c] + X[c * ld + r])) : TO(0);
-        }
-    } else {
-        TO *blk = out + (size_t)k * n * n;
-        for (uint32_t e = lane; e < n * n; e += 32) {
-            const uint32_t c = e / n, r = e - c * n;
-            blk[e] = TO(CT(0.5) * (X[r * ld + c] + X[c * ld + r]));
-        }
-    }
+    TO *row = static_cast<TO *>(const_cast<void *>(d.P)) + (size_t)k * (tri_layout ? 3 : 1) * n * n;
+    CT *s_raw = sR[warp][0], *s_t = sR[warp][1], *X = sX[warp];
+    if (n <= 8) invert_knot<TI, TO, CT, 8>(Sk, row, n, tri_layout, s_raw, s_t, X, lane);
+    else if (n <= 12) invert_knot<TI, TO, CT, 12>(Sk, row, n, tri_layout, s_raw, s_t, X, lane);
+    else if (n <= 16) invert_knot<TI, TO, CT, 16>(Sk, row, n, tri_layout, s_raw, s_t, X, lane);
+    else if (n <= 24) invert_knot<TI, TO, CT, 24>(Sk, row, n, tri_layout, s_raw, s_t, X, lane);
+    else invert_knot<TI, TO, CT, 32>(Sk, row, n, tri_layout, s_raw, s_t, X, lane);
 }
 
 // kind: 0 float S -> float Phi^-1 (float arithmetic); 1 double -> double;

@@ -312,7 +312,9 @@ class Plan:
         _check(lib().gbdpcg_plan_execute(self.p, _stream(stream)), "gbdpcg_plan_execute")
 
     def execute_host(self, h_S, h_P, h_g, h_l, with_results=False, stream=None):
-        """End-to-end from host arrays (numpy or pinned CPU tensors)."""
+        """End-to-end from host arrays (numpy or pinned CPU tensors).  With
+        with_results, returns the per-system results as a ctypes array of
+        Result (a sequence, filled in place by the library)."""
         def ptr(a):
             if a is None:
                 return None
@@ -321,18 +323,18 @@ class Plan:
         _check(lib().gbdpcg_plan_execute_host(self.p, ptr(h_S), ptr(h_P), ptr(h_g), ptr(h_l),
                                               ctypes.cast(res, ctypes.c_void_p) if res is not None else None,
                                               _stream(stream)), "gbdpcg_plan_execute_host")
-        return list(res) if res is not None else None
+        return res
 
     def solve_host(self, h_S, h_g, h_l, with_results=False, stream=None):
         """pcg_solve over the batch from host arrays: S and gamma in, Phi^-1 built
-        on the device, lambda out."""
+        on the device, lambda out (results as in execute_host)."""
         def ptr(a):
             return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data_as(ctypes.c_void_p)
         res = (Result * self.count)() if with_results else None
         _check(lib().gbdpcg_plan_solve_host(self.p, ptr(h_S), ptr(h_g), ptr(h_l),
                                             ctypes.cast(res, ctypes.c_void_p) if res is not None else None,
                                             _stream(stream)), "gbdpcg_plan_solve_host")
-        return list(res) if res is not None else None
+        return res
 
     def build_block_jacobi(self, stream=None):
         _check(lib().gbdpcg_plan_build_block_jacobi(self.p, _stream(stream)), "gbdpcg_plan_build_block_jacobi")
@@ -341,7 +343,7 @@ class Plan:
         arr = (Result * self.count)()
         _check(lib().gbdpcg_plan_results(self.p, ctypes.cast(arr, ctypes.c_void_p), _stream(stream)),
                "gbdpcg_plan_results")
-        return list(arr)
+        return arr  # ctypes array of Result: a sequence, no per-element conversion
 
     def launches(self):
         c = ctypes.c_uint32()

@@ -6,10 +6,18 @@
 // block-tridiagonal system (rows = cols = n N; row r belongs to knot r / n)
 // is scattered into the compressed block-tridiagonal layout the solver reads:
 // entry (r, c) goes to block b = c / n - r / n + 1 of knot k = r / n, at
-// k*3n^2 + (b*n + c % n)*n + r % n.  One thread per row, so no two threads
-// write the same element; duplicate entries of a row add up.  An entry
-// outside the three diagonal blocks of its row (or past the last column) is
-// not written and raises the error word.
+// k*3n^2 + (b*n + c % n)*n + r % n.
+//
+// One warp per knot.  The knot's n rows are one contiguous run of entries, so
+// the lanes read column indices and values coalesced; each entry is added
+// into a shared-memory tile of the knot's n x 3n block row (its row found by
+// a binary search over the knot's n + 1 row pointers, its block by two
+// comparisons), and the finished tile is written once, coalesced, padding
+// blocks included (no separate zeroing pass).  Duplicate entries of a row add
+// (in an unspecified order when there are more than two).  An entry outside
+// the three diagonal blocks of its row (or past the last column) is not
+// written and raises the error word.  For n > 32 (tiles too large for shared
+// memory) one thread per row scatters into the zeroed output instead.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -23,25 +31,83 @@ void set_last_error(const std::string &msg);
 
 namespace {
 
+constexpr int kCsrWarps = 4;  // knots per CTA
+
+// elements of one warp's tile, rounded to keep every tile 16-byte aligned
+__host__ __device__ inline uint32_t csr_tile_elems(uint32_t n) { return (3 * n * n + 3) & ~3u; }
+
 template <typename T>
-__global__ void csr_to_cbtd_kernel(const uint32_t *__restrict__ row_ptr, const uint32_t *__restrict__ col_ind,
-                                   const T *__restrict__ val, uint32_t n, uint32_t N, T *__restrict__ out,
-                                   uint32_t *err) {
+__host__ __device__ inline size_t csr_smem_bytes(uint32_t n) {
+    return (size_t)kCsrWarps * (csr_tile_elems(n) * sizeof(T) + 33 * sizeof(uint32_t));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kCsrWarps * 32)
+    csr_to_cbtd_kernel(const uint32_t *__restrict__ row_ptr, const uint32_t *__restrict__ col_ind,
+                       const T *__restrict__ val, uint32_t n, uint32_t N, T *__restrict__ out, uint32_t *err) {
+    extern __shared__ __align__(16) unsigned char csr_smem[];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t k = blockIdx.x * kCsrWarps + warp;
+    if (k >= N) return;  // warp-uniform; no CTA-wide barrier below
+    const uint32_t te = csr_tile_elems(n), nn3 = 3 * n * n;
+    T *tile = reinterpret_cast<T *>(csr_smem) + (size_t)warp * te;
+    uint32_t *rpl = reinterpret_cast<uint32_t *>(csr_smem + (size_t)kCsrWarps * te * sizeof(T)) + warp * 33;
+    for (uint32_t e = lane; e < nn3; e += 32) tile[e] = T(0);
+    if (lane <= n) rpl[lane] = row_ptr[(size_t)k * n + lane];
+    __syncwarp();
+    const uint32_t e0 = rpl[0], e1 = rpl[n], rows = n * N;
+    const uint32_t cbase = k * n - n;  // first column of knot k-1 (wraps for k = 0)
+    bool bad = false;
+    constexpr int U = 8;  // entries per lane in flight
+    for (uint32_t base = e0; base < e1; base += 32 * U) {
+        uint32_t cc[U];
+        T vv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t e = base + u * 32 + lane;
+            cc[u] = e < e1 ? col_ind[e] : 0u;
+            vv[u] = e < e1 ? val[e] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t e = base + u * 32 + lane;
+            if (e >= e1) break;
+            // row of entry e within the knot: rpl[lo] <= e < rpl[lo + 1]
+            uint32_t lo = 0, hi = n;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (rpl[mid] <= e) lo = mid; else hi = mid;
+            }
+            const uint32_t d = cc[u] - cbase;  // column offset from knot k-1's first column
+            if (cc[u] >= rows || d >= 3 * n) bad = true;
+            else atomicAdd(&tile[d * n + lo], vv[u]);  // (b n + j) n + i with d = b n + j
+        }
+    }
+    if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(err, 1u);
+    __syncwarp();
+    T *dst = out + (size_t)k * nn3;
+    for (uint32_t e = lane; e < nn3; e += 32) dst[e] = tile[e];
+}
+
+// n > 32: one thread per row, adding into the zeroed output (no two threads
+// write one element).
+template <typename T>
+__global__ void csr_rows_to_cbtd_kernel(const uint32_t *__restrict__ row_ptr, const uint32_t *__restrict__ col_ind,
+                                        const T *__restrict__ val, uint32_t n, uint32_t N, T *__restrict__ out,
+                                        uint32_t *err) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t rows = n * N;
     if (r >= rows) return;
     const uint32_t k = r / n, i = r - k * n;
     T *row = out + (size_t)k * 3 * n * n + i;
-    const uint32_t e0 = row_ptr[r], e1 = row_ptr[r + 1];
-    for (uint32_t e = e0; e < e1; ++e) {
-        const uint32_t c = col_ind[e];
-        const uint32_t kc = c / n;
-        if (c >= rows || kc + 1 < k || kc > k + 1) {
+    const uint32_t cbase = k * n - n;
+    for (uint32_t e = row_ptr[r], e1 = row_ptr[r + 1]; e < e1; ++e) {
+        const uint32_t c = col_ind[e], d = c - cbase;
+        if (c >= rows || d >= 3 * n) {
             atomicOr(err, 1u);
             continue;
         }
-        const uint32_t b = kc + 1 - k, j = c - kc * n;
-        row[(size_t)(b * n + j) * n] += val[e];
+        row[(size_t)d * n] += val[e];
     }
 }
 
@@ -56,12 +122,28 @@ int csr_to_cbtd(const uint32_t *d_row_ptr, const uint32_t *d_col_ind, const T *d
         gbdpcg::set_last_error("n and N must be positive");
         return GBDPCG_ERR_INVALID_ARGUMENT;
     }
-    cudaError_t e = cudaMemsetAsync(d_out, 0, sizeof(T) * 3 * (size_t)n * n * N, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_err, 0, sizeof(uint32_t), st);
-    if (e == cudaSuccess) {
-        const uint32_t rows = n * N, tpb = 128;
-        csr_to_cbtd_kernel<T><<<(rows + tpb - 1) / tpb, tpb, 0, st>>>(d_row_ptr, d_col_ind, d_val, n, N, d_out, d_err);
-        e = cudaGetLastError();
+    if ((uint64_t)n * N >= (1ull << 32) / 3) {
+        gbdpcg::set_last_error("csr_to_cbtd: n N too large for 32-bit column indices");
+        return GBDPCG_ERR_INVALID_ARGUMENT;
+    }
+    cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(uint32_t), st);
+    if (n <= 32) {
+        const size_t smem = csr_smem_bytes<T>(n);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(csr_to_cbtd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) {
+            csr_to_cbtd_kernel<T><<<(N + kCsrWarps - 1) / kCsrWarps, kCsrWarps * 32, smem, st>>>(
+                d_row_ptr, d_col_ind, d_val, n, N, d_out, d_err);
+            e = cudaGetLastError();
+        }
+    } else {
+        if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, sizeof(T) * 3 * (size_t)n * n * N, st);
+        if (e == cudaSuccess) {
+            const uint32_t rows = n * N, tpb = 128;
+            csr_rows_to_cbtd_kernel<T><<<(rows + tpb - 1) / tpb, tpb, 0, st>>>(d_row_ptr, d_col_ind, d_val, n, N,
+                                                                               d_out, d_err);
+            e = cudaGetLastError();
+        }
     }
     uint32_t h_err = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);

@@ -90,3 +90,24 @@ def test_csr_entry_outside_band_is_rejected(gb, oracle_mod, handle):
     # the in-band entries are still in place
     exp = _expected(M, n, N)
     assert out.cpu().numpy().tobytes() == exp.tobytes()
+
+
+@pytest.mark.parametrize("n,N", [(24, 16), (7, 5), (40, 3)])
+def test_csr_ragged_and_empty_rows(gb, oracle_mod, handle, n, N):
+    """A random half of the band's entries dropped, some rows left empty; n = 40
+    takes the one-thread-per-row path (tiles above 32 x 96 do not fit)."""
+    import torch
+    O = oracle_mod
+    M = O.generate(n, N, 5).cbtd(np.float32)
+    rng = np.random.default_rng(n * 100 + N)
+    keep = rng.random(M.size) < 0.5
+    for r in rng.choice(n * N, size=max(1, n * N // 7), replace=False):  # empty rows
+        k, i = divmod(int(r), n)
+        keep[k * 3 * n * n + i:(k + 1) * 3 * n * n:n] = False
+    Md = np.where(keep, M, np.float32(0)).astype(np.float32)
+    rp, ci, va = _csr_from_cbtd(O, Md, n, N)
+    assert (np.diff(rp.astype(np.int64)) == 0).any()
+    out = torch.full((3 * n * n * N,), 7.0, device="cuda:0")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda:0")
+    gb.csr_to_cbtd(_dev(rp), _dev(ci), _dev(va), n, N, out, err)
+    assert out.cpu().numpy().tobytes() == _expected(Md, n, N).tobytes()

@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--no-extras", action="store_true", help="skip the baselines and the other configurations")
+    ap.add_argument("--only", default=None, choices=["around-solve", "block-jacobi"],
+                    help="time one section alone and print its JSON (profiling): the kernels either side of "
+                         "the solve, or the block-Jacobi build over the batch")
+    ap.add_argument("--knots", type=int, default=65536, help="knots of the --only around-solve horizon")
     ap.add_argument("--algorithm", default="auto", choices=["auto", "standard", "recurrence", "single-reduction"])
     ap.add_argument("--storage", default="auto", choices=["auto", "registers", "shared", "split", "hybrid", "tmem"],
                     help="pin where the cluster solver keeps the matrix rows (profiling; default: the tuner's choice)")
@@ -429,6 +433,26 @@ def around_solve_kernels(gbdpcg, dev, hbm_gbs, n=24, N=65536, reps=5):
     return out
 
 
+def block_jacobi_build(plan, descs, hbm_gbs, reps=5):
+    """The block-Jacobi Phi^-1 build over the plan's systems (device-resident):
+    S_kk read and its inverse written once per knot."""
+    import torch
+    plan.build_block_jacobi()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        plan.build_block_jacobi()
+    b.record()
+    b.synchronize()
+    ms = a.elapsed_time(b) / reps
+    knots = sum(N for (n, N, _, _, _) in descs)
+    nbytes = sum(2 * 4 * n * n * N for (n, N, _, _, _) in descs)
+    return {"ms": ms, "knots": knots, "bytes": nbytes, "gbs": nbytes / (ms / 1e3) / 1e9,
+            "frac_of_hbm": nbytes / (ms / 1e3) / 1e9 / hbm_gbs,
+            "note": "one warp per knot, rotating Gauss-Jordan in registers: issue-bound, not HBM-bound"}
+
+
 def _gen_ill(n, N, seed):
     from gbdpcg.workload import generate
     sy = generate(n, N, seed, ill=True)
@@ -493,6 +517,16 @@ def main():
         import __graft_entry__
         __graft_entry__.build()
     gbdpcg.lib()
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    if args.only == "around-solve":
+        print(json.dumps({"around_solve": around_solve_kernels(gbdpcg, dev, hbm, N=args.knots)}), flush=True)
+        return
 
     descs, Sa, ga, nP = build_batch(rank, args.systems, max(1, (os.cpu_count() or 1) // max(1, world)))
     count = len(descs)
@@ -510,6 +544,9 @@ def main():
     plan = gbdpcg.Plan(h, layout=gbdpcg.PINV_BLOCKDIAG, cfg=cfg, packed=(descs, dS, dP, dg, dl))
     plan.build_block_jacobi()
     torch.cuda.synchronize()
+    if args.only == "block-jacobi":
+        print(json.dumps({"block_jacobi": block_jacobi_build(plan, descs, hbm)}), flush=True)
+        return
     tune_s = 0.0
     tune_flags = {"off": None, "shapes": 0, "shapes+recurrence": gbdpcg.TUNE_RECURRENCE,
                   "shapes+algorithms": gbdpcg.TUNE_RECURRENCE | gbdpcg.TUNE_SINGLE_REDUCTION}[args.tune]
@@ -583,13 +620,6 @@ def main():
     worst = max(relres64(Sa[oS:oS + 3 * n * n * N], ga[oV:oV + n * N], lam[oV:oV + n * N], n, N)
                 for (n, N, oS, oP, oV) in descs[:: max(1, count // 64)])
 
-    peaks = {}
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            peaks = json.load(f)
-    except OSError:
-        pass
-    hbm = peaks.get("hbm_gbs", 6800.0)
     achieved = algo_bytes / (ms_step / 1e3) / 1e9
     traffic = None
     try:
@@ -682,7 +712,8 @@ def main():
         for key, fn in (("single_system", lambda: single_system_latency(gbdpcg, h, dev)),
                         ("adjoint", lambda: adjoint_config(gbdpcg, h, dev, tune_flags)),
                         ("precision", lambda: precision_config(gbdpcg, h, dev)),
-                        ("around_solve", lambda: around_solve_kernels(gbdpcg, dev, hbm))):
+                        ("around_solve", lambda: around_solve_kernels(gbdpcg, dev, hbm)),
+                        ("block_jacobi", lambda: block_jacobi_build(plan, descs, hbm))):
             try:
                 line[key] = fn()
             except Exception as e:  # report, do not lose the headline line

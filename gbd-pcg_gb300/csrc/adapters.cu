@@ -10,9 +10,9 @@
 //
 // One warp per knot.  The knot's n rows are one contiguous run of entries, so
 // the lanes read column indices and values coalesced; each entry is added
-// into a shared-memory tile of the knot's n x 3n block row (its row found by
-// a binary search over the knot's n + 1 row pointers, its block by two
-// comparisons), and the finished tile is written once, coalesced, padding
+// into a shared-memory tile of the knot's n x 3n block row (its row from a
+// per-lane cursor over the knot's n + 1 row pointers, its block and column
+// from one subtraction), and the finished tile is written once, coalesced, padding
 // blocks included (no separate zeroing pass).  Duplicate entries of a row add
 // (in an unspecified order when there are more than two).  An entry outside
 // the three diagonal blocks of its row (or past the last column) is not
@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(kCsrWarps * 32)
     const uint32_t cbase = k * n - n;  // first column of knot k-1 (wraps for k = 0)
     bool bad = false;
     constexpr int U = 8;  // entries per lane in flight
+    uint32_t row = 0;     // this lane's entries only move forward: rpl[row] <= e < rpl[row + 1]
     for (uint32_t base = e0; base < e1; base += 32 * U) {
         uint32_t cc[U];
         T vv[U];
@@ -72,15 +73,10 @@ __global__ void __launch_bounds__(kCsrWarps * 32)
         for (int u = 0; u < U; ++u) {
             const uint32_t e = base + u * 32 + lane;
             if (e >= e1) break;
-            // row of entry e within the knot: rpl[lo] <= e < rpl[lo + 1]
-            uint32_t lo = 0, hi = n;
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (rpl[mid] <= e) lo = mid; else hi = mid;
-            }
+            while (rpl[row + 1] <= e) ++row;  // stops below n: e < rpl[n]
             const uint32_t d = cc[u] - cbase;  // column offset from knot k-1's first column
             if (cc[u] >= rows || d >= 3 * n) bad = true;
-            else atomicAdd(&tile[d * n + lo], vv[u]);  // (b n + j) n + i with d = b n + j
+            else atomicAdd(&tile[d * n + row], vv[u]);  // (b n + j) n + i with d = b n + j
         }
     }
     if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(err, 1u);

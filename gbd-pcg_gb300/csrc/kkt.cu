@@ -29,6 +29,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <type_traits>
 
 #include "../../include/gbdpcg.h"
 
@@ -47,8 +48,6 @@ constexpr int kkt_warps() { return sizeof(T) == 8 ? 2 : 4; }
 // multiple, so that 16-byte vectors of consecutive columns can be loaded.
 template <typename T>
 __host__ __device__ constexpr int kkt_vw() { return 16 / (int)sizeof(T); }
-template <typename T>
-__host__ __device__ constexpr uint32_t kkt_ld() { return kKktMaxN + kkt_vw<T>(); }
 
 template <typename T>
 struct Vec16;
@@ -68,78 +67,86 @@ struct Vec16<double> {
     }
 };
 
-// Lane r (< rows) loads row r of a column-major rows x cols block into sM[r][*]
-// (one coalesced column per load, all loads in flight together); columns from
-// cols up to the next vector boundary are zero.
-template <typename T>
-__device__ __forceinline__ void load_block(T *sM, uint32_t ld, const T *g, uint32_t rows, uint32_t cols,
-                                           uint32_t lane) {
-    constexpr int VW = kkt_vw<T>();
-    T t[kKktMaxN];
-#pragma unroll
-    for (int cc = 0; cc < kKktMaxN; ++cc) t[cc] = ((uint32_t)cc < cols && lane < rows) ? g[(size_t)cc * rows + lane] : T(0);
-    const uint32_t cpad = (cols + VW - 1) / VW * VW;
-#pragma unroll
-    for (int cc = 0; cc < kKktMaxN; ++cc)
-        if ((uint32_t)cc < cpad && lane < rows) sM[lane * ld + cc] = t[cc];
+// Shared-memory layout of one knot for the formation: Mt[l][r] = M[r][l] with
+// M = [A_k | B_k] (n x (n + m)), i.e. row l of Mt is column l of A_k (l < n)
+// or of B_k, contiguous in global memory, so it loads coalesced with no
+// transpose; rows are NP + 4 elements (a 16-byte multiple), rows n..NP-1 zero.
+template <int NP>
+__host__ __device__ constexpr uint32_t schur_ldt() { return NP + 4; }
+
+// per-warp elements: Mt (L rows) + d (L) + w (L) + Qi_{k+1} (32), L = n + m
+__host__ __device__ inline uint32_t schur_warp_elems(uint32_t L, uint32_t ldt) {
+    return (L * ldt + 2 * ((L + 3) & ~3u) + 32);
 }
 
-// acc[j] += sum_l a[l] * M[j][l] over l < cols (VW columns per load), and
-// g += sum_l a[l] * w[l], with a[l] = M[i][l] * d[l]: lane i's row of
-// M diag(d) M^T and of M diag(d) w.
+// Asynchronous copy of one element global -> shared (cp.async, no registers,
+// nothing waits until cp_async_wait_all); valid = false writes a zero instead.
 template <typename T>
-__device__ __forceinline__ void row_gram(const T *M, uint32_t ld, const T *d, const T *w, uint32_t i, uint32_t rows,
-                                         uint32_t cols, T (&acc)[kKktMaxN], T &g) {
-    constexpr int VW = kkt_vw<T>();
-    for (uint32_t l = 0; l < cols; l += VW) {
-        T mi[VW], dv[VW], wv[VW], a[VW];
-        Vec16<T>::get(M + i * ld + l, mi);
+__device__ __forceinline__ void cp_async_elem(T *smem, const T *gmem, bool valid) {
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    const uint32_t bytes = valid ? (uint32_t)sizeof(T) : 0u;
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(s), "l"(gmem), "r"(bytes) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(s), "l"(gmem), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// loads TR consecutive elements starting at an 8-byte-aligned float address
+// (pairs) or any double address
+template <typename T, int TR>
+__device__ __forceinline__ void load_run(const T *p, T (&v)[TR]) {
+    if constexpr (sizeof(T) == 4 && TR % 2 == 0) {
 #pragma unroll
-        for (int u = 0; u < VW; ++u) {
-            const bool in = l + u < cols;
-            dv[u] = in ? d[l + u] : T(0);
-            wv[u] = in ? w[l + u] : T(0);
-            a[u] = mi[u] * dv[u];
-            g += mi[u] * (dv[u] * wv[u]);
+        for (int t = 0; t < TR; t += 2) {
+            const float2 x = *reinterpret_cast<const float2 *>(p + t);
+            v[t] = x.x;
+            v[t + 1] = x.y;
         }
+    } else {
 #pragma unroll
-        for (int j = 0; j < kKktMaxN; ++j) {
-            if ((uint32_t)j < rows) {
-                T mj[VW];
-                Vec16<T>::get(M + j * ld + l, mj);
-#pragma unroll
-                for (int u = 0; u < VW; ++u) acc[j] += a[u] * mj[u];
-            }
-        }
+        for (int t = 0; t < TR; ++t) v[t] = p[t];
     }
 }
 
-template <typename T, int kKktWarps = kkt_warps<T>()>
-__global__ void __launch_bounds__(kKktWarps * 32)
+// One warp per knot.  The Gram product S_kk = M diag(d) M^T is a 2D register
+// tile per lane: lanes form a 4 x 8 grid, lane (rg, cg) owns rows
+// rg TR .. rg TR + TR - 1 and columns cg TC .. cg TC + TC - 1 of the NP x NP
+// product (TR = NP / 4, TC = NP / 8), and each column l of M adds a rank-1
+// term: TR + TC shared-memory loads for TR TC FMAs.  Every element is rounded
+// as sum_l fma(M[i][l] d_l, M[j][l], .) in ascending l, then + Qi_{k+1} on the
+// diagonal, and symmetrised as 0.5 (S + S^T) through shared memory.
+template <typename T, int NP, int W>
+__global__ void __launch_bounds__(W * 32)
     form_schur_kernel(const T *__restrict__ A, const T *__restrict__ B, const T *__restrict__ Qd,
                       const T *__restrict__ Rd, const T *__restrict__ q, const T *__restrict__ r,
                       const T *__restrict__ c, uint32_t n, uint32_t m, uint32_t N, T *__restrict__ S,
                       T *__restrict__ gamma) {
-    constexpr uint32_t ld = kkt_ld<T>();
-    __shared__ __align__(16) T sA[kKktWarps][kKktMaxN * ld];  // A_k, then S_kk
-    __shared__ __align__(16) T sB[kKktWarps][kKktMaxN * ld];
-    __shared__ T sv[kKktWarps][5][kKktMaxN];  // Qi_k, Ri_k, Qi_{k+1}, q_k, r_k
+    constexpr int TR = NP / 4, TC = NP / 8;
+    constexpr uint32_t ldt = schur_ldt<NP>();
+    extern __shared__ __align__(16) unsigned char schur_smem[];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t k = blockIdx.x * kKktWarps + warp;
+    const uint32_t k = blockIdx.x * W + warp;
     if (k >= N) return;  // warp-uniform; no CTA barrier below
-    T *Ak = sA[warp], *Bk = sB[warp];
-    T *qi = sv[warp][0], *ri = sv[warp][1], *qn = sv[warp][2], *qk = sv[warp][3], *rk = sv[warp][4];
-    load_block(Ak, ld, A + (size_t)k * n * n, n, n, lane);  // Ak[row][col]
-    load_block(Bk, ld, B + (size_t)k * n * m, n, m, lane);
+    const uint32_t L = n + m, L4 = (L + 3) & ~3u;
+    T *Mt = reinterpret_cast<T *>(schur_smem) + (size_t)warp * schur_warp_elems(L, ldt);
+    T *dv = Mt + L * ldt, *wv = dv + L4, *qn = wv + L4;
+    const T *Ak = A + (size_t)k * n * n, *Bk = B + (size_t)k * n * m;
+    // every column in flight at once (cp.async); rows n..NP-1 zero-filled
+    for (uint32_t l = 0; l < L; ++l) {
+        const T *src = l < n ? Ak + (size_t)l * n : Bk + (size_t)(l - n) * n;
+        if (lane < (uint32_t)NP) cp_async_elem(Mt + l * ldt + lane, src + (lane < n ? lane : 0u), lane < n);
+    }
     if (lane < n) {
-        qi[lane] = T(1) / Qd[(size_t)k * n + lane];
+        dv[lane] = T(1) / Qd[(size_t)k * n + lane];
+        wv[lane] = q[(size_t)k * n + lane];
         qn[lane] = T(1) / Qd[(size_t)(k + 1) * n + lane];
-        qk[lane] = q[(size_t)k * n + lane];
     }
     if (lane < m) {
-        ri[lane] = T(1) / Rd[(size_t)k * m + lane];
-        rk[lane] = r[(size_t)k * m + lane];
+        dv[n + lane] = T(1) / Rd[(size_t)k * m + lane];
+        wv[n + lane] = r[(size_t)k * m + lane];
     }
+    cp_async_wait_all();
     __syncwarp();
     T *Sk = S + (size_t)k * 3 * n * n;
     // block 0 of row k: S_{k,k-1}, element (i, j) = -Qi_k[j] A_k[i][j]; block 2
@@ -150,37 +157,52 @@ __global__ void __launch_bounds__(kKktWarps * 32)
         const uint32_t row = lane;
         for (uint32_t col = 0; col < n; ++col) {
             const uint32_t e = col * n + row;
-            Sk[e] = (k > 0) ? -qi[col] * Ak[row * ld + col] : T(0);
-            if (k > 0) Sup[e] = -qi[row] * Ak[col * ld + row];
+            Sk[e] = (k > 0) ? -dv[col] * Mt[col * ldt + row] : T(0);
+            if (k > 0) Sup[e] = -dv[row] * Mt[row * ldt + col];
             if (k + 1 == N) Sk[2 * (size_t)n * n + e] = T(0);
         }
+        // gamma_k = -(c_k + M diag(d) w - Qi_{k+1} q_{k+1})
+        T g = T(0);
+        for (uint32_t l = 0; l < L; ++l) g += Mt[l * ldt + row] * (dv[l] * wv[l]);
+        gamma[(size_t)k * n + row] = -(c[(size_t)k * n + row] + g - qn[row] * q[(size_t)(k + 1) * n + row]);
     }
-    // row i of S_kk (unsymmetrised) and gamma_k
-    T srow[kKktMaxN];
-    T g = T(0);
-    if (lane < n) {
-        const uint32_t i = lane;
+    // the Gram tile
+    const uint32_t rg = lane >> 3, cg = lane & 7, r0 = rg * TR, c0 = cg * TC;
+    T acc[TR][TC];
 #pragma unroll
-        for (int j = 0; j < kKktMaxN; ++j) srow[j] = T(0);
-        row_gram(Ak, ld, qi, qk, i, n, n, srow, g);  // A Q^-1 A^T, A Q^-1 q
-        row_gram(Bk, ld, ri, rk, i, n, m, srow, g);  // B R^-1 B^T, B R^-1 r
+    for (int t = 0; t < TR; ++t)
 #pragma unroll
-        for (int j = 0; j < kKktMaxN; ++j)
-            if ((uint32_t)j == i) srow[j] += qn[i];
-        gamma[(size_t)k * n + i] = -(c[(size_t)k * n + i] + g - qn[i] * q[(size_t)(k + 1) * n + i]);
+        for (int u = 0; u < TC; ++u) acc[t][u] = T(0);
+#pragma unroll 2
+    for (uint32_t l = 0; l < L; ++l) {
+        T a[TR], b[TC];
+        load_run<T, TR>(Mt + l * ldt + r0, a);
+#pragma unroll
+        for (int u = 0; u < TC; ++u) b[u] = Mt[l * ldt + c0 + u];
+        const T d = dv[l];
+#pragma unroll
+        for (int t = 0; t < TR; ++t) {
+            const T ad = a[t] * d;
+#pragma unroll
+            for (int u = 0; u < TC; ++u) acc[t][u] += ad * b[u];
+        }
     }
-    __syncwarp();  // every lane is done with Ak
-    if (lane < n) {
+    __syncwarp();  // every lane is done with Mt: it now holds S_kk, row stride NP + 1
+    constexpr uint32_t xs = NP + 1;
+    T *X = Mt;
 #pragma unroll
-        for (int j = 0; j < kKktMaxN; ++j)
-            if ((uint32_t)j < n) Ak[lane * ld + j] = srow[j];
-    }
+    for (int t = 0; t < TR; ++t)
+#pragma unroll
+        for (int u = 0; u < TC; ++u) {
+            const uint32_t i = r0 + t, j = c0 + u;
+            if (i < n && j < n) X[i * xs + j] = (i == j) ? acc[t][u] + qn[i] : acc[t][u];
+        }
     __syncwarp();
     // block 1: S_kk symmetrised
     if (lane < n) {
         const uint32_t row = lane;
         for (uint32_t col = 0; col < n; ++col)
-            Sk[n * n + col * n + row] = T(0.5) * (Ak[row * ld + col] + Ak[col * ld + row]);
+            Sk[n * n + col * n + row] = T(0.5) * (X[row * xs + col] + X[col * xs + row]);
     }
 }
 
@@ -268,9 +290,22 @@ int form_schur(const T *A, const T *B, const T *Qd, const T *Rd, const T *q, con
     int rc = check(p, 9, n, m, N);
     if (rc) return rc;
     constexpr int W = kkt_warps<T>();
-    form_schur_kernel<T><<<(N + W - 1) / W, W * 32, 0, st>>>(A, B, Qd, Rd, q, r, c, n, m,
-                                                                                       N, S, gamma);
-    return launched("form_schur");
+    auto go = [&](auto np) -> int {
+        constexpr int NP = decltype(np)::value;
+        const size_t smem = (size_t)W * schur_warp_elems(n + m, schur_ldt<NP>()) * sizeof(T);
+        cudaError_t e = cudaFuncSetAttribute(form_schur_kernel<T, NP, W>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) {
+            gbdpcg::set_last_error(std::string("form_schur: ") + cudaGetErrorString(e));
+            return GBDPCG_ERR_CUDA;
+        }
+        form_schur_kernel<T, NP, W><<<(N + W - 1) / W, W * 32, smem, st>>>(A, B, Qd, Rd, q, r, c, n, m, N, S, gamma);
+        return launched("form_schur");
+    };
+    if (n <= 8) return go(std::integral_constant<int, 8>());
+    if (n <= 16) return go(std::integral_constant<int, 16>());
+    if (n <= 24) return go(std::integral_constant<int, 24>());
+    return go(std::integral_constant<int, 32>());
 }
 
 template <typename T>

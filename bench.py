@@ -372,8 +372,9 @@ def precision_config(gbdpcg, h, dev, count=256, n=24, N=256, workers=8):
 
 def around_solve_kernels(gbdpcg, dev, hbm_gbs, n=24, N=65536, reps=5):
     """The steps either side of the solve on one long horizon (n = 24, m = 12,
-    N = 65536 knots, FP32, random data): Schur-complement formation, KKT
-    back-substitution and the CSR -> cbtd adapter.  HBM-bound kernels: GB/s of
+    N = 65536 knots, FP32, random data): Schur-complement formation (alone and
+    with the fused block-Jacobi Phi^-1), KKT back-substitution and the
+    CSR -> cbtd adapter.  HBM-bound kernels: GB/s of
     their compulsory bytes (each input read once, each output written once)
     against the measured copy bandwidth."""
     import torch
@@ -419,8 +420,11 @@ def around_solve_kernels(gbdpcg, dev, hbm_gbs, n=24, N=65536, reps=5):
 
     s = 4
     out = {"n": n, "m": m, "N": N, "dtype": "f32"}
-    rows_b = [("form_schur", lambda: gbdpcg.form_schur(A, B, Qd, Rd, q, r, c, n, m, N, S, g),
-               s * (N * n * n + N * n * m + 2 * (N + 1) * n + N * m + N * n + 3 * n * n * N + n * N)),
+    Pi = torch.empty(n * n * N, **f)
+    form_bytes = s * (N * n * n + N * n * m + 2 * (N + 1) * n + N * m + N * n + 3 * n * n * N + n * N)
+    rows_b = [("form_schur", lambda: gbdpcg.form_schur(A, B, Qd, Rd, q, r, c, n, m, N, S, g), form_bytes),
+              ("form_schur_pinv", lambda: gbdpcg.form_schur(A, B, Qd, Rd, q, r, c, n, m, N, S, g, Pinv_out=Pi),
+               form_bytes + s * n * n * N),
               ("kkt_backsub", lambda: gbdpcg.kkt_backsub(A, B, Qd, Rd, q, r, lam, n, m, N, x, u),
                s * (N * n * n + N * n * m + 2 * (N + 1) * n + 2 * N * m + N * n + (N + 1) * n)),
               ("csr_to_cbtd", lambda: gbdpcg.csr_to_cbtd(rp32, ci, val, n, N, S, err),

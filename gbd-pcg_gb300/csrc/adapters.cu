@@ -155,6 +155,101 @@ int csr_to_cbtd(const uint32_t *d_row_ptr, const uint32_t *d_col_ind, const T *d
     return GBDPCG_SUCCESS;
 }
 
+// Dense -> cbtd.  A dense n N x n N matrix (leading dimension ld, column- or
+// row-major) gives its three diagonal blocks per block row: block b of knot k
+// is D[k n .. k n + n, (k + b - 1) n .. (k + b - 1) n + n].  One CTA per (knot,
+// block); column-major sources are copied straight (contiguous on both sides),
+// row-major ones through a shared-memory transpose.  The padding blocks of
+// knots 0 and N-1 are written as zeros.
+template <typename T, bool ROW_MAJOR>
+__global__ void __launch_bounds__(128) dense_to_cbtd_kernel(const T *__restrict__ D, uint64_t ld, uint32_t n,
+                                                            uint32_t N, T *__restrict__ out) {
+    __shared__ T tile[32 * 33];
+    const uint32_t k = blockIdx.x / 3, b = blockIdx.x - 3 * (blockIdx.x / 3);
+    const uint32_t nn = n * n;
+    T *dst = out + (size_t)k * 3 * nn + (size_t)b * nn;
+    const bool present = (b != 0 || k > 0) && (b != 2 || k + 1 < N);
+    if (!present) {
+        for (uint32_t e = threadIdx.x; e < nn; e += blockDim.x) dst[e] = T(0);
+        return;
+    }
+    const uint64_t r0 = (uint64_t)k * n, c0 = (uint64_t)(k + b - 1) * n;
+    if constexpr (!ROW_MAJOR) {
+        for (uint32_t e = threadIdx.x; e < nn; e += blockDim.x) {
+            const uint32_t j = e / n, i = e - j * n;  // e = j n + i: (i, j) of the block
+            dst[e] = D[(c0 + j) * ld + r0 + i];
+        }
+    } else {
+        // n <= 32: the block goes through one padded tile
+        for (uint32_t e = threadIdx.x; e < nn; e += blockDim.x) {
+            const uint32_t i = e / n, j = e - i * n;  // e = i n + j: row-major read
+            tile[i * 33 + j] = D[(r0 + i) * ld + c0 + j];
+        }
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < nn; e += blockDim.x) {
+            const uint32_t j = e / n, i = e - j * n;
+            dst[e] = tile[i * 33 + j];
+        }
+    }
+}
+
+// Flags any nonzero entry of D outside the block-tridiagonal band.
+template <typename T, bool ROW_MAJOR>
+__global__ void dense_band_check_kernel(const T *__restrict__ D, uint64_t ld, uint32_t n, uint32_t N,
+                                        uint32_t *err) {
+    const uint64_t rows = (uint64_t)n * N, total = rows * rows;
+    bool bad = false;
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t outer = e / rows, inner = e - outer * rows;  // contiguous index inner
+        const uint64_t r = ROW_MAJOR ? outer : inner, cc = ROW_MAJOR ? inner : outer;
+        const uint64_t kr = r / n, kc = cc / n;
+        if (kr > kc + 1 || kc > kr + 1) bad |= D[outer * ld + inner] != T(0);
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, 1u);
+}
+
+template <typename T>
+int dense_to_cbtd(const T *d_D, uint64_t ld, int row_major, uint32_t n, uint32_t N, T *d_out, uint32_t *d_err,
+                  cudaStream_t st) {
+    if (!d_D || !d_out) {
+        gbdpcg::set_last_error("NULL pointer");
+        return GBDPCG_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0 || N == 0 || n > 32) {
+        gbdpcg::set_last_error("dense_to_cbtd: need 1 <= n <= 32 and N >= 1");
+        return GBDPCG_ERR_INVALID_ARGUMENT;
+    }
+    if (ld < (uint64_t)n * N || (uint64_t)N * 3 > 0x7fffffffull) {
+        gbdpcg::set_last_error("dense_to_cbtd: leading dimension below n N, or N too large");
+        return GBDPCG_ERR_INVALID_ARGUMENT;
+    }
+    cudaError_t e = cudaSuccess;
+    if (row_major) dense_to_cbtd_kernel<T, true><<<3 * N, 128, 0, st>>>(d_D, ld, n, N, d_out);
+    else dense_to_cbtd_kernel<T, false><<<3 * N, 128, 0, st>>>(d_D, ld, n, N, d_out);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && d_err) {
+        e = cudaMemsetAsync(d_err, 0, sizeof(uint32_t), st);
+        if (e == cudaSuccess) {
+            if (row_major) dense_band_check_kernel<T, true><<<1216, 256, 0, st>>>(d_D, ld, n, N, d_err);
+            else dense_band_check_kernel<T, false><<<1216, 256, 0, st>>>(d_D, ld, n, N, d_err);
+            e = cudaGetLastError();
+        }
+        uint32_t h_err = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h_err, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess && h_err) {
+            gbdpcg::set_last_error("dense_to_cbtd: a nonzero entry lies outside the block-tridiagonal band");
+            return GBDPCG_ERR_INVALID_ARGUMENT;
+        }
+    }
+    if (e != cudaSuccess) {
+        gbdpcg::set_last_error(std::string("dense_to_cbtd: ") + cudaGetErrorString(e));
+        return GBDPCG_ERR_CUDA;
+    }
+    return GBDPCG_SUCCESS;
+}
+
 }  // namespace
 
 extern "C" {
@@ -167,6 +262,16 @@ int gbdpcg_csr_to_cbtd_f32(const uint32_t *d_row_ptr, const uint32_t *d_col_ind,
 int gbdpcg_csr_to_cbtd_f64(const uint32_t *d_row_ptr, const uint32_t *d_col_ind, const double *d_val, uint32_t n,
                            uint32_t N, double *d_out, uint32_t *d_err, gbdpcg_stream_t stream) {
     return csr_to_cbtd<double>(d_row_ptr, d_col_ind, d_val, n, N, d_out, d_err, (cudaStream_t)stream);
+}
+
+int gbdpcg_dense_to_cbtd_f32(const float *d_D, uint64_t ld, int row_major, uint32_t n, uint32_t N, float *d_out,
+                             uint32_t *d_err, gbdpcg_stream_t stream) {
+    return dense_to_cbtd<float>(d_D, ld, row_major, n, N, d_out, d_err, (cudaStream_t)stream);
+}
+
+int gbdpcg_dense_to_cbtd_f64(const double *d_D, uint64_t ld, int row_major, uint32_t n, uint32_t N, double *d_out,
+                             uint32_t *d_err, gbdpcg_stream_t stream) {
+    return dense_to_cbtd<double>(d_D, ld, row_major, n, N, d_out, d_err, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -32,6 +32,7 @@
 #include <type_traits>
 
 #include "../../include/gbdpcg.h"
+#include "gauss_jordan.cuh"
 
 namespace gbdpcg {
 void set_last_error(const std::string &msg);
@@ -74,9 +75,10 @@ struct Vec16<double> {
 template <int NP>
 __host__ __device__ constexpr uint32_t schur_ldt() { return NP + 4; }
 
-// per-warp elements: Mt (L rows) + d (L) + w (L) + Qi_{k+1} (32), L = n + m
+// per-warp elements: Mt (L rows) + d (L) + w (L) + Qi_{k+1} (32) + two pivot
+// rows of the fused block-Jacobi inverse (32 each), L = n + m
 __host__ __device__ inline uint32_t schur_warp_elems(uint32_t L, uint32_t ldt) {
-    return (L * ldt + 2 * ((L + 3) & ~3u) + 32);
+    return (L * ldt + 2 * ((L + 3) & ~3u) + 96);
 }
 
 // Asynchronous copy of one element global -> shared (cp.async, no registers,
@@ -115,13 +117,17 @@ __device__ __forceinline__ void load_run(const T *p, T (&v)[TR]) {
 // product (TR = NP / 4, TC = NP / 8), and each column l of M adds a rank-1
 // term: TR + TC shared-memory loads for TR TC FMAs.  Every element is rounded
 // as sum_l fma(M[i][l] d_l, M[j][l], .) in ascending l, then + Qi_{k+1} on the
-// diagonal, and symmetrised as 0.5 (S + S^T) through shared memory.
-template <typename T, int NP, int W>
+// diagonal, and symmetrised as 0.5 (S + S^T) through shared memory.  With
+// PINV the warp then inverts the symmetrised S_kk (rotating Gauss-Jordan, the
+// block-Jacobi builder's own routine and rounding) and writes the compact
+// block-Jacobi Phi^-1, so the preconditioner is built with S and never
+// re-read.
+template <typename T, int NP, int W, bool PINV>
 __global__ void __launch_bounds__(W * 32)
     form_schur_kernel(const T *__restrict__ A, const T *__restrict__ B, const T *__restrict__ Qd,
                       const T *__restrict__ Rd, const T *__restrict__ q, const T *__restrict__ r,
                       const T *__restrict__ c, uint32_t n, uint32_t m, uint32_t N, T *__restrict__ S,
-                      T *__restrict__ gamma) {
+                      T *__restrict__ gamma, T *__restrict__ Pinv) {
     constexpr int TR = NP / 4, TC = NP / 8;
     constexpr uint32_t ldt = schur_ldt<NP>();
     extern __shared__ __align__(16) unsigned char schur_smem[];
@@ -130,7 +136,7 @@ __global__ void __launch_bounds__(W * 32)
     if (k >= N) return;  // warp-uniform; no CTA barrier below
     const uint32_t L = n + m, L4 = (L + 3) & ~3u;
     T *Mt = reinterpret_cast<T *>(schur_smem) + (size_t)warp * schur_warp_elems(L, ldt);
-    T *dv = Mt + L * ldt, *wv = dv + L4, *qn = wv + L4;
+    T *dv = Mt + L * ldt, *wv = dv + L4, *qn = wv + L4, *s_raw = qn + 32, *s_t = s_raw + 32;
     const T *Ak = A + (size_t)k * n * n, *Bk = B + (size_t)k * n * m;
     // every column in flight at once (cp.async); rows n..NP-1 zero-filled
     for (uint32_t l = 0; l < L; ++l) {
@@ -203,6 +209,27 @@ __global__ void __launch_bounds__(W * 32)
         const uint32_t row = lane;
         for (uint32_t col = 0; col < n; ++col)
             Sk[n * n + col * n + row] = T(0.5) * (X[row * xs + col] + X[col * xs + row]);
+    }
+    if constexpr (PINV) {
+        // lane r: row r of the symmetrised S_kk (the values just written),
+        // identity beyond n
+        T a[NP];
+#pragma unroll
+        for (int cc = 0; cc < NP; ++cc)
+            a[cc] = (lane < n && (uint32_t)cc < n) ? T(0.5) * (X[lane * xs + cc] + X[cc * xs + lane])
+                                                   : ((uint32_t)cc == lane ? T(1) : T(0));
+        gbdpcg::gj_rotate<T, NP>(a, s_raw, s_t, lane);  // ends with a warp sync: X is free
+        if (lane < n) {
+#pragma unroll
+            for (int cc = 0; cc < NP; ++cc)
+                if ((uint32_t)cc < n) X[lane * xs + cc] = a[cc];
+        }
+        __syncwarp();
+        if (lane < n) {  // symmetrised, compact n^2 per knot, column-major
+            T *Pk = Pinv + (size_t)k * n * n;
+            for (uint32_t col = 0; col < n; ++col)
+                Pk[col * n + lane] = T(0.5) * (X[lane * xs + col] + X[col * xs + lane]);
+        }
     }
 }
 
@@ -285,7 +312,7 @@ int launched(const char *what) {
 
 template <typename T>
 int form_schur(const T *A, const T *B, const T *Qd, const T *Rd, const T *q, const T *r, const T *c, uint32_t n,
-               uint32_t m, uint32_t N, T *S, T *gamma, cudaStream_t st) {
+               uint32_t m, uint32_t N, T *S, T *gamma, T *Pinv, cudaStream_t st) {
     const void *p[] = {A, B, Qd, Rd, q, r, c, S, gamma};
     int rc = check(p, 9, n, m, N);
     if (rc) return rc;
@@ -293,14 +320,16 @@ int form_schur(const T *A, const T *B, const T *Qd, const T *Rd, const T *q, con
     auto go = [&](auto np) -> int {
         constexpr int NP = decltype(np)::value;
         const size_t smem = (size_t)W * schur_warp_elems(n + m, schur_ldt<NP>()) * sizeof(T);
-        cudaError_t e = cudaFuncSetAttribute(form_schur_kernel<T, NP, W>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) {
-            gbdpcg::set_last_error(std::string("form_schur: ") + cudaGetErrorString(e));
-            return GBDPCG_ERR_CUDA;
-        }
-        form_schur_kernel<T, NP, W><<<(N + W - 1) / W, W * 32, smem, st>>>(A, B, Qd, Rd, q, r, c, n, m, N, S, gamma);
-        return launched("form_schur");
+        auto launch = [&](auto kern) -> int {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) {
+                gbdpcg::set_last_error(std::string("form_schur: ") + cudaGetErrorString(e));
+                return GBDPCG_ERR_CUDA;
+            }
+            kern<<<(N + W - 1) / W, W * 32, smem, st>>>(A, B, Qd, Rd, q, r, c, n, m, N, S, gamma, Pinv);
+            return launched("form_schur");
+        };
+        return Pinv ? launch(form_schur_kernel<T, NP, W, true>) : launch(form_schur_kernel<T, NP, W, false>);
     };
     if (n <= 8) return go(std::integral_constant<int, 8>());
     if (n <= 16) return go(std::integral_constant<int, 16>());
@@ -327,12 +356,34 @@ extern "C" {
 int gbdpcg_form_schur_f32(const float *d_A, const float *d_B, const float *d_Qd, const float *d_Rd,
                           const float *d_q, const float *d_r, const float *d_c, uint32_t n, uint32_t m, uint32_t N,
                           float *d_S, float *d_gamma, gbdpcg_stream_t stream) {
-    return form_schur<float>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_c, n, m, N, d_S, d_gamma, (cudaStream_t)stream);
+    return form_schur<float>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_c, n, m, N, d_S, d_gamma, nullptr,
+                             (cudaStream_t)stream);
 }
 int gbdpcg_form_schur_f64(const double *d_A, const double *d_B, const double *d_Qd, const double *d_Rd,
-                          const double *d_q, const double *d_r, const double *d_c, uint32_t n, uint32_t m,
-                          uint32_t N, double *d_S, double *d_gamma, gbdpcg_stream_t stream) {
-    return form_schur<double>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_c, n, m, N, d_S, d_gamma, (cudaStream_t)stream);
+                          const double *d_q, const double *d_r, const double *d_c, uint32_t n, uint32_t m, uint32_t N,
+                          double *d_S, double *d_gamma, gbdpcg_stream_t stream) {
+    return form_schur<double>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_c, n, m, N, d_S, d_gamma, nullptr,
+                              (cudaStream_t)stream);
+}
+int gbdpcg_form_schur_pinv_f32(const float *d_A, const float *d_B, const float *d_Qd, const float *d_Rd,
+                               const float *d_q, const float *d_r, const float *d_c, uint32_t n, uint32_t m,
+                               uint32_t N, float *d_S, float *d_gamma, float *d_Pinv, gbdpcg_stream_t stream) {
+    if (!d_Pinv) {
+        gbdpcg::set_last_error("NULL pointer");
+        return GBDPCG_ERR_INVALID_ARGUMENT;
+    }
+    return form_schur<float>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_c, n, m, N, d_S, d_gamma, d_Pinv,
+                             (cudaStream_t)stream);
+}
+int gbdpcg_form_schur_pinv_f64(const double *d_A, const double *d_B, const double *d_Qd, const double *d_Rd,
+                               const double *d_q, const double *d_r, const double *d_c, uint32_t n, uint32_t m,
+                               uint32_t N, double *d_S, double *d_gamma, double *d_Pinv, gbdpcg_stream_t stream) {
+    if (!d_Pinv) {
+        gbdpcg::set_last_error("NULL pointer");
+        return GBDPCG_ERR_INVALID_ARGUMENT;
+    }
+    return form_schur<double>(d_A, d_B, d_Qd, d_Rd, d_q, d_r, d_c, n, m, N, d_S, d_gamma, d_Pinv,
+                              (cudaStream_t)stream);
 }
 int gbdpcg_kkt_backsub_f32(const float *d_A, const float *d_B, const float *d_Qd, const float *d_Rd,
                            const float *d_q, const float *d_r, const float *d_lambda, uint32_t n, uint32_t m,

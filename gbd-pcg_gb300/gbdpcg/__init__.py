@@ -102,10 +102,14 @@ _SIGS = {
     "gbdpcg_plan_destroy": ([_P], _I),
     "gbdpcg_form_schur_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
     "gbdpcg_form_schur_f64": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_form_schur_pinv_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P, _P], _I),
+    "gbdpcg_form_schur_pinv_f64": ([_P] * 7 + [_U, _U, _U, _P, _P, _P, _P], _I),
     "gbdpcg_kkt_backsub_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
     "gbdpcg_kkt_backsub_f64": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
     "gbdpcg_csr_to_cbtd_f32": ([_P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_csr_to_cbtd_f64": ([_P, _P, _P, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_dense_to_cbtd_f32": ([_P, ctypes.c_uint64, _I, _U, _U, _P, _P, _P], _I),
+    "gbdpcg_dense_to_cbtd_f64": ([_P, ctypes.c_uint64, _I, _U, _U, _P, _P, _P], _I),
     "gbdpcg_plan_autotune": ([_P, _U, _U, _P], _I),
     "gbdpcg_tune_export": ([_P, _P, ctypes.c_size_t, _P], _I),
     "gbdpcg_tune_import": ([_P, ctypes.c_char_p], _I),
@@ -439,12 +443,28 @@ def csr_to_cbtd(row_ptr, col_ind, val, n, N, out, err, stream=None):
     _check(fn(_tp(row_ptr), _tp(col_ind), _tp(val), n, N, _tp(out), _tp(err), _stream(stream)), "gbdpcg_csr_to_cbtd")
 
 
-def form_schur(A, B, Qd, Rd, q, r, c, n, m, N, S_out, gamma_out, stream=None):
+def dense_to_cbtd(D, n, N, out, row_major=False, ld=None, err=None, stream=None):
+    """The three diagonal blocks per block row of a dense n N x n N device
+    matrix (leading dimension ld, default n N) -> cbtd `out`; with `err` (a
+    one-element int32 device tensor) entries outside the band are checked."""
+    fn = lib().gbdpcg_dense_to_cbtd_f64 if D.dtype.itemsize == 8 else lib().gbdpcg_dense_to_cbtd_f32
+    _check(fn(_tp(D), ld if ld is not None else n * N, 1 if row_major else 0, n, N, _tp(out), _tp(err),
+              _stream(stream)), "gbdpcg_dense_to_cbtd")
+
+
+def form_schur(A, B, Qd, Rd, q, r, c, n, m, N, S_out, gamma_out, Pinv_out=None, stream=None):
     """S = C Theta^-1 C^T (cbtd) and gamma = -(c + C Theta^-1 g) from the
-    trajectory-optimisation data (device tensors; A_k, B_k column-major)."""
-    fn = lib().gbdpcg_form_schur_f64 if A.dtype.itemsize == 8 else lib().gbdpcg_form_schur_f32
-    _check(fn(*[_tp(t) for t in (A, B, Qd, Rd, q, r, c)], n, m, N, _tp(S_out), _tp(gamma_out), _stream(stream)),
-           "gbdpcg_form_schur")
+    trajectory-optimisation data (device tensors; A_k, B_k column-major); with
+    Pinv_out, also the compact block-Jacobi Phi^-1 from the same pass."""
+    f64 = A.dtype.itemsize == 8
+    if Pinv_out is None:
+        fn = lib().gbdpcg_form_schur_f64 if f64 else lib().gbdpcg_form_schur_f32
+        _check(fn(*[_tp(t) for t in (A, B, Qd, Rd, q, r, c)], n, m, N, _tp(S_out), _tp(gamma_out),
+                  _stream(stream)), "gbdpcg_form_schur")
+        return
+    fn = lib().gbdpcg_form_schur_pinv_f64 if f64 else lib().gbdpcg_form_schur_pinv_f32
+    _check(fn(*[_tp(t) for t in (A, B, Qd, Rd, q, r, c)], n, m, N, _tp(S_out), _tp(gamma_out), _tp(Pinv_out),
+              _stream(stream)), "gbdpcg_form_schur_pinv")
 
 
 def kkt_backsub(A, B, Qd, Rd, q, r, lam, n, m, N, x_out, u_out, stream=None):

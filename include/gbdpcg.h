@@ -321,6 +321,17 @@ GBDPCG_API int gbdpcg_csr_to_cbtd_f32(const uint32_t *d_row_ptr, const uint32_t 
                                       uint32_t n, uint32_t N, float *d_out, uint32_t *d_err, gbdpcg_stream_t stream);
 GBDPCG_API int gbdpcg_csr_to_cbtd_f64(const uint32_t *d_row_ptr, const uint32_t *d_col_ind, const double *d_val,
                                       uint32_t n, uint32_t N, double *d_out, uint32_t *d_err, gbdpcg_stream_t stream);
+/* Dense -> cbtd on the device: the three diagonal blocks of every block row
+ * of a dense n N x n N matrix (leading dimension ld >= n N; column-major, or
+ * row-major when row_major != 0) into d_out (3 n^2 N elements; the padding
+ * blocks of knots 0 and N-1 are written as zeros).  n <= 32.  With a non-NULL
+ * d_err (one device word of scratch) the call also scans every entry outside
+ * the band, waits, and returns GBDPCG_ERR_INVALID_ARGUMENT if one is nonzero;
+ * with d_err NULL it is stream-ordered and checks nothing. */
+GBDPCG_API int gbdpcg_dense_to_cbtd_f32(const float *d_D, uint64_t ld, int row_major, uint32_t n, uint32_t N,
+                                        float *d_out, uint32_t *d_err, gbdpcg_stream_t stream);
+GBDPCG_API int gbdpcg_dense_to_cbtd_f64(const double *d_D, uint64_t ld, int row_major, uint32_t n, uint32_t N,
+                                        double *d_out, uint32_t *d_err, gbdpcg_stream_t stream);
 
 /* The steps either side of the solve in a trajectory optimiser (no reference
  * counterpart: the callers of solvePCG in MPCGPU / GATO).  Problem: states
@@ -336,6 +347,18 @@ GBDPCG_API int gbdpcg_form_schur_f32(const float *d_A, const float *d_B, const f
 GBDPCG_API int gbdpcg_form_schur_f64(const double *d_A, const double *d_B, const double *d_Qd, const double *d_Rd,
                                      const double *d_q, const double *d_r, const double *d_c, uint32_t n, uint32_t m,
                                      uint32_t N, double *d_S, double *d_gamma, gbdpcg_stream_t stream);
+/* form_schur_pinv: the same, and the block-Jacobi Phi^-1 = blockdiag(S_kk^-1)
+ * (compact, n^2 per knot, column-major) from the same warp that formed S_kk:
+ * bit for bit what gbdpcg_block_jacobi_* builds from the S written here, with
+ * no second pass over S. */
+GBDPCG_API int gbdpcg_form_schur_pinv_f32(const float *d_A, const float *d_B, const float *d_Qd, const float *d_Rd,
+                                          const float *d_q, const float *d_r, const float *d_c, uint32_t n,
+                                          uint32_t m, uint32_t N, float *d_S, float *d_gamma, float *d_Pinv,
+                                          gbdpcg_stream_t stream);
+GBDPCG_API int gbdpcg_form_schur_pinv_f64(const double *d_A, const double *d_B, const double *d_Qd,
+                                          const double *d_Rd, const double *d_q, const double *d_r,
+                                          const double *d_c, uint32_t n, uint32_t m, uint32_t N, double *d_S,
+                                          double *d_gamma, double *d_Pinv, gbdpcg_stream_t stream);
 /* kkt_backsub: z = -Theta^-1 (g + C^T lambda): x (n (N+1)) and u (m N). */
 GBDPCG_API int gbdpcg_kkt_backsub_f32(const float *d_A, const float *d_B, const float *d_Qd, const float *d_Rd,
                                       const float *d_q, const float *d_r, const float *d_lambda, uint32_t n,

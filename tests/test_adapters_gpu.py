@@ -111,3 +111,61 @@ def test_csr_ragged_and_empty_rows(gb, oracle_mod, handle, n, N):
     err = torch.zeros(1, dtype=torch.int32, device="cuda:0")
     gb.csr_to_cbtd(_dev(rp), _dev(ci), _dev(va), n, N, out, err)
     assert out.cpu().numpy().tobytes() == _expected(Md, n, N).tobytes()
+
+
+def _dense_from_cbtd(M, n, N, dt):
+    D = np.zeros((n * N, n * N), dt)
+    for k in range(N):
+        for b in range(3):
+            kc = k + b - 1
+            if 0 <= kc < N:
+                blk = M[k * 3 * n * n + b * n * n:k * 3 * n * n + (b + 1) * n * n].reshape(n, n).T  # (i, j)
+                D[k * n:(k + 1) * n, kc * n:(kc + 1) * n] = blk
+    return D
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("row_major", [False, True])
+@pytest.mark.parametrize("n,N,pad", [(14, 9, 0), (5, 4, 3), (24, 3, 8), (32, 2, 0), (6, 1, 0)])
+def test_dense_to_cbtd_matches_layout(gb, oracle_mod, handle, dt, row_major, n, N, pad):
+    """Dense (column- or row-major, leading dimension n N + pad) -> cbtd, bit
+    for bit, padding blocks zero; the band check passes on a banded matrix."""
+    import torch
+    O = oracle_mod
+    M = O.generate(n, N, 13).cbtd(dt)
+    D = _dense_from_cbtd(M, n, N, dt)
+    ld = n * N + pad
+    buf = np.full((n * N, ld), np.nan, dt)  # row-major storage with ld columns
+    if row_major:
+        buf[:, :n * N] = D
+    else:
+        buf[:, :n * N] = D.T  # row c of buf = column c of D
+    tdt = torch.float64 if dt == np.float64 else torch.float32
+    out = torch.full((3 * n * n * N,), 7.0, dtype=tdt, device="cuda:0")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda:0")
+    Dd = torch.from_numpy(np.ascontiguousarray(buf)).to("cuda:0")
+    if pad:
+        # the band check reads only the n N x n N part; NaN padding is not an entry
+        gb.dense_to_cbtd(Dd, n, N, out, row_major=row_major, ld=ld)
+    else:
+        gb.dense_to_cbtd(Dd, n, N, out, row_major=row_major, ld=ld, err=err)
+    torch.cuda.synchronize()
+    assert out.cpu().numpy().tobytes() == _expected(M, n, N).tobytes()
+
+
+def test_dense_entry_outside_band_is_rejected(gb, oracle_mod, handle):
+    import torch
+    O = oracle_mod
+    n, N = 4, 5
+    M = O.generate(n, N, 3).cbtd(np.float32)
+    D = _dense_from_cbtd(M, n, N, np.float32)
+    D[1, 3 * n + 2] = 0.5  # knot 0's row, knot 3's column
+    out = torch.empty(3 * n * n * N, device="cuda:0")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda:0")
+    with pytest.raises(gb.GbdpcgError) as e:
+        gb.dense_to_cbtd(torch.from_numpy(D).to("cuda:0"), n, N, out, row_major=True, err=err)
+    assert e.value.code == gb.ERR_INVALID_ARGUMENT
+    # without the check the band is still extracted
+    gb.dense_to_cbtd(torch.from_numpy(D).to("cuda:0"), n, N, out, row_major=True)
+    torch.cuda.synchronize()
+    assert out.cpu().numpy().tobytes() == _expected(M, n, N).tobytes()

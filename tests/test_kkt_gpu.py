@@ -42,6 +42,33 @@ def test_form_schur(gb, oracle_mod, handle, dt, tol, n, N):
     assert not Sc[0, 0:n].any() and not Sc[N - 1, 2 * n:].any()
 
 
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n,N", CASES + [(12, 7)])
+def test_form_schur_fused_pinv_matches_builder(gb, oracle_mod, handle, dt, n, N):
+    """form_schur_pinv writes the same S and gamma as form_schur, and a
+    Phi^-1 bit for bit equal to the block-Jacobi builder's on that S (same
+    symmetrised S_kk, same Gauss-Jordan routine; n = 12 pads to 16 in the
+    formation and to 12 in the builder)."""
+    import torch
+    O = oracle_mod
+    P = O.generate_problem(n, N, 24)
+    d = _dev(O.problem_device_layout(P, dt), dt)
+    tdt = torch.float64 if dt == np.float64 else torch.float32
+    m = P["m"]
+    S1 = torch.full((3 * n * n * N,), 9.0, dtype=tdt, device="cuda:0")
+    g1 = torch.empty(n * N, dtype=tdt, device="cuda:0")
+    gb.form_schur(d["A"], d["B"], d["Qd"], d["Rd"], d["q"], d["r"], d["c"], n, m, N, S1, g1)
+    S2 = torch.full_like(S1, 5.0)
+    g2 = torch.empty_like(g1)
+    Pf = torch.full((n * n * N,), 3.0, dtype=tdt, device="cuda:0")
+    gb.form_schur(d["A"], d["B"], d["Qd"], d["Rd"], d["q"], d["r"], d["c"], n, m, N, S2, g2, Pinv_out=Pf)
+    assert torch.equal(S1, S2) and torch.equal(g1, g2)
+    Pb = torch.empty_like(Pf)
+    handle.block_jacobi(S1, Pb, n, N, gb.PINV_BLOCKDIAG)
+    torch.cuda.synchronize()
+    assert Pf.cpu().numpy().tobytes() == Pb.cpu().numpy().tobytes()
+
+
 @pytest.mark.parametrize("dt,tol", [(np.float64, 1e-13), (np.float32, 2e-6)])
 @pytest.mark.parametrize("n,N", CASES)
 def test_kkt_backsub(gb, oracle_mod, handle, dt, tol, n, N):
@@ -61,9 +88,9 @@ def test_kkt_backsub(gb, oracle_mod, handle, dt, tol, n, N):
 
 @pytest.mark.parametrize("n,N", [(14, 64), (24, 100)])
 def test_form_solve_backsub_satisfies_kkt(gb, oracle_mod, handle, n, N):
-    """FP64 end to end on the GPU: form S and gamma, build the block-Jacobi
-    Phi^-1, PCG to 1e-12, back-substitute; the dense KKT residual is at the
-    PCG tolerance's level."""
+    """FP64 end to end on the GPU: form S, gamma and the block-Jacobi Phi^-1
+    in one pass, PCG to 1e-12, back-substitute; the dense KKT residual is at
+    the PCG tolerance's level."""
     import torch
     O = oracle_mod
     P = O.generate_problem(n, N, 23)
@@ -72,9 +99,8 @@ def test_form_solve_backsub_satisfies_kkt(gb, oracle_mod, handle, n, N):
     f64 = dict(dtype=torch.float64, device="cuda:0")
     S = torch.empty(3 * n * n * N, **f64)
     g = torch.empty(n * N, **f64)
-    gb.form_schur(d["A"], d["B"], d["Qd"], d["Rd"], d["q"], d["r"], d["c"], n, m, N, S, g)
     Pinv = torch.empty(n * n * N, **f64)
-    handle.block_jacobi(S, Pinv, n, N, gb.PINV_BLOCKDIAG)
+    gb.form_schur(d["A"], d["B"], d["Qd"], d["Rd"], d["q"], d["r"], d["c"], n, m, N, S, g, Pinv_out=Pinv)
     lam = torch.zeros(n * N, **f64)
     r = handle.solve(S, Pinv, g, lam, n, N, gb.PINV_BLOCKDIAG,
                      gb.config(max_iter=2000, exit_tol=1e-12, exit_mode=gb.EXIT_RELRES))

@@ -402,3 +402,67 @@ def test_recurrence_reference_exit(gb, oracle_mod, handle):
         r = gb.solve(S, Pt, g, lam, 14, N, gb.config(max_iter=200, algorithm=gb.ALGO_RECURRENCE))
         assert r.iters == it_r
         assert relerr(lam, lam_r) < 2e-5
+
+
+# The largest systems: at the cluster solver's capacity (16 CTAs, a CTA's rows
+# at the register or shared-memory cap), a large n > 32 system on the plain
+# kernel, and (below) one past both limits.
+BIG = [("f32", 24, 512, 31), ("f32", 14, 1024, 32), ("f32", 6, 1900, 33), ("f32", 32, 320, 34),
+       ("f64", 14, 512, 35), ("f32", 40, 300, 36)]
+
+
+@pytest.mark.parametrize("dts,n,N,seed", BIG)
+def test_maximum_sizes(gb, oracle_mod, handle, dts, n, N, seed):
+    """AUTO (cluster solver, or the plain kernel for n > 32) against the
+    oracle: passes within one and accuracy against the FP64 block-Cholesky
+    solution no worse than the reference's; the plain kernel bit for bit
+    wherever its N CTAs are co-resident."""
+    O = oracle_mod
+    dt = _dt(dts)
+    sy, S, P, g = system(O, n, N, seed, dt)
+    tol = _tol(dts)
+    lam_o, it_o, mie = O.ref_pcg(S, P, g, np.zeros(n * N, dt), n, N, 400, tol)
+    assert not mie
+    lam = np.zeros(n * N, dt)
+    r = gb.solve(S, P, g, lam, n, N, gb.config(max_iter=400, exit_tol=tol))
+    assert r.status == gb.CONVERGED
+    assert abs(int(r.iters) - it_o) <= 1, (r.iters, it_o)
+    x = O.block_cholesky_solve(S.astype(np.float64), n, N, g.astype(np.float64))
+    assert relerr(lam, x) <= 1.5 * relerr(lam_o, x) + (1e-12 if dts == "f64" else 1e-6)
+    lam_p = np.zeros(n * N, dt)
+    try:
+        rp = gb.solve(S, P, g, lam_p, n, N, gb.config(algorithm=gb.ALGO_PLAIN, max_iter=400, exit_tol=tol))
+    except gb.GbdpcgError as e:  # more knots than co-resident CTAs: reported, nothing launched
+        assert e.code == gb.ERR_UNSUPPORTED and "co-resident" in str(e)
+        return
+    assert rp.iters == it_o and lam_p.tobytes() == lam_o.tobytes()
+
+
+def test_too_large_is_reported(gb, handle):
+    """n = 14, N = 20000: no cluster shape holds it (1250 knots a CTA) and the
+    plain kernel's 20000 CTAs cannot be co-resident, so the call returns
+    UNSUPPORTED before any launch, and the handle stays usable.  (n = 6,
+    N = 4096 with a cbtd Phi^-1 is past both limits too.)"""
+    n, N = 14, 20000
+    S = np.zeros(3 * n * n * N, np.float32)
+    P = np.zeros_like(S)
+    g = np.ones(n * N, np.float32)
+    lam = np.zeros(n * N, np.float32)
+    with pytest.raises(gb.GbdpcgError) as e:
+        gb.solve(S, P, g, lam, n, N, gb.config(max_iter=10))
+    assert e.value.code == gb.ERR_UNSUPPORTED
+    assert not lam.any()
+    # a normal solve still works afterwards
+    O_n, O_N = 6, 8
+    S2 = np.zeros(3 * O_n * O_n * O_N, np.float32)
+    for k in range(O_N):
+        for i in range(O_n):
+            S2[k * 3 * O_n * O_n + (O_n + i) * O_n + i] = 2.0
+    P2 = np.zeros_like(S2)
+    for k in range(O_N):
+        for i in range(O_n):
+            P2[k * 3 * O_n * O_n + (O_n + i) * O_n + i] = 0.5
+    g2 = np.ones(O_n * O_N, np.float32)
+    lam2 = np.zeros_like(g2)
+    r = gb.solve(S2, P2, g2, lam2, O_n, O_N, gb.config(max_iter=10))
+    assert r.status == gb.CONVERGED and np.allclose(lam2, 0.5)

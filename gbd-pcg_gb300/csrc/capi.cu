@@ -1628,7 +1628,7 @@ int gbdpcg_tune_import(gbdpcg_handle_t h, const char *text) {
         const bool f64v = f[0] && !f[1];
         if (!np || !find_variant(h->reg, f64v, (int)f[2], np, f[3] != 0, st, rpt, alg))
             return fail(GBDPCG_ERR_UNSUPPORTED, "tuning table line " + std::to_string(lineno) +
-                                                    " names a kernel variant this build lacks");
+                                                    " names a kernel variant this library does not contain");
         TuneKey k;
         memset(&k, 0, sizeof(k));
         k.f64 = (uint8_t)f[0];

@@ -401,7 +401,7 @@ GBDPCG_API int gbdpcg_plan_autotune(gbdpcg_plan_t plan, uint32_t flags, uint32_t
  * *length to the full length without the NUL (call with capacity 0 to size). */
 GBDPCG_API int gbdpcg_tune_export(gbdpcg_handle_t h, char *buffer, size_t capacity, size_t *length);
 /* Adds the entries of a text produced by gbdpcg_tune_export (replacing equal
- * keys).  Entries naming a kernel variant this build lacks are rejected. */
+ * keys).  Entries naming a kernel variant this library does not contain are rejected. */
 GBDPCG_API int gbdpcg_tune_import(gbdpcg_handle_t h, const char *text);
 /* Empties the handle's tuning table. */
 GBDPCG_API int gbdpcg_tune_clear(gbdpcg_handle_t h);

@@ -1,6 +1,6 @@
 """ORACLE — test infrastructure only.
 
-CPU-side checker for the GB300 PCG solver.  Only tests/, __graft_entry__.smoke()
+CPU-side oracle for the GB300 PCG solver.  Only tests/, __graft_entry__.smoke()
 and bench.py's host-core baseline may import this module; the product never does.
 
 Contents

@@ -1,6 +1,6 @@
 /*
  * ORACLE — test infrastructure only.  CPU restatement of the reference PCG
- * solver (Sdevaud/GBD-PCG) used by tests/ as the parity checker and by
+ * solver (Sdevaud/GBD-PCG) used by tests/ as the parity oracle and by
  * bench.py as the timed host-core baseline.  The product never links it.
  *
  * Two families of functions:
@@ -27,7 +27,7 @@
  *    storage, the reference exit test or a relative recursive-residual exit
  *    ||r||_2 <= tol ||gamma||_2, optional double accumulation of the dot
  *    products — with dots summed sequentially.  This is the host-core
- *    baseline (a port: the reference ships no CPU path) and the checker for
+ *    baseline (a port: the reference ships no CPU path) and the oracle for
  *    the product kernels, whose reduction order differs.
  *
  * Compile with -ffp-contract=off: every fused multiply-add is explicit.

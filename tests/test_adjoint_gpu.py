@@ -1,5 +1,5 @@
-"""Adjoint of the PCG solve (no reference counterpart; north-star
-differentiation config): dL/dgamma = mu with S mu = dL/dlambda, and the
+"""Adjoint of the PCG solve (no reference counterpart; the differentiation
+configuration): dL/dgamma = mu with S mu = dL/dlambda, and the
 block-tridiagonal dL/dS = -1/2 (mu lambda^T + lambda mu^T), for
 L = 1/2 ||lambda - lambda*||^2.  Checked against a dense FP64 gradient and
 FP64 central finite differences (step 1e-6) on 64 random symmetric

@@ -2,7 +2,7 @@
 reference PCG, include/pcg.cuh:54-218) and against the reference kernel rebuilt
 for sm_103a.
 
-Tolerances (the benchmark spec): equal iteration counts; lambda within 1e-5 relative
+Tolerances: equal iteration counts; lambda within 1e-5 relative
 (2-norm) in FP32 and 1e-12 in FP64.  The plain algorithm keeps the reference's
 arithmetic order and must match bit for bit.
 """
@@ -61,7 +61,7 @@ def test_plain_bitexact_vs_oracle(gb, oracle_mod, handle, dts, n, N, seed):
     assert lam.tobytes() == lam_o.tobytes()
 
 
-# the sizes the benchmark spec states its parity bar on: n=14 with N=32 and N=128
+# the sizes the strict parity bar is stated on: n=14 with N=32 and N=128
 STRICT = {("f32", 14, 32), ("f32", 14, 128), ("f64", 14, 128), ("f64", 14, 32)}
 
 
@@ -70,7 +70,7 @@ def test_cluster_vs_oracle(gb, oracle_mod, handle, dts, n, N, seed):
     """The cluster solver through the host C ABI (solvePCG with a cbtd Pinv).
 
     It sums dot products in a different order than the reference, so its FP32
-    iterates differ at roundoff level.  On the spec sizes it must match
+    iterates differ at roundoff level.  On the strict-bar sizes it must match
     the reference's iteration count and lambda to 1e-5 (FP32) / 1e-12 (FP64);
     on the other sizes (up to n=32, where two CPU summation orders already
     differ by 1.1e-5) it must take the same passes +-1 and be as accurate as

@@ -247,6 +247,22 @@ def single_system_latency(gbdpcg, h, dev):
             if best:
                 row[name] = {"us_per_solve": best[0], "iters": best[1], "us_per_iteration": best[0] / best[1],
                              "cluster_size": best[2]}
+        # the reference's own call, one system from pageable host arrays:
+        # solvePCG (S, Pinv, gamma, lambda in; lambda out) and pcg_solve (Phi^-1
+        # built on the GPU); median wall time per call, copies included
+        Snp, gnp, Pnp = sy.cbtd(npdt), sy.gamma.astype(npdt), Pt.cpu().numpy()
+        cfgh = gbdpcg.config(max_iter=500, exit_tol=tol)
+        for name, PP in (("host_solvePCG", Pnp), ("host_pcg_solve", None)):
+            lamh = np.zeros(n * N, npdt)
+            gbdpcg.solve(Snp, PP, gnp, lamh, n, N, cfgh)  # warm
+            ts = []
+            for _ in range(30):
+                lamh[:] = 0
+                t0 = time.perf_counter()
+                rh = gbdpcg.solve(Snp, PP, gnp, lamh, n, N, cfgh)
+                ts.append(time.perf_counter() - t0)
+            row[name] = {"us_per_call": 1e6 * float(np.median(ts)), "iters": int(rh.iters),
+                         "path": "gbdpcg_solve from pageable numpy arrays, copies and sync included"}
         out.append(row)
     return out
 

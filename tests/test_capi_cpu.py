@@ -62,3 +62,30 @@ def test_python_wrapper_validates_shapes(gb):
         gb.solve(np.zeros(35, np.float32), None, np.zeros(6, np.float32), np.zeros(6, np.float32), 2, 3)
     with pytest.raises(TypeError):
         gb.solve(np.zeros(36, np.float64), None, np.zeros(6, np.float32), np.zeros(6, np.float32), 2, 3)
+
+
+def test_adapters_and_kkt_reject_bad_arguments(gb):
+    """The input adapters and the steps around the solve check their arguments
+    before any CUDA call (the pointers below are host memory and are never
+    dereferenced)."""
+    L = gb.lib()
+    buf = np.zeros(64, np.float32)
+    p = buf.ctypes.data_as(ctypes.c_void_p)
+    INV, UNS = gb.ERR_INVALID_ARGUMENT, gb.ERR_UNSUPPORTED
+    # CSR -> cbtd: NULL pointers, empty sizes
+    assert L.gbdpcg_csr_to_cbtd_f32(None, p, p, 2, 3, p, p, None) == INV
+    assert L.gbdpcg_csr_to_cbtd_f32(p, p, p, 0, 3, p, p, None) == INV
+    assert L.gbdpcg_csr_to_cbtd_f64(p, p, p, 2, 0, p, p, None) == INV
+    # dense -> cbtd: NULL, n > 32, leading dimension below n N
+    assert L.gbdpcg_dense_to_cbtd_f32(None, 6, 0, 2, 3, p, None, None) == INV
+    assert L.gbdpcg_dense_to_cbtd_f32(p, 99, 0, 33, 3, p, None, None) == INV
+    assert L.gbdpcg_dense_to_cbtd_f64(p, 5, 1, 2, 3, p, None, None) == INV
+    assert "leading dimension" in gb.last_error()
+    # Schur formation / back-substitution: NULL, empty, too large
+    args7 = [p] * 7
+    assert L.gbdpcg_form_schur_f32(*([None] + [p] * 6), 2, 1, 3, p, p, None) == INV
+    assert L.gbdpcg_form_schur_f32(*args7, 2, 0, 3, p, p, None) == INV
+    assert L.gbdpcg_form_schur_f64(*args7, 33, 1, 3, p, p, None) == UNS
+    assert L.gbdpcg_form_schur_pinv_f32(*args7, 2, 1, 3, p, p, None, None) == INV
+    assert L.gbdpcg_kkt_backsub_f32(*([p] * 6 + [None]), 2, 1, 3, p, p, None) == INV
+    assert L.gbdpcg_kkt_backsub_f64(*args7, 0, 1, 3, p, p, None) == INV

@@ -69,6 +69,10 @@ struct Registry {
     std::vector<VariantInfo> list;
     int max_smem_optin = 0;
     int sm_count = 0;
+    // the GPU reads pageable host memory through the host's page tables
+    // (Grace: address translation services), so kernels may use host arrays
+    // in place
+    bool host_direct = false;
 };
 
 std::mutex g_reg_mu;
@@ -111,6 +115,10 @@ int get_registry(int device, Registry **out) {
     GB_CUDA(cudaDeviceGetAttribute(&reg->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
                                    device));
     GB_CUDA(cudaDeviceGetAttribute(&reg->sm_count, cudaDevAttrMultiProcessorCount, device));
+    int pageable = 0, host_tables = 0;
+    GB_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device));
+    GB_CUDA(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device));
+    reg->host_direct = pageable != 0 && host_tables != 0;
     *out = reg.get();
     g_registries[device] = std::move(reg);
     return GBDPCG_SUCCESS;
@@ -840,15 +848,36 @@ static int solve_host(bool f64, const void *S, const void *P, const void *g, voi
     const uint32_t build_layout =
         (!P && (c.algorithm == GBDPCG_ALGO_PLAIN || n > 32)) ? GBDPCG_PINV_CBTD : layout;
     const size_t pmat = P || build_layout == GBDPCG_PINV_CBTD ? mat : (size_t)n * n * N * s;
-    rc = h->host_io.ensure(mat + pmat + 2 * vec + 1024);
-    if (rc) return rc;
-    char *dS = h->host_io.as<char>(), *dP = dS + round_up(mat, 256),
-         *dg = dP + round_up(pmat, 256), *dl = dg + round_up(vec, 256);
     cudaStream_t st = nullptr;
-    GB_CUDA(cudaMemcpyAsync(dS, S, mat, cudaMemcpyHostToDevice, st));
-    if (P) GB_CUDA(cudaMemcpyAsync(dP, P, mat, cudaMemcpyHostToDevice, st));
-    GB_CUDA(cudaMemcpyAsync(dg, g, vec, cudaMemcpyHostToDevice, st));
-    GB_CUDA(cudaMemcpyAsync(dl, l, vec, cudaMemcpyHostToDevice, st));
+    // Where the GPU reads host memory through the host's page tables, the
+    // kernels use the caller's arrays in place: S, Phi^-1 and gamma are read
+    // once per solve and lambda is written once, so there are no staging
+    // copies (GBDPCG_HOST_STAGING=1 forces the copies).  The results are the
+    // same bits either way.
+    const char *stage_env = getenv("GBDPCG_HOST_STAGING");
+    const bool direct = h->reg->host_direct && !(stage_env && stage_env[0] == '1');
+    char *dS, *dP, *dg, *dl;
+    if (direct) {
+        if (!P) {
+            rc = h->host_io.ensure(pmat + 256);
+            if (rc) return rc;
+        }
+        dS = static_cast<char *>(const_cast<void *>(S));
+        dP = P ? static_cast<char *>(const_cast<void *>(P)) : h->host_io.as<char>();
+        dg = static_cast<char *>(const_cast<void *>(g));
+        dl = static_cast<char *>(l);
+    } else {
+        rc = h->host_io.ensure(mat + pmat + 2 * vec + 1024);
+        if (rc) return rc;
+        dS = h->host_io.as<char>();
+        dP = dS + round_up(mat, 256);
+        dg = dP + round_up(pmat, 256);
+        dl = dg + round_up(vec, 256);
+        GB_CUDA(cudaMemcpyAsync(dS, S, mat, cudaMemcpyHostToDevice, st));
+        if (P) GB_CUDA(cudaMemcpyAsync(dP, P, mat, cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemcpyAsync(dg, g, vec, cudaMemcpyHostToDevice, st));
+        GB_CUDA(cudaMemcpyAsync(dl, l, vec, cudaMemcpyHostToDevice, st));
+    }
     if (!P) {
         if (n > 32) return fail(GBDPCG_ERR_UNSUPPORTED, "block-Jacobi builder needs n <= 32");
         rc = block_jacobi(h, f64 ? 1 : 0, dS, dP, build_layout, n, N, st);
@@ -856,7 +885,7 @@ static int solve_host(bool f64, const void *S, const void *P, const void *g, voi
     }
     rc = solve_dev(h, f64, dS, dP, build_layout, dg, dl, n, N, &c, nullptr, st);
     if (rc) return rc;
-    GB_CUDA(cudaMemcpyAsync(l, dl, vec, cudaMemcpyDeviceToHost, st));
+    if (!direct) GB_CUDA(cudaMemcpyAsync(l, dl, vec, cudaMemcpyDeviceToHost, st));
     gbdpcg_result r;
     rc = gbdpcg_last_result(h, &r);
     if (rc) return rc;

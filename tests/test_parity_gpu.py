@@ -466,3 +466,29 @@ def test_too_large_is_reported(gb, handle):
     lam2 = np.zeros_like(g2)
     r = gb.solve(S2, P2, g2, lam2, O_n, O_N, gb.config(max_iter=10))
     assert r.status == gb.CONVERGED and np.allclose(lam2, 0.5)
+
+
+@pytest.mark.parametrize("algo", ["auto", "plain"])
+@pytest.mark.parametrize("with_pinv", [True, False])
+@pytest.mark.parametrize("dts", ["f32", "f64"])
+def test_host_arrays_in_place_match_staged(gb, oracle_mod, handle, monkeypatch, algo, with_pinv, dts):
+    """Where the GPU reads host memory through the host's page tables, the
+    host-array solve uses the caller's arrays in place (no staging copies);
+    GBDPCG_HOST_STAGING=1 forces the copies.  Same bits, same passes, inputs
+    untouched, lambda read as the warm start and written in place."""
+    O = oracle_mod
+    dt = _dt(dts)
+    n, N = 14, 64
+    _, S, P, g = system(O, n, N, 41, dt)
+    S0, P0, g0 = S.copy(), P.copy(), g.copy()
+    cfg = gb.config(max_iter=300, exit_tol=_tol(dts),
+                    algorithm=gb.ALGO_PLAIN if algo == "plain" else gb.ALGO_AUTO)
+    PP = P if with_pinv else None
+    lam_d = np.full(n * N, 0.25, dt)
+    r_d = gb.solve(S, PP, g, lam_d, n, N, cfg)
+    monkeypatch.setenv("GBDPCG_HOST_STAGING", "1")
+    lam_s = np.full(n * N, 0.25, dt)
+    r_s = gb.solve(S, PP, g, lam_s, n, N, cfg)
+    assert r_d.status == r_s.status == gb.CONVERGED
+    assert r_d.iters == r_s.iters and lam_d.tobytes() == lam_s.tobytes()
+    assert S.tobytes() == S0.tobytes() and P.tobytes() == P0.tobytes() and g.tobytes() == g0.tobytes()

@@ -33,7 +33,7 @@
 namespace gbdpcg {
 cudaError_t launch_block_jacobi(int kind, const SysDesc *d_descs, const uint64_t *d_prefix,
                                 uint32_t nsys, uint64_t total_knots, int tri_layout,
-                                cudaStream_t stream);
+                                cudaStream_t stream, const SysDesc *one = nullptr);
 }
 
 using namespace gbdpcg;
@@ -752,23 +752,14 @@ static int block_jacobi(gbdpcg_handle_t h, int kind, const void *S, void *P, uin
     if (n == 0 || N == 0 || n > 32) return fail(GBDPCG_ERR_UNSUPPORTED, "block-Jacobi needs 1 <= n <= 32");
     if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad layout");
     HandleScope scope(h->device);
-    // descriptor + prefix live in the handle workspace, after the result slots
+    // the one descriptor goes to the kernel by value: stream-ordered, no upload
     SysDesc d;
     memset(&d, 0, sizeof(d));
     d.S = S;
     d.P = P;
     d.n = n;
     d.N = N;
-    char *base = h->ws.as<char>(sizeof(SysResult) * 2 + 256);
-    uint64_t prefix = 0;
-    GB_CUDA(cudaMemcpyAsync(base, &d, sizeof(d), cudaMemcpyHostToDevice, stream));
-    GB_CUDA(cudaMemcpyAsync(base + sizeof(SysDesc), &prefix, sizeof(prefix),
-                            cudaMemcpyHostToDevice, stream));
-    GB_CUDA(launch_block_jacobi(kind, reinterpret_cast<SysDesc *>(base),
-                                reinterpret_cast<uint64_t *>(base + sizeof(SysDesc)), 1, N,
-                                layout == GBDPCG_PINV_CBTD, stream));
-    // the host-side sources above must outlive the copies
-    GB_CUDA(cudaStreamSynchronize(stream));
+    GB_CUDA(launch_block_jacobi(kind, nullptr, nullptr, 1, N, layout == GBDPCG_PINV_CBTD, stream, &d));
     return GBDPCG_SUCCESS;
 }
 

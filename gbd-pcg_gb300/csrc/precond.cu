@@ -21,6 +21,7 @@
 // the FP32-inner refinement).
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "gauss_jordan.cuh"
 #include "pcg_types.h"
@@ -65,20 +66,23 @@ __device__ __forceinline__ void invert_knot(const TI *Sk, TO *row, uint32_t n, i
 template <typename TI, typename TO, typename CT>
 __global__ void __launch_bounds__(kPrecWarps * 32)
     block_jacobi_kernel(const SysDesc *__restrict__ descs, const uint64_t *__restrict__ knot_prefix,
-                        uint32_t nsys, uint64_t total_knots, int tri_layout) {
+                        uint32_t nsys, uint64_t total_knots, int tri_layout, const SysDesc one) {
     __shared__ CT sX[kPrecWarps][kPrecMaxN * (kPrecMaxN + 1)];
     __shared__ __align__(16) CT sR[kPrecWarps][2][kPrecMaxN];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint64_t gk = (uint64_t)blockIdx.x * kPrecWarps + warp;
     if (gk >= total_knots) return;  // warp-uniform; no CTA-wide barrier below
-    // system owning global knot gk: last s with knot_prefix[s] <= gk
+    // system owning global knot gk: last s with knot_prefix[s] <= gk (or the
+    // one system passed by value)
     uint32_t lo = 0, hi = nsys;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) / 2;
-        if (knot_prefix[mid] <= gk) lo = mid; else hi = mid;
+    if (descs) {
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (knot_prefix[mid] <= gk) lo = mid; else hi = mid;
+        }
     }
-    const SysDesc d = descs[lo];
-    const uint32_t n = d.n, k = (uint32_t)(gk - knot_prefix[lo]);
+    const SysDesc d = descs ? descs[lo] : one;
+    const uint32_t n = d.n, k = (uint32_t)(descs ? gk - knot_prefix[lo] : gk);
     if (n == 0 || n > (uint32_t)kPrecMaxN) return;
     const TI *Sk = static_cast<const TI *>(d.S) + (size_t)k * 3 * n * n + (size_t)n * n;
     TO *row = static_cast<TO *>(const_cast<void *>(d.P)) + (size_t)k * (tri_layout ? 3 : 1) * n * n;
@@ -92,20 +96,25 @@ __global__ void __launch_bounds__(kPrecWarps * 32)
 
 // kind: 0 float S -> float Phi^-1 (float arithmetic); 1 double -> double;
 // 2 double S -> float Phi^-1 (double arithmetic, for the refinement's inner solve)
+// d_descs == nullptr: the single system *one (total_knots = its N), passed to
+// the kernel by value (no descriptor upload).
 cudaError_t launch_block_jacobi(int kind, const SysDesc *d_descs, const uint64_t *d_prefix,
                                 uint32_t nsys, uint64_t total_knots, int tri_layout,
-                                cudaStream_t stream) {
+                                cudaStream_t stream, const SysDesc *one) {
     if (total_knots == 0) return cudaSuccess;
+    SysDesc o;
+    if (one) o = *one;
+    else memset(&o, 0, sizeof(o));
     const dim3 grid((unsigned)((total_knots + kPrecWarps - 1) / kPrecWarps)), block(kPrecWarps * 32);
     if (kind == 1)
         block_jacobi_kernel<double, double, double><<<grid, block, 0, stream>>>(
-            d_descs, d_prefix, nsys, total_knots, tri_layout);
+            d_descs, d_prefix, nsys, total_knots, tri_layout, o);
     else if (kind == 2)
         block_jacobi_kernel<double, float, double><<<grid, block, 0, stream>>>(
-            d_descs, d_prefix, nsys, total_knots, tri_layout);
+            d_descs, d_prefix, nsys, total_knots, tri_layout, o);
     else
         block_jacobi_kernel<float, float, float><<<grid, block, 0, stream>>>(
-            d_descs, d_prefix, nsys, total_knots, tri_layout);
+            d_descs, d_prefix, nsys, total_knots, tri_layout, o);
     return cudaGetLastError();
 }
 

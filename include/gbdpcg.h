@@ -231,8 +231,8 @@ GBDPCG_API int gbdpcg_block_jacobi_f64to32(gbdpcg_handle_t h, const double *d_S,
                                            uint32_t n, uint32_t N, gbdpcg_stream_t stream);
 
 /* Block-Jacobi preconditioner Phi^-1 = blockdiag(S_kk^-1) of a cbtd S, on the
- * GPU, in cbtd or compact layout.  No reference counterpart: the reference
- * takes Phi^-1 from its caller. */
+ * GPU, in cbtd or compact layout; stream-ordered.  No reference counterpart:
+ * the reference takes Phi^-1 from its caller. */
 GBDPCG_API int gbdpcg_block_jacobi_f32(gbdpcg_handle_t h, const float *d_S, float *d_Pinv,
                             uint32_t pinv_layout, uint32_t n, uint32_t N,
                             gbdpcg_stream_t stream);

@@ -21,6 +21,9 @@ struct PrecVec<float> {
         const float4 t = *reinterpret_cast<const float4 *>(p);
         v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
     }
+    __device__ static void put(float *p, const float *v) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
 };
 template <>
 struct PrecVec<double> {
@@ -29,19 +32,23 @@ struct PrecVec<double> {
         const double2 t = *reinterpret_cast<const double2 *>(p);
         v[0] = t.x; v[1] = t.y;
     }
+    __device__ static void put(double *p, const double *v) {
+        *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+    }
 };
 
 // Rotating Gauss-Jordan inverse of the NP x NP block whose row `lane` is a
-// (lanes >= NP hold nothing).  s_raw, s_t: NP-element, 16-byte aligned rows.
+// (lanes >= NP hold nothing).  s_raw, s_t: NP-element, 16-byte aligned rows;
+// NP a multiple of the 16-byte vector width.
 template <typename CT, int NP>
 __device__ __forceinline__ void gj_rotate(CT (&a)[NP], CT *s_raw, CT *s_t, uint32_t lane) {
     constexpr int W = PrecVec<CT>::W;
 #pragma unroll 1
     for (uint32_t j = 0; j < (uint32_t)NP; ++j) {
         const bool pivot = lane == j;
-        if (pivot) {
+        if (pivot) {  // the pivot row, 16 bytes a store
 #pragma unroll
-            for (int c = 0; c < NP; ++c) s_raw[c] = a[c];
+            for (int c = 0; c < NP; c += W) PrecVec<CT>::put(s_raw + c, a + c);
         }
         __syncwarp();
         CT piv = s_raw[0];

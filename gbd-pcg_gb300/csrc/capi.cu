@@ -241,9 +241,24 @@ int acc_kind(bool f64_system, bool refine, uint32_t dot_precision) {
     return (int)dot_precision;
 }
 
+// Cluster size a lone system (latency, not throughput) starts its search at:
+// C = 1 up to 40 knots (no cluster barriers), else about 16 knots a CTA (8 for
+// FP64 rows), rounded up to a power of two.  Measured on n = 14: N = 32 is
+// fastest at C = 1, N = 128 at C = 8 (FP32) and C = 16 (FP64).
+uint32_t lone_cluster_pref(bool f64_rows, uint32_t N) {
+    if (N <= 40) return 1;
+    const uint32_t per = f64_rows ? 8 : 16;
+    const uint32_t want = (N + per - 1) / per;
+    uint32_t p = 1;
+    while (p < want) p <<= 1;
+    return std::min<uint32_t>(16, p);
+}
+
+// c_pref > 1 (lone systems, cluster size not pinned): clusters from c_pref up
+// are tried first, then the smallest that fits.
 int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layout,
                  const gbdpcg_config &cfg, Shape *out, bool refine = false,
-                 const TuneChoice *tuned = nullptr) {
+                 const TuneChoice *tuned = nullptr, uint32_t c_pref = 1) {
     Shape s;
     const int np = np_for(n);
     if (refine) {
@@ -268,30 +283,34 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
     if (alg == 1 && acc == 2)
         return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm has no float-float accumulation");
     if (tuned && tuned_shape(reg, f64 && !refine, acc, np, ptri, n, N, *tuned, out)) return GBDPCG_SUCCESS;
-    for (const Pref &pf : storage_prefs(f64 && !refine, ptri, cfg.storage)) {
-        if (pf.rpt > 1 && (n % pf.rpt) != 0) continue;
-        VariantInfo *vi = find_variant(reg, f64 && !refine, acc, np, ptri, pf.st, pf.rpt, alg);
-        if (!vi) continue;
-        uint32_t cap = cfg.max_threads ? cfg.max_threads : (uint32_t)vi->max_threads;
-        cap = std::min<uint32_t>(cap, (uint32_t)vi->max_threads);
-        const uint32_t c_lo = cfg.cluster_size ? cfg.cluster_size : 1;
-        const uint32_t c_hi = cfg.cluster_size ? cfg.cluster_size : 16;
-        for (uint32_t C = c_lo; C <= c_hi; ++C) {
-            if (C > 8 && (C & (C - 1))) continue;  // large clusters: powers of two only
-            const uint32_t K = (N + C - 1) / C;
-            const uint32_t thr = (K * n + pf.rpt - 1) / pf.rpt;
-            if (thr > cap) continue;
-            if (vi->v.smem_bytes(K, C, 32) > (size_t)reg->max_smem_optin) continue;
-            s.vi = vi;
-            s.C = C;
-            s.K = K;
-            // CTA sizes are rounded to 64 threads so that systems of similar
-            // size share a launch
-            s.threads = std::min<uint32_t>(cap, std::max<uint32_t>(64, (thr + 63) / 64 * 64));
-            if (s.threads < thr) s.threads = (thr + 31) / 32 * 32;
-            *out = s;
-            return GBDPCG_SUCCESS;
+    const uint32_t first_lo = (cfg.cluster_size == 0 && c_pref > 1) ? c_pref : 1;
+    for (uint32_t from : {first_lo, 1u}) {
+        for (const Pref &pf : storage_prefs(f64 && !refine, ptri, cfg.storage)) {
+            if (pf.rpt > 1 && (n % pf.rpt) != 0) continue;
+            VariantInfo *vi = find_variant(reg, f64 && !refine, acc, np, ptri, pf.st, pf.rpt, alg);
+            if (!vi) continue;
+            uint32_t cap = cfg.max_threads ? cfg.max_threads : (uint32_t)vi->max_threads;
+            cap = std::min<uint32_t>(cap, (uint32_t)vi->max_threads);
+            const uint32_t c_lo = cfg.cluster_size ? cfg.cluster_size : from;
+            const uint32_t c_hi = cfg.cluster_size ? cfg.cluster_size : 16;
+            for (uint32_t C = c_lo; C <= c_hi; ++C) {
+                if (C > 8 && (C & (C - 1))) continue;  // large clusters: powers of two only
+                const uint32_t K = (N + C - 1) / C;
+                const uint32_t thr = (K * n + pf.rpt - 1) / pf.rpt;
+                if (thr > cap) continue;
+                if (vi->v.smem_bytes(K, C, 32) > (size_t)reg->max_smem_optin) continue;
+                s.vi = vi;
+                s.C = C;
+                s.K = K;
+                // CTA sizes are rounded to 64 threads so that systems of similar
+                // size share a launch
+                s.threads = std::min<uint32_t>(cap, std::max<uint32_t>(64, (thr + 63) / 64 * 64));
+                if (s.threads < thr) s.threads = (thr + 31) / 32 * 32;
+                *out = s;
+                return GBDPCG_SUCCESS;
+            }
         }
+        if (from == 1) break;  // the second pass would repeat the first
     }
     if (cfg.algorithm == GBDPCG_ALGO_AUTO && layout == GBDPCG_PINV_CBTD) {
         s.plain = true;  // too large for 16 CTAs of rows: one CTA per knot
@@ -464,7 +483,8 @@ int solve_one(gbdpcg_handle_s *h, bool f64, const SysDesc &d0, const gbdpcg_conf
     SysDesc d = d0;
     d.result = 0;
     Shape sh;
-    rc = choose_shape(h->reg, f64, d.n, d.N, layout, cfg, &sh, refine);
+    rc = choose_shape(h->reg, f64, d.n, d.N, layout, cfg, &sh, refine, nullptr,
+                      lone_cluster_pref(f64 && !refine, d.N));
     if (rc) return rc;
     h->d_last = d_res;
     h->last_stream = stream;

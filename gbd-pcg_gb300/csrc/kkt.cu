@@ -21,10 +21,13 @@
 // written in the cbtd layout (padding blocks of knots 0 and N-1 zero), gamma
 // and lambda are n N, x is n (N+1), u is m N.
 //
-// Both kernels run one warp per knot (lane i owns row i of the knot's
-// blocks); they read each input once and write each output once, so HBM
-// bandwidth bounds them.  S_kk is symmetrised through shared memory
-// (0.5 (S + S^T), exactly symmetric).
+// Both kernels run one warp per knot and read each input once and write each
+// output once, so HBM bandwidth bounds them.  The formation stages [A_k | B_k]
+// in shared memory and forms its Gram product as a register tile per lane;
+// S_kk is symmetrised through shared memory (0.5 (S + S^T), exactly
+// symmetric), and the formation can invert S_kk in the same warp (the
+// block-Jacobi Phi^-1).  The back-substitution's lane i reads column i of
+// A_k and B_k.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -41,20 +44,20 @@ void set_last_error(const std::string &msg);
 namespace {
 
 constexpr int kKktMaxN = 32;  // n, m <= 32
-// knots per CTA (4 float, 2 double: 36 KB of static shared memory either way)
+// knots per CTA (4 float, 2 double: at most about 40 KB of dynamic shared
+// memory either way in the formation)
 template <typename T>
 constexpr int kkt_warps() { return sizeof(T) == 8 ? 2 : 4; }
 
-// Shared-memory rows of a knot's blocks: kKktMaxN columns padded to a 16-byte
-// multiple, so that 16-byte vectors of consecutive columns can be loaded.
+// elements of one 16-byte vector
 template <typename T>
 __host__ __device__ constexpr int kkt_vw() { return 16 / (int)sizeof(T); }
 
+// 16-byte global loads of consecutive elements (the back-substitution's columns)
 template <typename T>
 struct Vec16;
 template <>
 struct Vec16<float> {
-    using type = float4;
     __device__ static void get(const float *p, float (&v)[4]) {
         const float4 t = *reinterpret_cast<const float4 *>(p);
         v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;

@@ -21,8 +21,15 @@ Printed JSON line (rank 0):
              exceed it).  `compulsory` gives the once-per-solve bytes.
   cpu_baseline  the oracle's C port of the same PCG on the host cores
   plain_pcg  one system per launch with the plain (reference-scheme) kernel
+  single_system  one system alone (n = 14, N = 32 and 128): us per iteration
+             of each form, and the host-array solvePCG / pcg_solve calls
+  adjoint, precision  the forward + adjoint and FP32 + FP64 refinement configs
+  around_solve  Schur formation (alone and with the fused Phi^-1), KKT
+             back-substitution and CSR -> cbtd on one long horizon
+  block_jacobi  the Phi^-1 build over the batch
 --impl reference: times the reference's CPU path on the host cores — the
 reference ships none, so the oracle's C port of its PCG (all host threads).
+--only around-solve | block-jacobi: that section alone (profiling).
 """
 from __future__ import annotations
 

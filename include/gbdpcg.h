@@ -18,7 +18,17 @@
  * given compactly: n^2 per knot, column-major.  Vectors are n*N, knot-major.
  *
  * Supported sizes: 1 <= n <= 32 on the cluster solver (any N up to what 16
- * CTAs hold); larger n runs the plain algorithm (one CTA per knot).
+ * CTAs hold); larger n, and systems past that with a cbtd Phi^-1, run the
+ * plain algorithm (one CTA per knot, all N co-resident); past both a call
+ * returns GBDPCG_ERR_UNSUPPORTED before launching anything.
+ *
+ * Groups of entry points: single solves (host arrays, device pointers),
+ * batched plans (graph replay, autotuner and its table, end-to-end pipelines
+ * from host memory), the block-Jacobi builder, the adjoint, FP32 + FP64
+ * refinement, an allocation-free solve, input adapters (CSR and dense to
+ * cbtd), and the steps either side of the solve in a trajectory optimiser
+ * (Schur-complement formation, optionally with the block-Jacobi Phi^-1, and
+ * KKT back-substitution).
  */
 #ifndef GBDPCG_H
 #define GBDPCG_H

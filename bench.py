@@ -34,6 +34,7 @@ reference ships none, so the oracle's C port of its PCG (all host threads).
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -628,10 +629,15 @@ def main():
         fn()  # warm
         barrier()
         ts = []
-        for _ in range(e2e_steps):
-            t0 = time.perf_counter()
-            fn()
-            ts.append(time.perf_counter() - t0)
+        gc.collect()
+        gc.disable()  # as timeit does: no cyclic collection inside a timed step
+        try:
+            for _ in range(e2e_steps):
+                t0 = time.perf_counter()
+                fn()
+                ts.append(time.perf_counter() - t0)
+        finally:
+            gc.enable()
         return (max_over_ranks(statistics.median(ts), world, dev), max_over_ranks(sum(ts), world, dev))
 
     e2e_med, e2e_s = host_steps(lambda: plan.solve_host(hS, hg, hl, with_results=True))

@@ -23,13 +23,16 @@ Printed JSON line (rank 0):
   plain_pcg  one system per launch with the plain (reference-scheme) kernel
   single_system  one system alone (n = 14, N = 32 and 128): us per iteration
              of each form, and the host-array solvePCG / pcg_solve calls
+  single_system_n128  n = 14, N = 128, seeds 0-9, FP32 and FP64: the reference
+             kernel rebuilt for sm_103a beside the plain kernel and the
+             cluster solver (seed means)
   adjoint, precision  the forward + adjoint and FP32 + FP64 refinement configs
   around_solve  Schur formation (alone and with the fused Phi^-1), KKT
              back-substitution and CSR -> cbtd on one long horizon
   block_jacobi  the Phi^-1 build over the batch
 --impl reference: times the reference's CPU path on the host cores — the
 reference ships none, so the oracle's C port of its PCG (all host threads).
---only around-solve | block-jacobi: that section alone (profiling).
+--only around-solve | block-jacobi | single-system-n128: that section alone.
 """
 from __future__ import annotations
 
@@ -63,9 +66,10 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--no-extras", action="store_true", help="skip the baselines and the other configurations")
-    ap.add_argument("--only", default=None, choices=["around-solve", "block-jacobi"],
+    ap.add_argument("--only", default=None, choices=["around-solve", "block-jacobi", "single-system-n128"],
                     help="time one section alone and print its JSON (profiling): the kernels either side of "
-                         "the solve, or the block-Jacobi build over the batch")
+                         "the solve, the block-Jacobi build over the batch, or the n = 14, N = 128 seeds "
+                         "beside the rebuilt reference kernel")
     ap.add_argument("--knots", type=int, default=65536, help="knots of the --only around-solve horizon")
     ap.add_argument("--algorithm", default="auto", choices=["auto", "standard", "recurrence", "single-reduction"])
     ap.add_argument("--storage", default="auto", choices=["auto", "registers", "shared", "split", "hybrid", "tmem"],
@@ -272,6 +276,98 @@ def single_system_latency(gbdpcg, h, dev):
             row[name] = {"us_per_call": 1e6 * float(np.median(ts)), "iters": int(rh.iters),
                          "path": "gbdpcg_solve from pageable numpy arrays, copies and sync included"}
         out.append(row)
+    return out
+
+
+def n128_seed_sweep(gbdpcg, h, dev, reps=20, seeds=range(10)):
+    """The larger single system, n = 14, N = 128, seeds 0-9, FP32 to 1e-6 and
+    FP64 to 1e-12 (the reference's exit test |r.z| < tol, max_iter 200):
+
+      reference_kernel  the reference's own kernel pcg<T, 14, 128>
+                        (include/pcg.cuh:54-218) rebuilt for sm_103a and
+                        launched as its device-pointer solvePCG launches it
+                        (include/interface.cuh:94-146: cooperative, N CTAs of
+                        64 threads), cbtd Phi^-1 — a baseline, never the product
+      plain             this library's plain kernel (the same scheme, runtime
+                        sizes), cbtd Phi^-1
+      cluster, recurrence  the cluster solver and its recurrence form, compact
+                        Phi^-1, at the cluster size fastest on seed 0
+
+    Every form: `reps` launches from the same inputs, CUDA events around each
+    launch (the reference launcher's own method), mean per launch; reported as
+    the mean over the seeds, with the per-seed passes."""
+    import torch
+    from gbdpcg.workload import generate
+    from oracle import oracle as O  # the rebuilt reference kernel's launcher (baseline only)
+    n, N = 14, 128
+    stream = torch.cuda.current_stream()
+
+    def per_launch(fn):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        return 1e3 * float(np.mean(ts))
+
+    out = {"n": n, "N": N, "seeds": list(seeds), "reps_per_seed": reps,
+           "timing": "CUDA events around each launch, mean of the launches, then mean over seeds"}
+    for dts, tdt, npdt, tol in (("f32", torch.float32, np.float32, 1e-6), ("f64", torch.float64, np.float64, 1e-12)):
+        forms = {k: {"us": [], "iters": []} for k in ("reference_kernel", "plain", "cluster", "recurrence")}
+        csize = {}
+        for seed in seeds:
+            sy = generate(n, N, seed)
+            S = torch.from_numpy(sy.cbtd(npdt)).to(dev)
+            g = torch.from_numpy(sy.gamma.astype(npdt)).to(dev)
+            P = torch.empty(n * n * N, dtype=tdt, device=dev)
+            h.block_jacobi(S, P, n, N, gbdpcg.PINV_BLOCKDIAG)
+            Pt = torch.zeros(N, 3 * n, n, dtype=tdt, device=dev)
+            Pt[:, n:2 * n, :] = P.view(N, n, n)
+            Pt = Pt.view(-1)
+            lam = torch.zeros(n * N, dtype=tdt, device=dev)
+            if O.have_ref_kernel(dts, n, N):
+                _, it, mie, ms = O.ref_kernel_solve(S.cpu().numpy(), Pt.cpu().numpy(), g.cpu().numpy(),
+                                                    np.zeros(n * N, npdt), n, N, 200, tol, reps=reps + 1)
+                forms["reference_kernel"]["us"].append(1e3 * float(np.mean(ms[1:])))
+                forms["reference_kernel"]["iters"].append(it)
+            for name, algo, PP, lay in (("plain", gbdpcg.ALGO_PLAIN, Pt, gbdpcg.PINV_CBTD),
+                                        ("cluster", gbdpcg.ALGO_CLUSTER, P, gbdpcg.PINV_BLOCKDIAG),
+                                        ("recurrence", gbdpcg.ALGO_RECURRENCE, P, gbdpcg.PINV_BLOCKDIAG)):
+                cfg = gbdpcg.config(max_iter=200, exit_tol=tol, algorithm=algo, zero_guess=1)
+                if name not in csize:  # cluster size: fastest on the first seed
+                    best = None
+                    for C in ((0,) if algo == gbdpcg.ALGO_PLAIN else (1, 2, 4, 8, 16)):
+                        cfg.cluster_size = C
+                        try:
+                            us = per_launch(lambda: h.solve(S, PP, g, lam, n, N, lay, cfg, sync=False))
+                        except gbdpcg.GbdpcgError:
+                            continue
+                        if best is None or us < best[0]:
+                            best = (us, C)
+                    csize[name] = best[1]
+                cfg.cluster_size = csize[name]
+                forms[name]["us"].append(per_launch(lambda: h.solve(S, PP, g, lam, n, N, lay, cfg, sync=False)))
+                forms[name]["iters"].append(int(h.last_result().iters))
+        row = {}
+        for name, f in forms.items():
+            if not f["us"]:
+                row[name] = {"unavailable": "reference kernel not built"}
+                continue
+            us, it = float(np.mean(f["us"])), float(np.mean(f["iters"]))
+            row[name] = {"us_per_solve_mean": us, "iters_mean": it, "us_per_iteration": us / it,
+                         "iters_per_seed": f["iters"], "us_per_solve_per_seed": f["us"]}
+            if name in csize and name != "plain":
+                row[name]["cluster_size"] = csize[name]
+        if "us_per_solve_mean" in row["reference_kernel"]:
+            ref = row["reference_kernel"]["us_per_solve_mean"]
+            row["speedup_vs_reference_kernel"] = {k: ref / row[k]["us_per_solve_mean"]
+                                                  for k in ("plain", "cluster", "recurrence")}
+        out[dts] = row
     return out
 
 
@@ -555,6 +651,11 @@ def main():
     if args.only == "around-solve":
         print(json.dumps({"around_solve": around_solve_kernels(gbdpcg, dev, hbm, N=args.knots)}), flush=True)
         return
+    if args.only == "single-system-n128":
+        h1 = gbdpcg.Handle(local)
+        print(json.dumps({"single_system_n128": n128_seed_sweep(gbdpcg, h1, dev)}), flush=True)
+        h1.close()
+        return
 
     descs, Sa, ga, nP = build_batch(rank, args.systems, max(1, (os.cpu_count() or 1) // max(1, world)))
     count = len(descs)
@@ -749,6 +850,7 @@ def main():
                                           f"oracle/pcg_oracle.c, {dt:.1f} s"}
     if not args.no_extras and world == 1:
         for key, fn in (("single_system", lambda: single_system_latency(gbdpcg, h, dev)),
+                        ("single_system_n128", lambda: n128_seed_sweep(gbdpcg, h, dev)),
                         ("adjoint", lambda: adjoint_config(gbdpcg, h, dev, tune_flags)),
                         ("precision", lambda: precision_config(gbdpcg, h, dev)),
                         ("around_solve", lambda: around_solve_kernels(gbdpcg, dev, hbm)),

@@ -404,6 +404,16 @@ int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
     return GBDPCG_SUCCESS;
 }
 
+}  // namespace
+
+namespace gbdpcg {
+// The config checks of the handle entry points, for entry points in other
+// translation units (a config one entry point rejects, every one rejects).
+int check_config(const gbdpcg_config *cfg, uint32_t layout) { return check_cfg(cfg, layout); }
+}  // namespace gbdpcg
+
+namespace {
+
 // Launch the plain algorithm for one system (cooperative, N CTAs of 64 threads).
 int launch_plain(gbdpcg_handle_s *h, bool f64, const SysDesc &d, SysResult *d_res,
                  cudaStream_t stream, DevBuf &scratch) {

@@ -12,20 +12,25 @@
 // This entry point runs the same plain kernel (one CTA per knot, the
 // reference's arithmetic order) with its scratch — r and p (n*N floats each),
 // the two dot-partial arrays (N floats each) and the result record — placed
-// in one file-scope __device__ array of kNoAllocScratchBytes.  Every GPU that
-// loads the library reserves that array until the process exits.  The device
-// address of the array is looked up with cudaGetSymbolAddress once per
-// device, on the first call on that device, with that device current; make
-// that first call before any stream capture.  All calls share the array and
-// it keeps the last call's contents; nothing in it needs to start at zero
-// (the kernel writes every scratch element before reading it).  Calls whose
-// kernels overlap on the GPU (two streams, two threads) race on the array.
+// in one file-scope __device__ array of kNoAllocScratchBytes.  The array lives
+// in the library's device code, which CUDA loads into a device's context when
+// the library's kernels are first needed there (lazily, by default), so the
+// first call on each device is what loads the module and reserves the array.
+// That first call can therefore still fail for want of device memory: make it
+// at start-up, as a warm-up, before other allocators take the memory and
+// before any stream capture.  From then on the device holds the array until
+// the process exits.  Every call looks up the array's device address with
+// cudaGetSymbolAddress, with the calling device current (a host-side lookup
+// that allocates nothing), so a context reset that reloads the module is
+// picked up.  All calls share the array and it keeps the last call's
+// contents; nothing in it needs to start at zero (the kernel writes every
+// scratch element before reading it).  Calls whose kernels overlap on the GPU
+// (two streams, two threads) race on the array.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
 
-#include <mutex>
 #include <string>
 
 #include "../../include/gbdpcg.h"
@@ -34,6 +39,7 @@
 
 namespace gbdpcg {
 void set_last_error(const std::string &msg);
+int check_config(const gbdpcg_config *cfg, uint32_t layout);
 }
 
 namespace {
@@ -45,42 +51,29 @@ constexpr size_t kNoAllocScratchBytes =
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void *g_scratch_ptr[kMaxDevices] = {};
-int g_sm_count[kMaxDevices] = {};
-int g_smem_optin[kMaxDevices] = {};
-
 int noalloc_fail(int code, const std::string &msg) {
     gbdpcg::set_last_error(msg);  // read back with gbdpcg_last_error()
     return code;
 }
 
-// Device address of the scratch array and device limits, looked up once per
-// device with that device current.
+// Device address of the scratch array on the current device, and that
+// device's limits.  Looked up on every call: nothing is cached across calls.
 int scratch_for_current_device(void **ptr, int *sm_count, int *smem_optin) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return noalloc_fail(GBDPCG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(GBDPCG_ERR_UNSUPPORTED, "device index too large");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            return noalloc_fail(GBDPCG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        int sms = 0, optin = 0;
-        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (e != cudaSuccess)
-            return noalloc_fail(GBDPCG_ERR_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
-        g_sm_count[dev] = sms;
-        g_smem_optin[dev] = optin;
-        g_scratch_ptr[dev] = p;
-    }
-    *ptr = g_scratch_ptr[dev];
-    *sm_count = g_sm_count[dev];
-    *smem_optin = g_smem_optin[dev];
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return noalloc_fail(GBDPCG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    int sms = 0, optin = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess)
+        return noalloc_fail(GBDPCG_ERR_CUDA, std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
+    *ptr = p;
+    *sm_count = sms;
+    *smem_optin = optin;
     return GBDPCG_SUCCESS;
 }
 
@@ -101,11 +94,12 @@ int gbdpcg_solve_plain_noalloc_f32(const float *d_S, const float *d_Pinv, const 
                                 " exceed the allocation-free limits n*N <= " +
                                 std::to_string(kNoAllocMaxVec) + ", N <= " +
                                 std::to_string(kNoAllocMaxKnots));
-    if (cfg->exit_mode > GBDPCG_EXIT_RELRES || !(cfg->exit_tol >= 0))
-        return noalloc_fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad config field");
+    // the checks of the handle entry points (cbtd Phi^-1, as the plain algorithm reads it)
+    int rc = gbdpcg::check_config(cfg, GBDPCG_PINV_CBTD);
+    if (rc) return rc;
     void *scratch = nullptr;
     int sm_count = 0, smem_optin = 0;
-    int rc = scratch_for_current_device(&scratch, &sm_count, &smem_optin);
+    rc = scratch_for_current_device(&scratch, &sm_count, &smem_optin);
     if (rc) return rc;
     cudaStream_t stream = (cudaStream_t)stream_;
     char *base = static_cast<char *>(scratch);

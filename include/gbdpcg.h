@@ -55,7 +55,10 @@ typedef enum {
     GBDPCG_ERR_UNSUPPORTED = 2,      /* size or option combination not supported */
     GBDPCG_ERR_CUDA = 3,             /* a CUDA call failed; see gbdpcg_last_error() */
     GBDPCG_ERR_NO_MEMORY = 4,
-    GBDPCG_ERR_NOT_CONVERGED = 5     /* returned by nothing but gbdpcg_status_string() knows it */
+    GBDPCG_ERR_NOT_CONVERGED = 5     /* a solve ended without meeting its exit test; the C ABI
+                                        reports that per system (gbdpcg_result.status) and the
+                                        C++ drop-in (gpu_pcg.cuh) raises this code for it when
+                                        built with GBDPCG_ERROR_ON_MAX_ITER */
 } gbdpcg_status;
 
 /* ---- per-system outcome (gbdpcg_result.status) ---- */
@@ -208,13 +211,18 @@ GBDPCG_API int gbdpcg_last_result(gbdpcg_handle_t h, gbdpcg_result *result);
  * unbounded time; a process whose device memory another allocator already
  * owns; deployments that forbid allocation after start-up.  It runs the plain
  * algorithm (one CTA per knot, the reference's arithmetic order; cbtd Pinv)
- * with its scratch in one array of about 1 MiB compiled into the library,
- * which every GPU that loads the library reserves until the process exits.
- * Limits: n*N <= GBDPCG_NOALLOC_MAX_ELEMS and N <= GBDPCG_NOALLOC_MAX_KNOTS,
- * else GBDPCG_ERR_UNSUPPORTED.  No handle, no cudaMalloc/cudaFree.  The first
- * call on a device looks up the array's device address (cudaGetSymbolAddress)
- * with that device current; make it before any stream capture.  Calls share
- * the array: calls that overlap on the GPU race.  If `result` is non-NULL the
+ * with its scratch in one array of about 1 MiB compiled into the library's
+ * device code.  CUDA loads that code into a device lazily, so the first call
+ * on each device is what loads it and reserves the array there, and that call
+ * can fail for want of device memory: make it at start-up, as a warm-up,
+ * before other allocators take the memory and before any stream capture.
+ * From then on the device holds the array until the process exits.  Every
+ * call looks up the array's device address (cudaGetSymbolAddress, no
+ * allocation) with the calling device current.  Limits: n*N <=
+ * GBDPCG_NOALLOC_MAX_ELEMS and N <= GBDPCG_NOALLOC_MAX_KNOTS, else
+ * GBDPCG_ERR_UNSUPPORTED.  The config is checked like the handle entry
+ * points' configs.  No handle, no cudaMalloc/cudaFree.  Calls share the
+ * array: calls that overlap on the GPU race.  If `result` is non-NULL the
  * call waits for the stream and fills it. */
 #define GBDPCG_NOALLOC_MAX_ELEMS 131072
 #define GBDPCG_NOALLOC_MAX_KNOTS 4096

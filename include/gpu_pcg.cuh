@@ -35,6 +35,11 @@
 // Errors print "GPUassert: <message>" and exit with the status code, as
 // gpuErrchk does (include/gpuassert.cuh:10); define GBDPCG_THROW_ON_ERROR to
 // throw std::runtime_error instead.
+// A solve that stops without meeting its exit test (pcg_max_iter passes, or a
+// non-finite p.Sp / r.z) returns its iteration count, as the reference does
+// (include/pcg.cuh:212 records d_max_iter_exit and nothing reads it); define
+// GBDPCG_ERROR_ON_MAX_ITER to treat it as the error GBDPCG_ERR_NOT_CONVERGED
+// instead (printed and exited, or thrown, like any other error).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -85,13 +90,17 @@ struct pcg_config {
 
 inline void gpuAssert(int code, const char *file, int line, bool abort = true) {
     if (code != GBDPCG_SUCCESS) {
+        // the library records a message for its own failures; a solve that did
+        // not converge is reported by this header, not by a failed call
+        const char *detail = code == GBDPCG_ERR_NOT_CONVERGED
+                                 ? "the solve stopped without meeting its exit test"
+                                 : gbdpcg_last_error();
 #ifdef GBDPCG_THROW_ON_ERROR
         (void)abort;
         throw std::runtime_error(std::string("GPUassert: ") + gbdpcg_status_string(code) + ": " +
-                                 gbdpcg_last_error() + " " + file + " " + std::to_string(line));
+                                 detail + " " + file + " " + std::to_string(line));
 #else
-        fprintf(stderr, "GPUassert: %s: %s %s %d\n", gbdpcg_status_string(code), gbdpcg_last_error(),
-                file, line);
+        fprintf(stderr, "GPUassert: %s: %s %s %d\n", gbdpcg_status_string(code), detail, file, line);
         if (abort) exit(code);
 #endif
     }
@@ -116,6 +125,17 @@ inline gbdpcg_config to_config(const pcg_config<T> *c) {
         g.max_iter = c->pcg_max_iter;
     }
     return g;
+}
+
+// GBDPCG_ERR_NOT_CONVERGED for a solve that ended without meeting its exit
+// test, when the caller asked for that (GBDPCG_ERROR_ON_MAX_ITER).
+inline int convergence_status(const gbdpcg_result &res) {
+#ifdef GBDPCG_ERROR_ON_MAX_ITER
+    return res.status == GBDPCG_CONVERGED ? GBDPCG_SUCCESS : GBDPCG_ERR_NOT_CONVERGED;
+#else
+    (void)res;
+    return GBDPCG_SUCCESS;
+#endif
 }
 
 inline gbdpcg_handle_t thread_handle() {
@@ -146,6 +166,7 @@ uint32_t solvePCG(T *h_S, T *h_Pinv, T *h_gamma, T *h_lambda, unsigned stateSize
     else
         rc = gbdpcg_solve_f64(h_S, h_Pinv, h_gamma, h_lambda, stateSize, knotPoints, &cfg, &res);
     gpuErrchk(rc);
+    gpuErrchk(gbdpcg_detail::convergence_status(res));
     return res.iters;
 }
 
@@ -168,6 +189,7 @@ uint32_t solvePCG(const uint32_t state_size, const uint32_t knot_points, T *d_S,
         rc = gbdpcg_solve_dev_f64(h, d_S, d_Pinv, GBDPCG_PINV_CBTD, d_gamma, d_lambda, state_size,
                                   knot_points, &cfg, &res, nullptr);
     gpuErrchk(rc);
+    gpuErrchk(gbdpcg_detail::convergence_status(res));
     return res.iters;
 }
 

@@ -4,8 +4,9 @@
   oracle/_build/libref_launcher.so   nvcc, from oracle/ref_launcher.cu (host code)
   oracle/_ref/ref_pcg_{f32,f64}.cubin
       nvcc, device-only, from oracle/ref_kernels.cu, which includes the
-      reference's include/pcg.cuh from the reference checkout; built only where
-      that checkout exists (the cubins are architecture-neutral on the host side
+      reference's include/pcg.cuh from the reference checkout (directory
+      GBDPCG_REFERENCE_DIR, else `reference` beside this repository); built
+      only where that checkout exists (the cubins are architecture-neutral on the host side
       and are carried to machines that have no checkout).
 
 Usage: python oracle/build_oracle.py [--force]
@@ -21,7 +22,11 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_INCLUDE = "/root/reference/include"
+# the reference checkout: GBDPCG_REFERENCE_DIR, else a `reference` directory
+# beside this repository's root
+REFERENCE_DIR = os.environ.get("GBDPCG_REFERENCE_DIR") or os.path.join(
+    os.path.dirname(os.path.dirname(HERE)), "reference")
+REFERENCE_INCLUDE = os.path.join(REFERENCE_DIR, "include")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

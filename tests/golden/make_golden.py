@@ -23,7 +23,10 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-EXAMPLE = "/root/reference/examples/pcg_solve.cu"
+# the reference checkout: GBDPCG_REFERENCE_DIR, else a `reference` directory
+# beside this repository's root
+REFERENCE_DIR = os.environ.get("GBDPCG_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT), "reference")
+EXAMPLE = os.path.join(REFERENCE_DIR, "examples", "pcg_solve.cu")
 
 
 def _array(src: str, name: str) -> list[float]:
@@ -49,6 +52,10 @@ REF_CASES = [("f32", 14, 32, 0, 200, 1e-6), ("f32", 14, 128, 0, 200, 1e-6), ("f3
              ("f32", 6, 64, 2, 200, 1e-6), ("f32", 12, 64, 3, 200, 1e-6),
              ("f32", 24, 128, 4, 200, 1e-6), ("f32", 3, 5, 5, 50, 1e-6),
              ("f32", 5, 2, 6, 50, 1e-6), ("f64", 3, 5, 7, 50, 1e-12)]
+# the larger single system n = 14, N = 128 on seeds 1..9 (seed 0 is above),
+# FP32 to 1e-6 and FP64 to 1e-12
+REF_CASES += [(dts, 14, 128, seed, 200, tol) for dts, tol in (("f32", 1e-6), ("f64", 1e-12))
+              for seed in range(1, 10)]
 
 
 def make_ref_outputs(path: str) -> None:

@@ -89,3 +89,24 @@ def test_adapters_and_kkt_reject_bad_arguments(gb):
     assert L.gbdpcg_form_schur_pinv_f32(*args7, 2, 1, 3, p, p, None, None) == INV
     assert L.gbdpcg_kkt_backsub_f32(*([p] * 6 + [None]), 2, 1, 3, p, p, None) == INV
     assert L.gbdpcg_kkt_backsub_f64(*args7, 0, 1, 3, p, p, None) == INV
+
+
+def test_noalloc_checks_like_the_handle_entry_points(gb):
+    """The allocation-free solve rejects the configs the handle entry points
+    reject, with the same status, before any CUDA call (host pointers below,
+    never dereferenced), and checks its size limits first."""
+    L = gb.lib()
+    r = gb.Result()
+    a = np.zeros(36, np.float32)
+    p = a.ctypes.data_as(ctypes.c_void_p)
+    for bad in (gb.config(zero_guess=2), gb.config(exit_mode=7), gb.config(algorithm=9),
+                gb.config(exit_tol=-1.0), gb.config(cluster_size=17), gb.config(inner_tol=1.5)):
+        rc_noalloc = L.gbdpcg_solve_plain_noalloc_f32(p, p, p, p, 2, 3, ctypes.byref(bad), ctypes.byref(r), None)
+        rc_handle = L.gbdpcg_solve_f32(p, p, p, p, 2, 3, ctypes.byref(bad), ctypes.byref(r))
+        assert rc_noalloc == rc_handle == gb.ERR_INVALID_ARGUMENT
+    # n*N beyond the scratch array (N itself within its limit), and N beyond it
+    good = gb.config()
+    for n, N in ((64, 2049), (1, 4097)):
+        assert L.gbdpcg_solve_plain_noalloc_f32(p, p, p, p, n, N, ctypes.byref(good), ctypes.byref(r),
+                                                None) == gb.ERR_UNSUPPORTED
+        assert "allocation-free limits" in gb.last_error()

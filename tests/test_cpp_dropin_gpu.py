@@ -96,3 +96,25 @@ def test_csr_overload_through_cpp_interface(exe, oracle_mod, handle, tmp_path, d
     it_c, lam_c = _run(exe, tmp_path, n, N, S, P, g, 200, tol)
     it_r, lam_r = _run(exe, tmp_path, n, N, S, P, g, 200, tol, csr=True)
     assert it_r == it_c and lam_r.tobytes() == lam_c.tobytes()
+
+
+@pytest.mark.gpu
+def test_not_converged_is_an_error_when_asked(gb, oracle_mod, handle, tmp_path):
+    """Built with GBDPCG_ERROR_ON_MAX_ITER, a drop-in solve that stops at
+    pcg_max_iter is the error GBDPCG_ERR_NOT_CONVERGED (printed, exit code 5,
+    like gpuErrchk); without it the iteration count is returned as the
+    reference returns it."""
+    O = oracle_mod
+    strict = _compile(gb, str(tmp_path / "dropin_strict"), ["-DGBDPCG_ERROR_ON_MAX_ITER"])
+    n, N = 14, 32
+    sy = O.generate(n, N, 0)
+    S, P, g = sy.cbtd(np.float32), O.block_jacobi(sy.D).astype(np.float32), sy.gamma.astype(np.float32)
+    path = str(tmp_path / "in.bin")
+    with open(path, "wb") as f:
+        f.write(np.array([n, N, 4, 1], np.uint32).tobytes())
+        for a in (S, P, g, np.zeros(n * N, np.float32)):
+            f.write(a.tobytes())
+    r = subprocess.run([strict, path, "2", "1e-6"], capture_output=True, text=True)
+    assert r.returncode == 5 and "not converged" in r.stderr, (r.returncode, r.stderr)
+    r = subprocess.run([strict, path, "200", "1e-6"], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.startswith("iters "), r.stderr

@@ -106,6 +106,33 @@ def test_vs_rebuilt_reference_kernel(gb, oracle_mod, handle, dts, n, N, seed):
     assert relerr(lam, lam_r) < (F64_TOL if dts == "f64" else F32_TOL)
 
 
+# the larger single system: n = 14, N = 128, seeds 0-9, FP32 to 1e-6 and FP64 to 1e-12
+CONFIG_N128 = [(dts, 14, 128, seed) for dts in ("f32", "f64") for seed in range(10)]
+
+
+@pytest.mark.parametrize("dts,n,N,seed", CONFIG_N128)
+def test_n128_seeds_vs_rebuilt_reference_kernel(gb, oracle_mod, handle, dts, n, N, seed):
+    """n = 14, N = 128 on seeds 0-9: the reference kernel rebuilt for sm_103a
+    equals the oracle bit for bit; the plain kernel equals both bit for bit;
+    the cluster solver (the drop-in's default, host arrays) takes the
+    reference's passes with lambda within 1e-5 (FP32) / 1e-12 (FP64)."""
+    O = oracle_mod
+    if not O.have_ref_kernel(dts, n, N):
+        pytest.skip("reference kernel not built at this size")
+    dt = _dt(dts)
+    _, S, P, g = system(O, n, N, seed, dt)
+    lam_r, it_r, mie_r, _ = O.ref_kernel_solve(S, P, g, np.zeros(n * N, dt), n, N, 200, _tol(dts))
+    lam_o, it_o, mie_o = O.ref_pcg(S, P, g, np.zeros(n * N, dt), n, N, 200, _tol(dts))
+    assert lam_r.tobytes() == lam_o.tobytes() and it_r == it_o and mie_r == mie_o == 0
+    lam_p = np.zeros(n * N, dt)
+    rp = gb.solve(S, P, g, lam_p, n, N, gb.config(algorithm=gb.ALGO_PLAIN, max_iter=200, exit_tol=_tol(dts)))
+    assert rp.iters == it_r and lam_p.tobytes() == lam_r.tobytes()
+    lam = np.zeros(n * N, dt)
+    r = gb.solve(S, P, g, lam, n, N, gb.config(max_iter=200, exit_tol=_tol(dts)))
+    assert r.status == gb.CONVERGED and r.iters == it_r, (r.iters, it_r)
+    assert relerr(lam, lam_r) < (F64_TOL if dts == "f64" else F32_TOL)
+
+
 @pytest.mark.parametrize("C", [1, 2, 3, 4, 5, 8, 16])
 def test_cluster_sizes_agree(gb, oracle_mod, handle, C):
     import torch

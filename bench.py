@@ -30,9 +30,14 @@ Printed JSON line (rank 0):
   around_solve  Schur formation (alone and with the fused Phi^-1), KKT
              back-substitution and CSR -> cbtd on one long horizon
   block_jacobi  the Phi^-1 build over the batch
+  timeline   one execution's per-system timeline (staging share, us per
+             iteration and idle tails per launch class, busy SMs over the
+             step) and the latency floor of the dominant class and of one
+             n = 14, N = 32 system; roofline.latency repeats the floors
 --impl reference: times the reference's CPU path on the host cores — the
 reference ships none, so the oracle's C port of its PCG (all host threads).
---only around-solve | block-jacobi | single-system-n128: that section alone.
+--only around-solve | block-jacobi | single-system | single-system-n128 | timeline:
+that section alone.
 """
 from __future__ import annotations
 
@@ -66,7 +71,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--no-extras", action="store_true", help="skip the baselines and the other configurations")
-    ap.add_argument("--only", default=None, choices=["around-solve", "block-jacobi", "single-system-n128"],
+    ap.add_argument("--only", default=None, choices=["around-solve", "block-jacobi", "single-system",
+                                                     "single-system-n128", "timeline"],
                     help="time one section alone and print its JSON (profiling): the kernels either side of "
                          "the solve, the block-Jacobi build over the batch, or the n = 14, N = 128 seeds "
                          "beside the rebuilt reference kernel")
@@ -371,6 +377,135 @@ def n128_seed_sweep(gbdpcg, h, dev, reps=20, seeds=range(10)):
     return out
 
 
+def timeline_summary(stamps, cta_sm, launches, sm_count):
+    """Reads one execution's timeline (gbdpcg_plan_timeline_read): per launch
+    class, the share of each system's time spent staging its rows, the us per
+    PCG iteration, and how long the class's clusters sat idle after the
+    class's last system started; over the step, the fraction of SM-time with
+    no CTA of the solver resident and busy, and the step's tail (from the last
+    moment 90% of the SMs were busy to the end)."""
+    ok = stamps["iters"] > 0
+    st = stamps[ok]
+    t0 = int(st["t_pop"].min())
+    t_end = int(st["t_done"].max())
+    T = t_end - t0
+    cta_base = np.concatenate([[0], np.cumsum([l["ctas"] for l in launches if l["cluster"] > 0])])
+    classes = []
+    for c, l in enumerate(launches):
+        if l["cluster"] == 0:
+            continue
+        m = st["launch"] == c
+        if not m.any():
+            continue
+        s = st[m]
+        busy = (s["t_done"] - s["t_pop"]).astype(np.float64)
+        stage = (s["t_staged"] - s["t_pop"]).astype(np.float64)
+        per_iter = (s["t_solved"] - s["t_staged"]).astype(np.float64) / s["iters"]
+        c_end = int(s["t_done"].max())
+        last_done = {}
+        for rec in s:
+            last_done[int(rec["cluster"])] = max(last_done.get(int(rec["cluster"]), 0), int(rec["t_done"]))
+        idle_cta_ns = sum(c_end - v for v in last_done.values()) * l["cluster"]
+        classes.append({"launch": c, "cluster": l["cluster"], "threads": l["threads"], "storage": l["storage"],
+                        "rows_per_thread": l["rows_per_thread"], "algorithm": l["algorithm"],
+                        "systems": int(m.sum()), "cta_busy_ms": float(busy.sum() * l["cluster"] / 1e6),
+                        "staging_share": float(stage.sum() / busy.sum()),
+                        "us_per_iteration_median": float(np.median(per_iter) / 1e3),
+                        "start_ms": (int(s["t_pop"].min()) - t0) / 1e6, "end_ms": (c_end - t0) / 1e6,
+                        "tail_idle_cta_ms": idle_cta_ns / 1e6})
+    # busy SMs over the step: an SM is busy while a CTA of a cluster is solving a system
+    ev = []
+    for rec in st:
+        base = int(cta_base[rec["launch"]]) + int(rec["cluster"]) * launches[rec["launch"]]["cluster"]
+        sms = set(int(x) for x in cta_sm[base:base + launches[rec["launch"]]["cluster"]])
+        ev.append((int(rec["t_pop"]), 1, sms))
+        ev.append((int(rec["t_done"]), -1, sms))
+    ev.sort(key=lambda e: (e[0], e[1]))
+    act = np.zeros(max(sm_count, int(cta_sm.max()) + 1 if cta_sm.size else sm_count), np.int64)
+    busy_sm_ns, nbusy, last_t = 0.0, 0, t0
+    last_full = t0
+    for t, d, sms in ev:
+        busy_sm_ns += nbusy * (t - last_t)
+        if nbusy >= 0.9 * sm_count:
+            last_full = t
+        last_t = t
+        for x in sms:
+            if d > 0:
+                act[x] += 1
+                if act[x] == 1:
+                    nbusy += 1
+            else:
+                act[x] -= 1
+                if act[x] == 0:
+                    nbusy -= 1
+    classes.sort(key=lambda r: -r["cta_busy_ms"])
+    return {"step_ms": T / 1e6, "sm_busy_frac": busy_sm_ns / (sm_count * T), "tail_ms": (t_end - last_full) / 1e6,
+            "tail_share": (t_end - last_full) / T,
+            "staging_share": float(((st["t_staged"] - st["t_pop"]).sum()) / (st["t_done"] - st["t_pop"]).sum()),
+            "classes": classes}
+
+
+def latency_floor(gbdpcg, cls, grid_clusters, dev_index=0, reps=100000):
+    """The floor that the synchronisation primitives put under one PCG
+    iteration of a launch shape: two cluster-wide reductions (1 and 2 values)
+    and two CTA barriers (standard form) or one (recurrence form), each
+    measured by gbdpcg_probe_primitives on the shape (cluster size, CTA size)
+    with all the shape's clusters running at once; frac = floor / achieved."""
+    C, thr = cls["cluster"], cls["threads"]
+    under_load = gbdpcg.probe_primitives(dev_index, C, thr, grid_clusters, reps)
+    alone = gbdpcg.probe_primitives(dev_index, C, thr, 1, reps)
+    rec = cls["algorithm"] == gbdpcg.ALGO_RECURRENCE
+    barriers = 1 if rec else 2
+    floor = under_load["allreduce_ns"][0] + under_load["allreduce_ns"][1] + barriers * under_load["syncthreads_ns"]
+    ach = cls["us_per_iteration_median"] * 1e3
+    return {"shape": {"cluster": C, "threads": thr, "storage": cls["storage"], "algorithm": cls["algorithm"],
+                      "clusters_at_once": grid_clusters},
+            "model": f"allreduce(1) + allreduce(2) + {barriers} x __syncthreads per iteration",
+            "floor_us_per_iter": floor / 1e3, "achieved_us_per_iter": ach / 1e3, "frac": floor / ach,
+            "primitives_under_load_ns": under_load, "primitives_alone_ns": alone}
+
+
+def timeline_and_floor(gbdpcg, h, plan, launches, dev, sm_count):
+    """Timeline of one execution of the benchmark plan, and the latency floor
+    of its dominant class and of one n = 14, N = 32 system (its own plan)."""
+    import torch
+    from gbdpcg.workload import generate
+    plan.timeline(True)
+    plan.execute()
+    plan.execute()
+    stamps, sms = plan.timeline_read()
+    plan.timeline(False)
+    summ = timeline_summary(stamps, sms, launches, sm_count)
+    dom = summ["classes"][0]
+    out = {"timeline": summ,
+           "latency": {"dominant_class": latency_floor(gbdpcg, dom, launches[dom["launch"]]["ctas"] // dom["cluster"])}}
+    # one n = 14, N = 32 system alone (FP32, tol 1e-6, reference exit test, seed 0)
+    n, N = 14, 32
+    sy = generate(n, N, 0)
+    S = torch.from_numpy(sy.cbtd(np.float32)).to(dev)
+    g = torch.from_numpy(sy.gamma.astype(np.float32)).to(dev)
+    P = torch.empty(n * n * N, device=dev)
+    h.block_jacobi(S, P, n, N, gbdpcg.PINV_BLOCKDIAG)
+    lam = torch.zeros(n * N, device=dev)
+    for algo, key in ((gbdpcg.ALGO_CLUSTER, "n14_N32_standard"), (gbdpcg.ALGO_RECURRENCE, "n14_N32_recurrence")):
+        cfg = gbdpcg.config(max_iter=200, exit_tol=1e-6, algorithm=algo, zero_guess=1, cluster_size=1)
+        p1 = gbdpcg.Plan(h, [{"S": S, "Pinv": P, "gamma": g, "lambda": lam, "n": n, "N": N}],
+                         gbdpcg.PINV_BLOCKDIAG, cfg)
+        l1 = p1.launches()
+        p1.timeline(True)
+        times = []
+        for _ in range(5):
+            p1.execute()
+            s1, m1 = p1.timeline_read()
+            times.append(s1)
+        s1 = min(times, key=lambda x: int(x["t_solved"][0] - x["t_staged"][0]))
+        cls = dict(l1[0], launch=0, us_per_iteration_median=float(s1["t_solved"][0] - s1["t_staged"][0]) / 1e3
+                   / int(s1["iters"][0]))
+        out["latency"][key] = latency_floor(gbdpcg, cls, 1)
+        p1.close()
+    return out
+
+
 def adjoint_config(gbdpcg, h, dev, tune_flags=None, count=1024, n=14, N=64):
     """Forward + adjoint cost: batch 1024, n=14, N=64, FP32, L = 1/2 ||lambda - lambda*||^2.
     With tune_flags, both plans are autotuned alike (None: neither)."""
@@ -651,6 +786,11 @@ def main():
     if args.only == "around-solve":
         print(json.dumps({"around_solve": around_solve_kernels(gbdpcg, dev, hbm, N=args.knots)}), flush=True)
         return
+    if args.only == "single-system":
+        h1 = gbdpcg.Handle(local)
+        print(json.dumps({"single_system": single_system_latency(gbdpcg, h1, dev)}), flush=True)
+        h1.close()
+        return
     if args.only == "single-system-n128":
         h1 = gbdpcg.Handle(local)
         print(json.dumps({"single_system_n128": n128_seed_sweep(gbdpcg, h1, dev)}), flush=True)
@@ -684,7 +824,13 @@ def main():
         plan.autotune(flags=tune_flags)
         tune_s = time.perf_counter() - t0
     launches = plan.launches()
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
     stream = torch.cuda.current_stream()
+    if args.only == "timeline":
+        for _ in range(3):
+            plan.execute()
+        print(json.dumps({"timeline": timeline_and_floor(gbdpcg, h, plan, launches, dev, sm_count)}), flush=True)
+        return
     for _ in range(max(3, args.warmup)):
         plan.execute()
     res = plan.results()
@@ -854,11 +1000,19 @@ def main():
                         ("adjoint", lambda: adjoint_config(gbdpcg, h, dev, tune_flags)),
                         ("precision", lambda: precision_config(gbdpcg, h, dev)),
                         ("around_solve", lambda: around_solve_kernels(gbdpcg, dev, hbm)),
-                        ("block_jacobi", lambda: block_jacobi_build(plan, descs, hbm))):
+                        ("block_jacobi", lambda: block_jacobi_build(plan, descs, hbm)),
+                        ("timeline", lambda: timeline_and_floor(gbdpcg, h, plan, launches, dev, sm_count))):
             try:
                 line[key] = fn()
             except Exception as e:  # report, do not lose the headline line
                 line[key] = {"error": repr(e)}
+        lat = line.get("timeline", {}).get("latency")
+        if lat:
+            # the bound that binds: per-iteration latency against the floor the
+            # synchronisation primitives put under an iteration
+            line["roofline"]["latency"] = {
+                k: {"floor_us_per_iter": v["floor_us_per_iter"], "achieved_us_per_iter": v["achieved_us_per_iter"],
+                    "frac": v["frac"], "shape": v["shape"]} for k, v in lat.items()}
     print(json.dumps(line), flush=True)
     plan.close()
     h.close()

@@ -561,6 +561,11 @@ struct gbdpcg_plan_s {
     cudaStream_t build_stream = nullptr;  // highest priority: the Phi^-1 builds of solve_host
     std::vector<cudaStream_t> piece_streams;
     std::vector<cudaEvent_t> piece_events;  // [copied i], [solved i], start, [built i]
+    // timeline (gbdpcg_plan_timeline): one record per work-list item, and the
+    // SM of every CTA of every launch (launch c's CTAs from cta_off[c])
+    bool timeline = false;
+    DevBuf d_stamps, d_ctasm;
+    std::vector<uint32_t> cta_off;
     ~gbdpcg_plan_s() {
         for (auto &pc : pieces) delete pc.plan;
         if (copy_stream) cudaStreamDestroy(copy_stream);
@@ -590,6 +595,8 @@ TuneKey tune_key(const gbdpcg_plan_s *p, bool adjoint, uint32_t n, uint32_t N) {
     k.N = N;
     return k;
 }
+
+int timeline_buffers(gbdpcg_plan_s *p);
 
 // Merges classes with the same launch shape, orders each class's systems
 // longest first and the classes by their largest system, builds the device
@@ -637,10 +644,27 @@ int plan_layout(gbdpcg_plan_s *p) {
     if (!order.empty())
         GB_CUDA(cudaMemcpy(p->d_order.p, order.data(), sizeof(uint32_t) * order.size(),
                            cudaMemcpyHostToDevice));
+    if (p->timeline && (rc = timeline_buffers(p))) return rc;
     if (p->gexec) cudaGraphExecDestroy(p->gexec);
     if (p->graph) cudaGraphDestroy(p->graph);
     p->gexec = nullptr;
     p->graph = nullptr;
+    return GBDPCG_SUCCESS;
+}
+
+// Sizes the timeline buffers to the current launch classes (called whenever
+// the layout changes while the timeline is on, never during a capture).
+int timeline_buffers(gbdpcg_plan_s *p) {
+    p->cta_off.assign(p->classes.size() + 1, 0);
+    size_t items = 0;
+    for (size_t c = 0; c < p->classes.size(); ++c) {
+        items += p->classes[c].items.size();
+        p->cta_off[c + 1] = p->cta_off[c] + p->classes[c].grid_clusters * p->classes[c].sh.C;
+    }
+    int rc;
+    if ((rc = p->d_stamps.ensure(sizeof(StampRec) * std::max<size_t>(1, items)))) return rc;
+    if ((rc = p->d_ctasm.ensure(sizeof(uint32_t) * std::max<size_t>(1, p->cta_off.back())))) return rc;
+    GB_CUDA(cudaMemset(p->d_stamps.p, 0, sizeof(StampRec) * std::max<size_t>(1, items)));
     return GBDPCG_SUCCESS;
 }
 
@@ -661,6 +685,11 @@ int plan_enqueue(gbdpcg_plan_s *p, cudaStream_t stream) {
         lp.kmax = pc.kmax;
         lp.queue = p->d_queues.as<uint32_t>() + c;
         lp.results = p->d_results.as<SysResult>();
+        lp.launch_id = c;
+        if (p->timeline) {
+            lp.stamps = p->d_stamps.as<StampRec>() + pc.order_off;
+            lp.cta_sm = p->d_ctasm.as<uint32_t>() + p->cta_off[c];
+        }
         int rc = launch_cluster(pc.sh, lp, pc.grid_clusters, s);
         if (rc) return rc;
     }
@@ -1396,6 +1425,49 @@ int gbdpcg_plan_launch_kernel(gbdpcg_plan_t p, uint32_t i, uint32_t *storage, ui
     if (storage) *storage = 2;
     if (rows_per_thread) *rows_per_thread = 1;
     if (algorithm) *algorithm = GBDPCG_ALGO_PLAIN;
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_timeline(gbdpcg_plan_t p, int enable) {
+    if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (enable != 0 && enable != 1) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "enable must be 0 or 1");
+    HandleScope scope(p->h->device);
+    if ((bool)enable == p->timeline) return GBDPCG_SUCCESS;
+    p->timeline = enable != 0;
+    if (p->timeline) {
+        int rc = timeline_buffers(p);
+        if (rc) {
+            p->timeline = false;
+            return rc;
+        }
+    }
+    // the launches carry the timeline pointers: capture them again
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    p->gexec = nullptr;
+    p->graph = nullptr;
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_plan_timeline_read(gbdpcg_plan_t p, gbdpcg_stamp *stamps, uint32_t capacity, uint32_t *count,
+                              uint32_t *cta_sm, uint32_t sm_capacity, uint32_t *sm_count,
+                              gbdpcg_stream_t stream) {
+    static_assert(sizeof(gbdpcg_stamp) == sizeof(StampRec), "gbdpcg_stamp mirrors StampRec");
+    if (!p || !count || !sm_count) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (!p->timeline) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "the plan's timeline is off");
+    HandleScope scope(p->h->device);
+    size_t items = 0;
+    for (const auto &pc : p->classes) items += pc.items.size();
+    const uint32_t ctas = p->cta_off.empty() ? 0 : p->cta_off.back();
+    *count = (uint32_t)items;
+    *sm_count = ctas;
+    GB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    if (stamps && capacity)
+        GB_CUDA(cudaMemcpy(stamps, p->d_stamps.p, sizeof(StampRec) * std::min<size_t>(capacity, items),
+                           cudaMemcpyDeviceToHost));
+    if (cta_sm && sm_capacity && ctas)
+        GB_CUDA(cudaMemcpy(cta_sm, p->d_ctasm.p, sizeof(uint32_t) * std::min<uint32_t>(sm_capacity, ctas),
+                           cudaMemcpyDeviceToHost));
     return GBDPCG_SUCCESS;
 }
 

@@ -511,6 +511,55 @@ __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, A *wscr,
     for (int q = 0; q < NQ; ++q) v[q] = acc_normalize(v[q]);
 }
 
+// Timeline of a launch (LaunchParams::stamps): the GPU's global nanosecond
+// clock, read by the cluster's leading thread at four points of each system.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ uint32_t sm_id() {
+    uint32_t s;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(s));
+    return s;
+}
+
+struct Stamper {
+    bool on;
+    uint64_t t_pop = 0, t_staged = 0, t_solved = 0;
+    __device__ Stamper(const LaunchParams &lp, uint32_t rank)
+        : on(lp.stamps != nullptr && rank == 0 && threadIdx.x == 0) {
+        if (lp.cta_sm && threadIdx.x == 0) lp.cta_sm[blockIdx.x] = sm_id();
+    }
+    __device__ __forceinline__ void pop() {
+        if (on) t_pop = global_ns();
+    }
+    __device__ __forceinline__ void staged() {
+        if (on) t_staged = global_ns();
+    }
+    __device__ __forceinline__ void solved() {
+        if (on) t_solved = global_ns();
+    }
+    // a rejected system: every time equal, no iterations
+    __device__ __forceinline__ void rejected() {
+        t_staged = t_solved = t_pop;
+    }
+    __device__ __forceinline__ void done(const LaunchParams &lp, uint32_t item, uint32_t iters) {
+        if (!on) return;
+        StampRec rec;
+        rec.t_pop = t_pop;
+        rec.t_staged = t_staged;
+        rec.t_solved = t_solved;
+        rec.t_done = global_ns();
+        rec.system = lp.order ? lp.order[item] : item;
+        rec.launch = lp.launch_id;
+        rec.cluster = blockIdx.x / cg::this_cluster().num_blocks();
+        rec.iters = iters;
+        lp.stamps[item] = rec;
+    }
+};
+
 __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uint32_t C) {
     if (C > 1)
         cluster.sync();
@@ -572,6 +621,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         trow = tbase + ((((tid >> 5) & 3u) * 32u) << 16) + (tid >> 7) * (uint32_t)(RPT * 3 * NPT);
     }
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
+    Stamper stamp(lp, rank);
     for (uint32_t pass = 0;; ++pass) {
         // ---- pull the next system (cluster leader pops, broadcasts by DSMEM)
         uint32_t item;
@@ -587,6 +637,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             __syncthreads();  // the previous system's epilogue has finished with shared memory
         }
         if (item >= lp.count) break;
+        stamp.pop();
         const SysDesc d = lp.descs ? lp.descs[lp.order ? lp.order[item] : item] : lp.one;
         const uint32_t n = d.n, N = d.N;
         const uint32_t K = (N + C - 1) / C;
@@ -597,6 +648,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 res.status = -1;
                 lp.results[d.result] = res;
             }
+            stamp.rejected();
+            stamp.done(lp, item, 0);
             group_sync(cluster, C);  // s_item is read by every CTA before the next pop
             continue;                // uniform: every CTA of the cluster sees the same descriptor
         }
@@ -756,6 +809,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         T *my_p = vp + (lk + 1) * NP + i;  // this thread's rows in the windows
         T *my_r = vr + (lk + 1) * NP + i;
         __syncthreads();
+        stamp.staged();
 
         // ---- r = gamma - S lambda0   (include/pcg.cuh:119-126)
         T gam[RPT], lam[RPT], r[RPT], p[RPT], z[RPT], y[RPT];
@@ -999,6 +1053,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         }
 
         // ---- outputs   (include/pcg.cuh:212-217)
+        stamp.solved();
         T *lam_out = static_cast<T *>(d.lambda);
         if (act) {
 #pragma unroll
@@ -1060,6 +1115,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 }
             }
         }
+        stamp.done(lp, item, iter);
     }
     if constexpr (S_TM) {  // every TMEM access of the CTA is done
         tmem_fence_before_sync();
@@ -1128,6 +1184,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
 
     for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
+    Stamper stamp(lp, rank);
     for (uint32_t pass = 0;; ++pass) {
         uint32_t item;
         if (lp.queue) {
@@ -1142,6 +1199,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
             __syncthreads();
         }
         if (item >= lp.count) break;
+        stamp.pop();
         const SysDesc d = lp.descs ? lp.descs[lp.order ? lp.order[item] : item] : lp.one;
         const uint32_t n = d.n, N = d.N;
         const uint32_t K = (N + C - 1) / C;
@@ -1152,6 +1210,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
                 res.status = -1;
                 lp.results[d.result] = res;
             }
+            stamp.rejected();
+            stamp.done(lp, item, 0);
             group_sync(cluster, C);
             continue;
         }
@@ -1231,6 +1291,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
         T *my_u = vu + (lk + 1) * NP + i;
         T *my_r = vr + (lk + 1) * NP + i;
         __syncthreads();
+        stamp.staged();
 
         // ---- r0 = gamma - S x0 (the u window holds x0 for this product)
         T gam[RPT], lam[RPT], r[RPT], u[RPT], w[RPT], p[RPT], s[RPT];
@@ -1398,6 +1459,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
             g = g_new;
         }
 
+        stamp.solved();
         T *lam_out = static_cast<T *>(d.lambda);
         if (act) {
 #pragma unroll
@@ -1414,6 +1476,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
             res.pad = 0;
             lp.results[d.result] = res;
         }
+        stamp.done(lp, item, iter);
     }
 }
 

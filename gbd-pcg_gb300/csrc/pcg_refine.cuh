@@ -63,6 +63,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
 
     for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(double)); e += nthr) slots64[e] = 0.0;
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
+    Stamper stamp(lp, rank);
     for (uint32_t pass = 0;; ++pass) {
         uint32_t item;
         if (lp.queue) {
@@ -77,6 +78,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
             __syncthreads();
         }
         if (item >= lp.count) break;
+        stamp.pop();
         const SysDesc d = lp.descs ? lp.descs[lp.order ? lp.order[item] : item] : lp.one;
         const uint32_t n = d.n, N = d.N;
         const uint32_t K = (N + C - 1) / C;
@@ -87,6 +89,8 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
                 res.status = -1;
                 lp.results[d.result] = res;
             }
+            stamp.rejected();
+            stamp.done(lp, item, 0);
             group_sync(cluster, C);
             continue;
         }
@@ -152,6 +156,8 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
         T *my_r = vr + (lk + 1) * NP + i;
         double *my_d = vd + (lk + 1) * NP + i;
 
+        __syncthreads();  // rows staged
+        stamp.staged();
         double gam[RPT], lam[RPT], r64[RPT];
 #pragma unroll
         for (int q = 0; q < RPT; ++q) {
@@ -343,6 +349,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
             for (int q = 0; q < RPT; ++q) lam[q] += (double)x[q];
         }
 
+        stamp.solved();
         double *lam_out = static_cast<double *>(d.lambda);
         if (act) {
 #pragma unroll
@@ -359,6 +366,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
             res.pad = 0;
             lp.results[d.result] = res;
         }
+        stamp.done(lp, item, iters);
     }
 }
 

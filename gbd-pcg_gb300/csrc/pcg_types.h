@@ -55,6 +55,20 @@ struct SysResult {
     uint32_t pad;
 };
 
+// Timeline record of one system in one launch (globaltimer nanoseconds),
+// written by the leading thread of the cluster that solved it when a launch
+// is given a stamp array.  Layout equals gbdpcg_stamp of gbdpcg.h.
+struct StampRec {
+    uint64_t t_pop;     // the cluster took the system from the work list
+    uint64_t t_staged;  // its rows are on chip (the leading CTA's view)
+    uint64_t t_solved;  // the PCG loop has ended
+    uint64_t t_done;    // outputs (and any epilogue) written
+    uint32_t system;    // index of the system in the plan
+    uint32_t launch;    // launch (class) index
+    uint32_t cluster;   // cluster index within the launch's grid
+    uint32_t iters;
+};
+
 // Launch-wide parameters of the persistent cluster kernel.
 struct LaunchParams {
     const SysDesc *descs;    // null: the single system `one` (passed by value)
@@ -64,6 +78,10 @@ struct LaunchParams {
     uint32_t *queue;         // work-queue head (zeroed before the launch); null: static
                              // round-robin of items over clusters
     SysResult *results;
+    StampRec *stamps;        // null: no timeline; else one record per work-list item
+    uint32_t *cta_sm;        // null, or the SM of every CTA of the grid (blockIdx.x order)
+    uint32_t launch_id;      // launch index written into the stamps
+    uint32_t pad_;
     SysDesc one;
 };
 

@@ -1,0 +1,168 @@
+// Latency of the synchronisation primitives one PCG iteration of the cluster
+// solver is built from (gbdpcg_probe_primitives): the CTA barrier, the
+// cluster barrier, a distributed-shared-memory store followed by the cluster
+// barrier, and cluster_allreduce of 1, 2 and 3 values — the reduction the
+// solver itself runs (pcg_cluster.cuh), on the same shared-memory slot layout.
+// Each probe kernel repeats one primitive `reps` times in a loop whose values
+// depend on the previous repetition (nothing can be hoisted or overlapped),
+// timed with CUDA events around the launch; the loop alone is measured the
+// same way and subtracted.  Every loop is bounded; no probe waits on a flag.
+// The iteration floor of the solver's forms is built from these numbers:
+// standard form 2 reductions + 2 CTA barriers, recurrence form 2 reductions +
+// 1 CTA barrier (the reference has 4 grid-wide barriers per iteration,
+// include/pcg.cuh:166,178,190,207).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <string>
+
+#include "../../include/gbdpcg.h"
+#include "pcg_cluster.cuh"
+
+namespace gbdpcg {
+void set_last_error(const std::string &msg);
+}
+
+namespace {
+
+using namespace gbdpcg;
+
+enum { PROBE_LOOP = 0, PROBE_SYNCTHREADS = 1, PROBE_CLUSTER = 2, PROBE_DSMEM = 3, PROBE_REDUCE = 4 };
+
+template <int KIND, int NQ>
+__global__ void probe_kernel(uint32_t reps, float *sink) {
+    const cg::cluster_group cluster = cg::this_cluster();
+    const uint32_t C = cluster.num_blocks(), rank = cluster.block_rank();
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const uint32_t nwarps = blockDim.x >> 5;
+    float *slots = reinterpret_cast<float *>(smem_raw);
+    float *wscr = slots + 2 * kMaxValues * slot_stride(C);
+    float *cell = wscr + nwarps * kMaxValues * 32;
+    for (uint32_t e = threadIdx.x; e < 2 * kMaxValues * slot_stride(C); e += blockDim.x) slots[e] = 0.f;
+    if (threadIdx.x == 0) cell[0] = 0.f;
+    if (C > 1)
+        cluster.sync();
+    else
+        __syncthreads();
+    float v = (float)(threadIdx.x & 7) * 1e-3f;
+    for (uint32_t it = 0; it < reps; ++it) {
+        if constexpr (KIND == PROBE_LOOP) {
+            v = fmaf(v, 0.999f, 1e-3f);
+        } else if constexpr (KIND == PROBE_SYNCTHREADS) {
+            v = fmaf(v, 0.999f, 1e-3f);
+            __syncthreads();
+        } else if constexpr (KIND == PROBE_CLUSTER) {
+            v = fmaf(v, 0.999f, 1e-3f);
+            cluster.sync();
+        } else if constexpr (KIND == PROBE_DSMEM) {
+            // one boundary push to the next rank's shared memory, then the barrier
+            // that makes it visible, as a halo push before a reduction
+            if (threadIdx.x == 0) *cluster.map_shared_rank(cell, (rank + 1) % C) = v;
+            cluster.sync();
+            v = fmaf(cell[0], 0.5f, v);
+        } else {
+            float q[NQ];
+#pragma unroll
+            for (int j = 0; j < NQ; ++j) q[j] = v + (float)j;
+            cluster_allreduce<float, NQ>(q, slots, wscr, (int)(it & 1), cluster, C, rank);
+            v = fmaf(q[0], 1e-9f, v * 0.5f);
+        }
+    }
+    if (v == 12345.678f) sink[0] = v;  // keeps the chain alive
+}
+
+size_t probe_smem(uint32_t C, uint32_t threads) {
+    return (2 * kMaxValues * slot_stride(C) + (threads / 32) * kMaxValues * 32 + 32) * sizeof(float);
+}
+
+int probe_fail(int code, const std::string &msg) {
+    set_last_error(msg);
+    return code;
+}
+
+// ns per repetition of one probe kernel (grid of `clusters` clusters of C CTAs)
+int time_probe(const void *func, uint32_t C, uint32_t threads, uint32_t clusters, uint32_t reps, float *sink,
+               double *ns) {
+    const size_t smem = probe_smem(C, threads);
+    cudaError_t e = cudaSuccess;
+    if (C > 8) e = cudaFuncSetAttribute(func, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return probe_fail(GBDPCG_ERR_CUDA, std::string("probe set-up: ") + cudaGetErrorString(e));
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (clusters == 0) {
+        int active = 0;
+        cfg.gridDim = dim3(C);
+        e = cudaOccupancyMaxActiveClusters(&active, func, &cfg);
+        if (e != cudaSuccess || active <= 0)
+            return probe_fail(GBDPCG_ERR_UNSUPPORTED, "probe: cluster shape cannot be scheduled");
+        clusters = (uint32_t)active;
+    }
+    cfg.gridDim = dim3(clusters * C);
+    uint32_t r = reps;
+    void *args[] = {&r, &sink};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float ms = 0.f;
+    e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaLaunchKernelExC(&cfg, func, args);  // warm
+    if (e == cudaSuccess) e = cudaEventRecord(e0, 0);
+    if (e == cudaSuccess) e = cudaLaunchKernelExC(&cfg, func, args);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (e != cudaSuccess) return probe_fail(GBDPCG_ERR_CUDA, std::string("probe: ") + cudaGetErrorString(e));
+    *ns = (double)ms * 1e6 / (double)reps;
+    return GBDPCG_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbdpcg_probe_primitives(int device, uint32_t cluster, uint32_t threads, uint32_t clusters, uint32_t reps,
+                            gbdpcg_probe *out) {
+    if (!out) return probe_fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (cluster < 1 || cluster > 16 || threads < 32 || threads > 1024 || threads % 32 || reps == 0)
+        return probe_fail(GBDPCG_ERR_INVALID_ARGUMENT, "cluster 1..16, threads a multiple of 32 up to 1024, reps > 0");
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != device && cudaSetDevice(device) != cudaSuccess)
+        return probe_fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad device");
+    float *sink = nullptr;
+    int rc = GBDPCG_SUCCESS;
+    if (cudaMalloc(&sink, sizeof(float)) != cudaSuccess) rc = probe_fail(GBDPCG_ERR_NO_MEMORY, "probe sink");
+    double loop = 0, t[7] = {0, 0, 0, 0, 0, 0, 0};
+    const void *fns[7] = {(const void *)&probe_kernel<PROBE_LOOP, 1>, (const void *)&probe_kernel<PROBE_SYNCTHREADS, 1>,
+                          (const void *)&probe_kernel<PROBE_CLUSTER, 1>, (const void *)&probe_kernel<PROBE_DSMEM, 1>,
+                          (const void *)&probe_kernel<PROBE_REDUCE, 1>, (const void *)&probe_kernel<PROBE_REDUCE, 2>,
+                          (const void *)&probe_kernel<PROBE_REDUCE, 3>};
+    for (int k = 0; k < 7 && rc == GBDPCG_SUCCESS; ++k) {
+        if ((k == 2 || k == 3) && cluster == 1) continue;  // no cluster barrier in a one-CTA cluster
+        rc = time_probe(fns[k], cluster, threads, clusters, reps, sink, k == 0 ? &loop : &t[k]);
+    }
+    if (sink) cudaFree(sink);
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    if (rc) return rc;
+    memset(out, 0, sizeof(*out));
+    auto net = [&](double x) { return x > loop ? x - loop : 0.0; };
+    out->loop_ns = loop;
+    out->syncthreads_ns = net(t[1]);
+    out->cluster_barrier_ns = cluster > 1 ? net(t[2]) : 0.0;
+    out->dsmem_store_barrier_ns = cluster > 1 ? net(t[3]) : 0.0;
+    for (int q = 0; q < 3; ++q) out->allreduce_ns[q] = net(t[4 + q]);
+    return GBDPCG_SUCCESS;
+}
+
+}  // extern "C"

@@ -63,6 +63,29 @@ class PackedSystem(ctypes.Structure):
                 ("Pinv_off", ctypes.c_uint64), ("vec_off", ctypes.c_uint64)]
 
 
+class Stamp(ctypes.Structure):
+    """gbdpcg_stamp: one system's timeline (GPU global clock, ns)."""
+    _fields_ = [("t_pop", ctypes.c_uint64), ("t_staged", ctypes.c_uint64), ("t_solved", ctypes.c_uint64),
+                ("t_done", ctypes.c_uint64), ("system", ctypes.c_uint32), ("launch", ctypes.c_uint32),
+                ("cluster", ctypes.c_uint32), ("iters", ctypes.c_uint32)]
+
+
+class Probe(ctypes.Structure):
+    """gbdpcg_probe: ns per repetition of each synchronisation primitive."""
+    _fields_ = [("loop_ns", ctypes.c_double), ("syncthreads_ns", ctypes.c_double),
+                ("cluster_barrier_ns", ctypes.c_double), ("dsmem_store_barrier_ns", ctypes.c_double),
+                ("allreduce_ns", ctypes.c_double * 3)]
+
+
+def probe_primitives(device=0, cluster=1, threads=128, clusters=1, reps=100000) -> dict:
+    """Latency of the solver's synchronisation primitives (gbdpcg_probe_primitives)."""
+    p = Probe()
+    _check(lib().gbdpcg_probe_primitives(device, cluster, threads, clusters, reps, ctypes.byref(p)),
+           "gbdpcg_probe_primitives")
+    return {"loop_ns": p.loop_ns, "syncthreads_ns": p.syncthreads_ns, "cluster_barrier_ns": p.cluster_barrier_ns,
+            "dsmem_store_barrier_ns": p.dsmem_store_barrier_ns, "allreduce_ns": list(p.allreduce_ns)}
+
+
 class System(ctypes.Structure):
     _fields_ = [("S", ctypes.c_void_p), ("Pinv", ctypes.c_void_p), ("gamma", ctypes.c_void_p),
                 ("lambda_", ctypes.c_void_p), ("lambda_fwd", ctypes.c_void_p), ("dS", ctypes.c_void_p),
@@ -100,6 +123,9 @@ _SIGS = {
     "gbdpcg_plan_launch_info": ([_P, _U, _P, _P, _P, _P, _P], _I),
     "gbdpcg_plan_launch_kernel": ([_P, _U, _P, _P, _P], _I),
     "gbdpcg_plan_destroy": ([_P], _I),
+    "gbdpcg_plan_timeline": ([_P, _I], _I),
+    "gbdpcg_plan_timeline_read": ([_P, _P, _U, _P, _P, _U, _P, _P], _I),
+    "gbdpcg_probe_primitives": ([_I, _U, _U, _U, _U, _P], _I),
     "gbdpcg_form_schur_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
     "gbdpcg_form_schur_f64": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
     "gbdpcg_form_schur_pinv_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P, _P], _I),
@@ -364,6 +390,27 @@ class Plan:
             d.update(zip(("storage", "rows_per_thread", "algorithm"), [x.value for x in k]))
             out.append(d)
         return out
+
+    def timeline(self, enable=True):
+        """Switch the per-system timeline of the executions on or off."""
+        _check(lib().gbdpcg_plan_timeline(self.p, 1 if enable else 0), "gbdpcg_plan_timeline")
+
+    def timeline_read(self, stream=None):
+        """The last execution's timeline: (structured numpy array of the
+        records, numpy array of the SM of every CTA of every launch)."""
+        import numpy as np
+        n, m = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(lib().gbdpcg_plan_timeline_read(self.p, None, 0, ctypes.byref(n), None, 0, ctypes.byref(m),
+                                               _stream(stream)), "gbdpcg_plan_timeline_read")
+        recs = (Stamp * max(1, n.value))()
+        sms = (ctypes.c_uint32 * max(1, m.value))()
+        _check(lib().gbdpcg_plan_timeline_read(self.p, ctypes.cast(recs, ctypes.c_void_p), n.value, ctypes.byref(n),
+                                               ctypes.cast(sms, ctypes.c_void_p), m.value, ctypes.byref(m),
+                                               _stream(stream)), "gbdpcg_plan_timeline_read")
+        dt = np.dtype([("t_pop", "<u8"), ("t_staged", "<u8"), ("t_solved", "<u8"), ("t_done", "<u8"),
+                       ("system", "<u4"), ("launch", "<u4"), ("cluster", "<u4"), ("iters", "<u4")])
+        return (np.frombuffer(bytes(recs), dtype=dt)[:n.value].copy(),
+                np.frombuffer(bytes(sms), dtype=np.uint32)[:m.value].copy())
 
     def autotune(self, flags=0, reps=0, stream=None):
         """Times each launch class's candidate shapes on the plan's systems and

@@ -393,6 +393,47 @@ GBDPCG_API int gbdpcg_plan_launch_kernel(gbdpcg_plan_t plan, uint32_t i, uint32_
                                          uint32_t *rows_per_thread, uint32_t *algorithm);
 GBDPCG_API int gbdpcg_plan_destroy(gbdpcg_plan_t plan);
 
+/* Timeline of a plan's executions (no reference counterpart: measurement).
+ * With the timeline on, every execution records for each system solved by a
+ * cluster launch the GPU's global nanosecond clock (%globaltimer) at four
+ * points, read by the leading thread of the cluster that solved it, and the
+ * SM of every CTA of every launch.  It costs a few stores per system; the
+ * launches are captured again when it is switched. */
+typedef struct {
+    uint64_t t_pop;     /* the cluster took the system from its launch's work list */
+    uint64_t t_staged;  /* the system's matrix rows are on chip (the leading CTA's view) */
+    uint64_t t_solved;  /* the PCG iteration has ended */
+    uint64_t t_done;    /* lambda, the result and any adjoint output written */
+    uint32_t system;    /* index of the system in the plan */
+    uint32_t launch;    /* launch index (gbdpcg_plan_launch_info) */
+    uint32_t cluster;   /* cluster of the launch's grid that solved it */
+    uint32_t iters;     /* PCG passes (0: rejected by the launch) */
+} gbdpcg_stamp;
+GBDPCG_API int gbdpcg_plan_timeline(gbdpcg_plan_t plan, int enable);
+/* Latency of the synchronisation primitives one cluster-solver iteration is
+ * made of (no reference counterpart: measurement), on a grid of `clusters`
+ * clusters of `cluster` CTAs of `threads` threads (clusters = 0: as many as
+ * fit at once), each primitive repeated `reps` times in a dependent loop and
+ * timed with CUDA events; nanoseconds per repetition, the loop's own cost
+ * subtracted.  The cluster-barrier fields are 0 for cluster = 1.
+ * Synchronous; allocates one word of device memory. */
+typedef struct {
+    double loop_ns;                 /* one repetition of the empty dependent loop */
+    double syncthreads_ns;          /* __syncthreads */
+    double cluster_barrier_ns;      /* barrier.cluster arrive (release) + wait (acquire) */
+    double dsmem_store_barrier_ns;  /* one store into the next CTA's shared memory + the cluster barrier */
+    double allreduce_ns[3];         /* the solver's cluster-wide reduction of 1, 2, 3 values */
+} gbdpcg_probe;
+GBDPCG_API int gbdpcg_probe_primitives(int device, uint32_t cluster, uint32_t threads, uint32_t clusters,
+                                       uint32_t reps, gbdpcg_probe *out);
+/* Waits for the stream and copies the last execution's records (one per
+ * system of the cluster launches, grouped by launch; at most `capacity`) and
+ * the SM of each CTA (launch 0's CTAs first, in grid order; at most
+ * `sm_capacity`).  *count and *sm_count receive the full sizes. */
+GBDPCG_API int gbdpcg_plan_timeline_read(gbdpcg_plan_t plan, gbdpcg_stamp *stamps, uint32_t capacity,
+                                         uint32_t *count, uint32_t *cta_sm, uint32_t sm_capacity,
+                                         uint32_t *sm_count, gbdpcg_stream_t stream);
+
 /* Autotuner (no reference counterpart: the reference fixes 64 threads per CTA
  * and one CTA per knot).  For every launch class of the plan it times, on the
  * plan's own systems, the class alone with each launch shape that holds all

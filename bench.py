@@ -447,20 +447,25 @@ def timeline_summary(stamps, cta_sm, launches, sm_count):
 
 def latency_floor(gbdpcg, cls, grid_clusters, dev_index=0, reps=100000):
     """The floor that the synchronisation primitives put under one PCG
-    iteration of a launch shape: two cluster-wide reductions (1 and 2 values)
-    and two CTA barriers (standard form) or one (recurrence form), each
-    measured by gbdpcg_probe_primitives on the shape (cluster size, CTA size)
-    with all the shape's clusters running at once; frac = floor / achieved."""
+    iteration of a launch shape: two cluster-wide reductions (1 and 2 values,
+    in the form the kernel uses at that cluster size) and two CTA barriers
+    (standard form) or one (recurrence form), each measured by
+    gbdpcg_probe_primitives on the shape (cluster size, CTA size) with all the
+    shape's clusters running at once; frac = floor / achieved."""
     C, thr = cls["cluster"], cls["threads"]
     under_load = gbdpcg.probe_primitives(dev_index, C, thr, grid_clusters, reps)
     alone = gbdpcg.probe_primitives(dev_index, C, thr, 1, reps)
     rec = cls["algorithm"] == gbdpcg.ALGO_RECURRENCE
     barriers = 1 if rec else 2
-    floor = under_load["allreduce_ns"][0] + under_load["allreduce_ns"][1] + barriers * under_load["syncthreads_ns"]
+    # the cluster kernels reduce with transaction-counted stores for C >= 2,
+    # with the CTA-barrier form for C = 1
+    red = under_load["allreduce_tx_ns"] if C > 1 else under_load["allreduce_ns"]
+    floor = red[0] + red[1] + barriers * under_load["syncthreads_ns"]
     ach = cls["us_per_iteration_median"] * 1e3
     return {"shape": {"cluster": C, "threads": thr, "storage": cls["storage"], "algorithm": cls["algorithm"],
                       "clusters_at_once": grid_clusters},
-            "model": f"allreduce(1) + allreduce(2) + {barriers} x __syncthreads per iteration",
+            "model": f"reduction(1 value) + reduction(2 values) + {barriers} x __syncthreads per iteration "
+                     f"({'transaction-counted' if C > 1 else 'CTA-barrier'} reductions)",
             "floor_us_per_iter": floor / 1e3, "achieved_us_per_iter": ach / 1e3, "frac": floor / ach,
             "primitives_under_load_ns": under_load, "primitives_alone_ns": alone}
 

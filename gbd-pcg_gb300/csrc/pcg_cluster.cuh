@@ -60,6 +60,12 @@ enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2, ST_HYB = 3, ST_TMEM = 4 };
 // can share the SM (an allocation would otherwise wait on the first one).
 constexpr size_t kTmemExclusiveSmem = 120 * 1024;
 
+// Per-CTA bookkeeping area of the kernels' shared memory (32-byte aligned):
+// word 0 the popped work item, word 1 the tensor-memory base address, bytes
+// 32..47 the two mbarriers of the transaction-counted reductions, word 12 the
+// CTA's reduction-timeout flag.
+constexpr size_t kItemBytes = 64;
+
 // Reduction slots: [2 buffers][3 values][C ranks x 32 warps]
 constexpr int kMaxValues = 3;
 __host__ __device__ constexpr size_t slot_stride(uint32_t C) { return (size_t)32 * C; }
@@ -88,7 +94,7 @@ struct SmemPlan {
         return round_up((size_t)nwarps * kMaxValues * 32 * sizeof(A), 32);
     }
     __host__ __device__ static size_t bytes(uint32_t kmax, uint32_t C, uint32_t nwarps) {
-        const size_t b = 2 * vec(kmax) + 2 * halo() + slots(C) + wscr(nwarps) + 32 + mat_s(kmax) + mat_p(kmax);
+        const size_t b = 2 * vec(kmax) + 2 * halo() + slots(C) + wscr(nwarps) + kItemBytes + mat_s(kmax) + mat_p(kmax);
         return (ST == ST_TMEM && b < kTmemExclusiveSmem) ? kTmemExclusiveSmem : b;
     }
 };
@@ -382,6 +388,39 @@ __device__ __forceinline__ void tmem_pmatvec(uint32_t trow, const float *x, floa
     y[1] = a1;
 }
 
+// Hint the L2 to fetch [p, p + bytes) from HBM now (cp.async.bulk.prefetch:
+// one instruction for a whole contiguous range, no registers, no completion to
+// wait for).  Only the 16-byte-aligned interior is named, so the hint never
+// reaches outside the array.
+__device__ __forceinline__ void prefetch_l2_range(const void *p, size_t bytes) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+    const uintptr_t lo = (a + 15) & ~(uintptr_t)15, hi = (a + bytes) & ~(uintptr_t)15;
+    if (hi <= lo) return;
+    for (uintptr_t x = lo; x < hi; x += (uintptr_t)1 << 30) {
+        const uint32_t sz = (uint32_t)((hi - x) < ((uintptr_t)1 << 30) ? (hi - x) : ((uintptr_t)1 << 30));
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(x), "r"(sz) : "memory");
+    }
+}
+
+// One element global -> shared memory: an asynchronous copy (cp.async, which
+// holds no register and does not wait) when the types agree, so that all of a
+// thread's elements are in flight at once; a load and a converting store
+// otherwise.  stage_wait() completes the thread's copies.
+template <typename TO, typename TI>
+__device__ __forceinline__ void stage_elem(TO *dst, const TI *src) {
+    if constexpr (std::is_same<TO, TI>::value && (sizeof(TO) == 4 || sizeof(TO) == 8)) {
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)),
+                     "l"(src), "n"((int)sizeof(TO))
+                     : "memory");
+    } else {
+        *dst = static_cast<TO>(__ldg(src));
+    }
+}
+
+// Waits for this thread's staging copies (a barrier must follow before other
+// threads read them).
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Stage the block rows of knots [kb, kb+nk) (blk = NB n^2 elements each,
 // column-major n x NB n) into the column-interleaved layout M[c*R + k*n + i].
 template <typename TO, typename TI>
@@ -390,7 +429,7 @@ __device__ __forceinline__ void stage_rows(TO *M, uint32_t R, const TI *__restri
     for (uint32_t e = tid; e < nk * blk; e += nthr) {
         const uint32_t kl = e / blk, w = e - kl * blk;
         const uint32_t c = w / n, i = w - c * n;
-        M[(size_t)c * R + kl * n + i] = static_cast<TO>(__ldg(g + e));
+        stage_elem(M + (size_t)c * R + kl * n + i, g + e);
     }
 }
 
@@ -403,7 +442,7 @@ __device__ __forceinline__ void stage_block(TO *M, uint32_t R, const TI *__restr
     for (uint32_t e = tid; e < nk * blk; e += nthr) {
         const uint32_t kl = e / blk, w = e - kl * blk;
         const uint32_t c = w / n, i = w - c * n;
-        M[(size_t)c * R + kl * n + i] = static_cast<TO>(__ldg(g + (size_t)kl * stride + w));
+        stage_elem(M + (size_t)c * R + kl * n + i, g + (size_t)kl * stride + w);
     }
 }
 
@@ -428,33 +467,66 @@ __device__ __forceinline__ void warp_sum_n(A (&v)[NQ]) {
     }
 }
 
-// Sum of the 32 values at p (A-typed, 16-byte aligned) with vector loads into
-// four accumulator chains (element j into chain j mod 4), then (c0+c1)+(c2+c3).
-template <typename A>
-__device__ __forceinline__ A sum32(const A *p) {
+// Sum of the M (32 or 64) values at p (A-typed, 16-byte aligned) with vector
+// loads into four accumulator chains (element j into chain j mod 4), then
+// (c0+c1)+(c2+c3).
+template <typename A, int M>
+__device__ __forceinline__ A sum_slots(const A *p) {
+    static_assert(M % 4 == 0, "four chains");
     A c0 = A(0), c1 = A(0), c2 = A(0), c3 = A(0);
     if constexpr (std::is_same<A, f2acc>::value) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < M / 4; ++j) {
             const float4 t0 = reinterpret_cast<const float4 *>(p)[2 * j];
             const float4 t1 = reinterpret_cast<const float4 *>(p)[2 * j + 1];
             c0 += f2acc(t0.x, t0.y); c1 += f2acc(t0.z, t0.w); c2 += f2acc(t1.x, t1.y); c3 += f2acc(t1.z, t1.w);
         }
     } else if constexpr (sizeof(A) == 4) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < M / 4; ++j) {
             const float4 t = reinterpret_cast<const float4 *>(p)[j];
             c0 += t.x; c1 += t.y; c2 += t.z; c3 += t.w;
         }
     } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < M / 4; ++j) {
             const double2 t0 = reinterpret_cast<const double2 *>(p)[2 * j];
             const double2 t1 = reinterpret_cast<const double2 *>(p)[2 * j + 1];
             c0 += t0.x; c1 += t0.y; c2 += t1.x; c3 += t1.y;
         }
     }
     return (c0 + c1) + (c2 + c3);
+}
+
+template <typename A>
+__device__ __forceinline__ A sum32(const A *p) {
+    return sum_slots<A, 32>(p);
+}
+
+// The slots of one reduction value, summed identically in every thread: up
+// to 32 slots (zero beyond `total`) with vector loads and four chains, and up
+// to 64 that way too for float accumulators; more with a strided sum per lane
+// and a warp butterfly.  (Double and float-float additions are many times
+// dearer than float ones on GB300, so for them every thread adding 64 slots
+// costs more than the butterfly's shuffles.)
+template <typename A, int NQ>
+__device__ __forceinline__ void sum_all_slots(A (&v)[NQ], const A *sl, uint32_t stride, uint32_t total) {
+    if (total <= 32) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) v[q] = sum_slots<A, 32>(sl + q * stride);
+    } else if (std::is_same<A, float>::value && total <= 64) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) v[q] = sum_slots<A, 64>(sl + q * stride);
+    } else {
+        const uint32_t lane = threadIdx.x & 31;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) {
+            A s = A(0);
+            for (uint32_t j = lane; j < total; j += 32) s += sl[q * stride + j];
+            v[q] = s;
+        }
+        warp_sum_n<A, NQ>(v);
+    }
 }
 
 // Cluster-wide sum of NQ values, identical in every thread of the cluster.
@@ -465,9 +537,9 @@ __device__ __forceinline__ A sum32(const A *p) {
 //   2. one barrier (barrier.cluster, or __syncthreads when C == 1), whose
 //      release/acquire makes the stores — and any halo pushes the caller made
 //      before this call — visible;
-//   3. every thread sums the slots: the first 32 (zero beyond C*W) with sum32;
-//      when C*W > 32, lane l sums slots l, l+32, ... and a warp butterfly
-//      finishes.
+//   3. every thread sums the slots: up to 32 (64 for float; zero beyond C*W)
+//      with vector loads (sum_all_slots); beyond that, lane l sums slots l,
+//      l+32, ... and a warp butterfly finishes.
 // Every thread of every CTA reads the same slots in the same order, so all hold
 // the same bits.  `buf` alternates between call sites so that a slot array is
 // rewritten only after a barrier that every reader has passed.  Slots
@@ -495,18 +567,7 @@ __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, A *wscr,
         __syncthreads();
     else
         cluster.sync();
-    if (total <= 32) {
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) v[q] = sum32(sl + q * stride);
-    } else {
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-            A s = A(0);
-            for (uint32_t j = lane; j < total; j += 32) s += sl[q * stride + j];
-            v[q] = s;
-        }
-        warp_sum_n<A, NQ>(v);
-    }
+    sum_all_slots<A, NQ>(v, sl, stride, total);
 #pragma unroll
     for (int q = 0; q < NQ; ++q) v[q] = acc_normalize(v[q]);
 }
@@ -560,6 +621,157 @@ struct Stamper {
     }
 };
 
+// ---------------------------------------------------------------- reductions by
+// transaction-counted stores.  A cluster barrier (barrier.cluster with release
+// and acquire) makes a CTA wait until its own distributed-shared-memory
+// stores have reached the other CTAs and then until every CTA has arrived.
+// Here each warp's partial sums go to every CTA with st.async, which counts
+// the bytes on the receiving CTA's mbarrier (complete_tx); each CTA waits only
+// until all of the bytes addressed to it have arrived.  Two mbarriers (and two
+// slot buffers) alternate between calls: a CTA's partials for call k+2 can
+// only be sent after every CTA has received all of call k+1, which every warp
+// of the receiving CTA sent only after it had read its call-k slots.  Halo
+// values a reduction's caller sends to its neighbours go the same way, counted
+// on the same mbarrier, so their arrival is what the reduction waits for too.
+// Every wait is bounded: after about a second without completion it sets the
+// CTA's timeout flag and returns (the caller reports the system as timed out;
+// every later wait of the CTA returns at once).
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint32_t map_rank_u32(uint32_t local, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Makes mbarrier initialisations visible to the other CTAs of the cluster
+// (they must be followed by a cluster barrier before any remote use).
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void st_async(uint32_t raddr, float v, uint32_t rbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f32 [%0], %1, [%2];" ::"r"(raddr), "f"(v),
+                 "r"(rbar)
+                 : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t raddr, double v, uint32_t rbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.f64 [%0], %1, [%2];" ::"r"(raddr), "d"(v),
+                 "r"(rbar)
+                 : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t raddr, f2acc v, uint32_t rbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(raddr),
+                 "f"(v.hi), "f"(v.lo), "r"(rbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase of `bar` with the given parity; gives up after about a
+// second (globaltimer), setting *timed_out.  Returns at once if *timed_out is set.
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t *bar, uint32_t parity, volatile uint32_t *timed_out) {
+    if (mbar_try_wait(bar, parity)) return;
+    const uint64_t t0 = global_ns();
+    for (uint32_t spin = 1;; ++spin) {
+        if (mbar_try_wait(bar, parity)) return;
+        if (*timed_out) return;
+        if ((spin & 255u) == 0 && global_ns() - t0 > 1000000000ull) {
+            *timed_out = 1u;
+            return;
+        }
+    }
+}
+
+// Shared state of the transaction-counted reductions of one CTA.
+struct TxReduce {
+    uint64_t *bar;        // [2] mbarriers, one per slot buffer
+    uint32_t parity;      // bit b: parity of the phase buffer b waits for next
+    uint32_t *timed_out;  // CTA-wide flag
+};
+
+// Cluster-wide sum of NQ values, identical in every thread of the cluster, for
+// C >= 2 (C == 1 uses cluster_allreduce, whose barrier is __syncthreads).
+// Same slots, same summation order and same result bits as
+// cluster_allreduce: warp sums with sum32 into slot [rank*W + w] of every CTA,
+// then every thread sums the slots.  `extra_bytes`: halo values the
+// neighbours send on the same buffer (push_halo_tx) before this call.
+template <typename A, int NQ>
+__device__ __forceinline__ void cluster_allreduce_tx(A (&v)[NQ], A *slots, A *wscr, int buf, TxReduce &tx,
+                                                     uint32_t C, uint32_t rank, uint32_t extra_bytes = 0) {
+    static_assert(NQ <= kMaxValues, "slot array holds kMaxValues values");
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t nwarps = blockDim.x >> 5;
+    const uint32_t stride = (uint32_t)slot_stride(C);
+    A *sl = slots + (size_t)buf * stride * kMaxValues;
+    A *ws = wscr + (size_t)warp * kMaxValues * 32;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) ws[q * 32 + lane] = v[q];
+    __syncwarp();
+    if (threadIdx.x == 0)
+        mbar_arrive_expect_tx(tx.bar + buf, (uint32_t)(NQ * C * nwarps * sizeof(A)) + extra_bytes);
+    const uint32_t my = rank * nwarps + warp, total = C * nwarps;
+    if (lane < C) {
+        const uint32_t rbar = map_rank_u32(smem_u32(tx.bar + buf), lane);
+        const uint32_t rsl = map_rank_u32(smem_u32(sl), lane);
+#pragma unroll
+        for (int q = 0; q < NQ; ++q)
+            st_async(rsl + (uint32_t)((q * stride + my) * sizeof(A)), sum32(ws + q * 32), rbar);
+    }
+    mbar_wait_bounded(tx.bar + buf, (tx.parity >> buf) & 1u, tx.timed_out);
+    tx.parity ^= 1u << buf;
+    sum_all_slots<A, NQ>(v, sl, stride, total);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) v[q] = acc_normalize(v[q]);
+}
+
+// Halo values for a neighbouring CTA, sent like the reduction partials: RPT
+// consecutive values into the neighbour's copy of `dst_local` (an address in
+// this CTA's shared memory; the neighbour has the same layout), counted on the
+// neighbour's mbarrier `buf`, i.e. part of the bytes its next reduction on
+// that buffer waits for (cluster_allreduce_tx's extra_bytes).
+template <typename T, int RPT>
+__device__ __forceinline__ void push_halo_tx(const T *dst_local, uint32_t to, const T (&v)[RPT], const TxReduce &tx,
+                                             int buf) {
+    const uint32_t ra = map_rank_u32(smem_u32(dst_local), to);
+    const uint32_t rb = map_rank_u32(smem_u32(tx.bar + buf), to);
+#pragma unroll
+    for (int q = 0; q < RPT; ++q) st_async(ra + (uint32_t)(q * sizeof(T)), v[q], rb);
+}
+
+// A cluster-wide reduction of the cluster solver: the transaction-counted
+// form for C >= 2 (with `extra_bytes` of halo values expected on the same
+// buffer), the CTA-barrier form for C == 1.
+template <typename A, int NQ>
+__device__ __forceinline__ void solver_allreduce(A (&v)[NQ], A *slots, A *wscr, int buf, TxReduce &tx,
+                                                 const cg::cluster_group &cluster, uint32_t C, uint32_t rank,
+                                                 uint32_t extra_bytes) {
+    if (C == 1)
+        cluster_allreduce<A, NQ>(v, slots, wscr, buf, cluster, C, rank);
+    else
+        cluster_allreduce_tx<A, NQ>(v, slots, wscr, buf, tx, C, rank, extra_bytes);
+}
+
 __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uint32_t C) {
     if (C > 1)
         cluster.sync();
@@ -603,12 +815,24 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     T *zh = reinterpret_cast<T *>(sp); sp += Plan::halo();
     A *slots = reinterpret_cast<A *>(sp); sp += Plan::slots(C);
     A *wscr = reinterpret_cast<A *>(sp); sp += Plan::wscr(nthr >> 5);
-    uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
+    uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += kItemBytes;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp);
     const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
 
     for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
+    // transaction-counted reductions (C >= 2): two mbarriers of one arrival each,
+    // initialised and made visible to the cluster before any CTA sends to them
+    TxReduce tx{reinterpret_cast<uint64_t *>(s_item + 8), 0u, s_item + 12};
+    if (C > 1) {
+        if (tid == 0) {
+            mbar_init(tx.bar, 1);
+            mbar_init(tx.bar + 1, 1);
+            *tx.timed_out = 0u;
+            mbar_init_fence();
+        }
+        cluster.sync();
+    }
     // tensor memory: warp 0 allocates every column (the CTA is alone on its SM);
     // warp w reaches lanes (w % 4) * 32 + lane, its rows at columns (w / 4) * 3 RPT NPT
     uint32_t tbase = 0, trow = 0;
@@ -668,6 +892,14 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         const uint32_t R = (K * n + 1) & ~1u;  // row stride of staged matrices (even)
         const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
         const bool first_knot = act && lk == 0 && kb > 0, last_knot = act && lk + 1 == nk && ke < N;
+        // halo bytes the neighbours send to this CTA before a reduction (n values each)
+        const uint32_t halo_in = ((has_left ? n : 0u) + (has_right ? n : 0u)) * (uint32_t)sizeof(T);
+        // this CTA's block rows of S and Phi^-1 into L2 at once: the staging
+        // loads below then wait on L2, not on HBM, round after round
+        if (tid == 0 && nk > 0) {
+            prefetch_l2_range(S + (size_t)kb * blkS, (size_t)nk * blkS * sizeof(T));
+            prefetch_l2_range(P + (size_t)kb * blkP, (size_t)nk * blkP * sizeof(T));
+        }
 
         for (uint32_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
 
@@ -808,6 +1040,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         };
         T *my_p = vp + (lk + 1) * NP + i;  // this thread's rows in the windows
         T *my_r = vr + (lk + 1) * NP + i;
+        stage_wait();
         __syncthreads();
         stamp.staged();
 
@@ -858,16 +1091,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             p[q] = z[q];
             if (act) my_p[q] = p[q];
         }
-        if (first_knot) {
-            T *dst = cluster.map_shared_rank(vp, rank - 1) + (K + 1) * NP + i;
-#pragma unroll
-            for (int q = 0; q < RPT; ++q) dst[q] = z[q];
-        }
-        if (last_knot) {
-            T *dst = cluster.map_shared_rank(vp, rank + 1) + i;
-#pragma unroll
-            for (int q = 0; q < RPT; ++q) dst[q] = z[q];
-        }
+        if (first_knot) push_halo_tx<T, RPT>(vp + (K + 1) * NP + i, rank - 1, z, tx, 1);
+        if (last_knot) push_halo_tx<T, RPT>(vp + i, rank + 1, z, tx, 1);
         A eta, gg;
         {
             A v2[2] = {A(0), A(0)};
@@ -876,7 +1101,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 acc_madd(v2[0], r[q], z[q]);
                 acc_madd(v2[1], gam[q], gam[q]);
             }
-            cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
+            solver_allreduce<A, 2>(v2, slots, wscr, 1, tx, cluster, C, rank, halo_in);
             eta = v2[0];
             gg = v2[1];
         }
@@ -893,23 +1118,15 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             matS_rows(y);
             for (; iter < max_iter;) {
                 if constexpr (PTRI) {  // neighbours need this CTA's boundary y for their r halo
-                    if (first_knot) {
-                        T *dst = cluster.map_shared_rank(uh, rank - 1) + NP + i;
-#pragma unroll
-                        for (int q = 0; q < RPT; ++q) dst[q] = y[q];
-                    }
-                    if (last_knot) {
-                        T *dst = cluster.map_shared_rank(uh, rank + 1) + i;
-#pragma unroll
-                        for (int q = 0; q < RPT; ++q) dst[q] = y[q];
-                    }
+                    if (first_knot) push_halo_tx<T, RPT>(uh + NP + i, rank - 1, y, tx, 0);
+                    if (last_knot) push_halo_tx<T, RPT>(uh + i, rank + 1, y, tx, 0);
                 }
                 A pap;
                 {
                     A v1[1] = {A(0)};
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) acc_madd(v1[0], p[q], y[q]);
-                    cluster_allreduce<A, 1>(v1, slots, wscr, 0, cluster, C, rank);
+                    solver_allreduce<A, 1>(v1, slots, wscr, 0, tx, cluster, C, rank, PTRI ? halo_in : 0u);
                     pap = v1[0];
                 }
                 const T alpha = (pap == A(0)) ? T(0) : acc_ratio<T>(eta, pap);
@@ -935,16 +1152,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) my_p[q] = z[q];
                 }
-                if (first_knot) {
-                    T *dst = cluster.map_shared_rank(vp, rank - 1) + (K + 1) * NP + i;
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) dst[q] = z[q];
-                }
-                if (last_knot) {
-                    T *dst = cluster.map_shared_rank(vp, rank + 1) + i;
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) dst[q] = z[q];
-                }
+                if (first_knot) push_halo_tx<T, RPT>(vp + (K + 1) * NP + i, rank - 1, z, tx, 1);
+                if (last_knot) push_halo_tx<T, RPT>(vp + i, rank + 1, z, tx, 1);
                 {
                     A v2[2] = {A(0), A(0)};
 #pragma unroll
@@ -952,7 +1161,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                         acc_madd(v2[0], r[q], z[q]);
                         if (relres) acc_madd(v2[1], r[q], r[q]);
                     }
-                    cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
+                    solver_allreduce<A, 2>(v2, slots, wscr, 1, tx, cluster, C, rank, halo_in);
                     eta_new = v2[0];
                     rr = v2[1];
                 }
@@ -973,23 +1182,15 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             for (; iter < max_iter;) {
                 matS_rows(y);
                 if constexpr (PTRI) {  // neighbours need this CTA's boundary upsilon for their r halo
-                    if (first_knot) {
-                        T *dst = cluster.map_shared_rank(uh, rank - 1) + NP + i;
-#pragma unroll
-                        for (int q = 0; q < RPT; ++q) dst[q] = y[q];
-                    }
-                    if (last_knot) {
-                        T *dst = cluster.map_shared_rank(uh, rank + 1) + i;
-#pragma unroll
-                        for (int q = 0; q < RPT; ++q) dst[q] = y[q];
-                    }
+                    if (first_knot) push_halo_tx<T, RPT>(uh + NP + i, rank - 1, y, tx, 0);
+                    if (last_knot) push_halo_tx<T, RPT>(uh + i, rank + 1, y, tx, 0);
                 }
                 A pap;
                 {
                     A v1[1] = {A(0)};
 #pragma unroll
                     for (int q = 0; q < RPT; ++q) acc_madd(v1[0], p[q], y[q]);
-                    cluster_allreduce<A, 1>(v1, slots, wscr, 0, cluster, C, rank);
+                    solver_allreduce<A, 1>(v1, slots, wscr, 0, tx, cluster, C, rank, PTRI ? halo_in : 0u);
                     pap = v1[0];
                 }
                 const T alpha = (pap == A(0)) ? T(0) : acc_ratio<T>(eta, pap);
@@ -1010,16 +1211,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 }
                 __syncthreads();
                 matP_rows(z);
-                if (first_knot) {
-                    T *dst = cluster.map_shared_rank(zh, rank - 1) + NP + i;
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) dst[q] = z[q];
-                }
-                if (last_knot) {
-                    T *dst = cluster.map_shared_rank(zh, rank + 1) + i;
-#pragma unroll
-                    for (int q = 0; q < RPT; ++q) dst[q] = z[q];
-                }
+                if (first_knot) push_halo_tx<T, RPT>(zh + NP + i, rank - 1, z, tx, 1);
+                if (last_knot) push_halo_tx<T, RPT>(zh + i, rank + 1, z, tx, 1);
                 {
                     A v2[2] = {A(0), A(0)};
 #pragma unroll
@@ -1027,7 +1220,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                         acc_madd(v2[0], r[q], z[q]);
                         if (relres) acc_madd(v2[1], r[q], r[q]);
                     }
-                    cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
+                    solver_allreduce<A, 2>(v2, slots, wscr, 1, tx, cluster, C, rank, halo_in);
                     eta_new = v2[0];
                     rr = v2[1];
                 }
@@ -1060,6 +1253,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             for (int q = 0; q < RPT; ++q) lam_out[(size_t)k * n + i + q] = lam[q];
         }
         if (rank == 0 && tid == 0) {
+            if (C > 1)  // a reduction wait of some CTA of the cluster gave up
+                for (uint32_t c = 0; c < C; ++c)
+                    if (*cluster.map_shared_rank(tx.timed_out, c)) status = ST_TIMEOUT;
             SysResult res;
             res.iters = iter;
             res.status = status;
@@ -1117,6 +1313,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         }
         stamp.done(lp, item, iter);
     }
+    if (C > 1) cluster.sync();  // every transaction-counted store into this CTA has landed
     if constexpr (S_TM) {  // every TMEM access of the CTA is done
         tmem_fence_before_sync();
         __syncthreads();
@@ -1175,7 +1372,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
     T *wh0 = reinterpret_cast<T *>(sp); sp += Plan::halo();         // received w halos, buffer 0
     A *slots = reinterpret_cast<A *>(sp); sp += Plan::slots(C);
     A *wscr = reinterpret_cast<A *>(sp); sp += Plan::wscr(nthr >> 5);
-    uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
+    uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += kItemBytes;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp); sp += Plan::mat_p(lp.kmax);
     T *mh = reinterpret_cast<T *>(sp); sp += PlanSR::mhalo();       // Phi^-1 of the halo knots
@@ -1230,6 +1427,10 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
         const uint32_t R = (K * n + 1) & ~1u;  // row stride of staged matrices (even)
         const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
         const bool first_knot = act && lk == 0 && kb > 0, last_knot = act && lk + 1 == nk && ke < N;
+        if (tid == 0 && nk > 0) {  // this CTA's rows into L2 before they are staged
+            prefetch_l2_range(S + (size_t)kb * blkS, (size_t)nk * blkS * sizeof(T));
+            prefetch_l2_range(P + (size_t)kb * blkP, (size_t)nk * blkP * sizeof(T));
+        }
 
         for (uint32_t e = tid; e < zero_elems; e += nthr) vu[e] = T(0);
         // Phi^-1 blocks of the halo knots (column-major n x n)
@@ -1290,6 +1491,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
         };
         T *my_u = vu + (lk + 1) * NP + i;
         T *my_r = vr + (lk + 1) * NP + i;
+        stage_wait();
         __syncthreads();
         stamp.staged();
 

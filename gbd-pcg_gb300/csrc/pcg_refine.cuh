@@ -53,7 +53,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
     double *wscr64 = reinterpret_cast<double *>(sp); sp += Plan::wscr(nthr >> 5);
     AI *slots = reinterpret_cast<AI *>(slots64);  // the same bytes for the inner reductions
     AI *wscr = reinterpret_cast<AI *>(wscr64);
-    uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += 32;
+    uint32_t *s_item = reinterpret_cast<uint32_t *>(sp); sp += kItemBytes;
     T *ms = reinterpret_cast<T *>(sp); sp += Plan::mat_s(lp.kmax);
     T *mp = reinterpret_cast<T *>(sp); sp += Plan::mat_p(lp.kmax);
     double *vd = reinterpret_cast<double *>(sp);  // FP64 lambda window
@@ -109,6 +109,10 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
         const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
         const bool first_knot = act && lk == 0 && kb > 0, last_knot = act && lk + 1 == nk && ke < N;
         const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
+        if (tid == 0 && nk > 0) {  // this CTA's rows into L2 before they are staged
+            prefetch_l2_range(S64 + (size_t)kb * blkS, (size_t)nk * blkS * sizeof(double));
+            prefetch_l2_range(P + (size_t)kb * blkP, (size_t)nk * blkP * sizeof(T));
+        }
 
         for (uint32_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
         for (uint32_t e = tid; e < zero_d; e += nthr) vd[e] = 0.0;
@@ -156,6 +160,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
         T *my_r = vr + (lk + 1) * NP + i;
         double *my_d = vd + (lk + 1) * NP + i;
 
+        stage_wait();
         __syncthreads();  // rows staged
         stamp.staged();
         double gam[RPT], lam[RPT], r64[RPT];

@@ -24,6 +24,7 @@ enum : int32_t {
     ST_CONVERGED = 0,
     ST_MAX_ITER = 1,
     ST_BREAKDOWN = 2,          // non-finite p.Sp or r.z
+    ST_TIMEOUT = 3,            // a cluster reduction's wait gave up (about a second); results invalid
 };
 
 // One system of a work list.  All pointers are device pointers; element type is

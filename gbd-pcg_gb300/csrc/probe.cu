@@ -1,8 +1,9 @@
 // Latency of the synchronisation primitives one PCG iteration of the cluster
 // solver is built from (gbdpcg_probe_primitives): the CTA barrier, the
 // cluster barrier, a distributed-shared-memory store followed by the cluster
-// barrier, and cluster_allreduce of 1, 2 and 3 values — the reduction the
-// solver itself runs (pcg_cluster.cuh), on the same shared-memory slot layout.
+// barrier, and the cluster-wide reductions of 1, 2 and 3 values the solver
+// runs (pcg_cluster.cuh: cluster_allreduce, and cluster_allreduce_tx, the form
+// the cluster kernels use for C >= 2), on the same shared-memory slot layout.
 // Each probe kernel repeats one primitive `reps` times in a loop whose values
 // depend on the previous repetition (nothing can be hoisted or overlapped),
 // timed with CUDA events around the launch; the loop alone is measured the
@@ -28,7 +29,7 @@ namespace {
 
 using namespace gbdpcg;
 
-enum { PROBE_LOOP = 0, PROBE_SYNCTHREADS = 1, PROBE_CLUSTER = 2, PROBE_DSMEM = 3, PROBE_REDUCE = 4 };
+enum { PROBE_LOOP = 0, PROBE_SYNCTHREADS = 1, PROBE_CLUSTER = 2, PROBE_DSMEM = 3, PROBE_REDUCE = 4, PROBE_REDUCE_TX = 5 };
 
 template <int KIND, int NQ>
 __global__ void probe_kernel(uint32_t reps, float *sink) {
@@ -39,12 +40,21 @@ __global__ void probe_kernel(uint32_t reps, float *sink) {
     float *slots = reinterpret_cast<float *>(smem_raw);
     float *wscr = slots + 2 * kMaxValues * slot_stride(C);
     float *cell = wscr + nwarps * kMaxValues * 32;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(cell + 8);
+    uint32_t *timed_out = reinterpret_cast<uint32_t *>(bar + 2);
     for (uint32_t e = threadIdx.x; e < 2 * kMaxValues * slot_stride(C); e += blockDim.x) slots[e] = 0.f;
-    if (threadIdx.x == 0) cell[0] = 0.f;
+    if (threadIdx.x == 0) {
+        cell[0] = 0.f;
+        *timed_out = 0u;
+        mbar_init(bar, 1);
+        mbar_init(bar + 1, 1);
+        mbar_init_fence();
+    }
     if (C > 1)
         cluster.sync();
     else
         __syncthreads();
+    TxReduce tx{bar, 0u, timed_out};
     float v = (float)(threadIdx.x & 7) * 1e-3f;
     for (uint32_t it = 0; it < reps; ++it) {
         if constexpr (KIND == PROBE_LOOP) {
@@ -61,18 +71,29 @@ __global__ void probe_kernel(uint32_t reps, float *sink) {
             if (threadIdx.x == 0) *cluster.map_shared_rank(cell, (rank + 1) % C) = v;
             cluster.sync();
             v = fmaf(cell[0], 0.5f, v);
-        } else {
+        } else if constexpr (KIND == PROBE_REDUCE) {
             float q[NQ];
 #pragma unroll
             for (int j = 0; j < NQ; ++j) q[j] = v + (float)j;
             cluster_allreduce<float, NQ>(q, slots, wscr, (int)(it & 1), cluster, C, rank);
             v = fmaf(q[0], 1e-9f, v * 0.5f);
+        } else {
+            float q[NQ];
+#pragma unroll
+            for (int j = 0; j < NQ; ++j) q[j] = v + (float)j;
+            cluster_allreduce_tx<float, NQ>(q, slots, wscr, (int)(it & 1), tx, C, rank);
+            v = fmaf(q[0], 1e-9f, v * 0.5f);
         }
     }
-    if (v == 12345.678f) sink[0] = v;  // keeps the chain alive
+    if (*timed_out)
+        sink[0] = 1.f;  // a reduction wait gave up
+    else if (v == 12345.678f)
+        sink[0] = v;  // keeps the chain alive
+    if (C > 1) cluster.sync();  // no CTA leaves while a peer may still store into it
 }
 
 size_t probe_smem(uint32_t C, uint32_t threads) {
+    // slots, warp scratch, then 32 words: a cell, two mbarriers, the timeout flag
     return (2 * kMaxValues * slot_stride(C) + (threads / 32) * kMaxValues * 32 + 32) * sizeof(float);
 }
 
@@ -142,16 +163,23 @@ int gbdpcg_probe_primitives(int device, uint32_t cluster, uint32_t threads, uint
         return probe_fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad device");
     float *sink = nullptr;
     int rc = GBDPCG_SUCCESS;
-    if (cudaMalloc(&sink, sizeof(float)) != cudaSuccess) rc = probe_fail(GBDPCG_ERR_NO_MEMORY, "probe sink");
-    double loop = 0, t[7] = {0, 0, 0, 0, 0, 0, 0};
-    const void *fns[7] = {(const void *)&probe_kernel<PROBE_LOOP, 1>, (const void *)&probe_kernel<PROBE_SYNCTHREADS, 1>,
-                          (const void *)&probe_kernel<PROBE_CLUSTER, 1>, (const void *)&probe_kernel<PROBE_DSMEM, 1>,
-                          (const void *)&probe_kernel<PROBE_REDUCE, 1>, (const void *)&probe_kernel<PROBE_REDUCE, 2>,
-                          (const void *)&probe_kernel<PROBE_REDUCE, 3>};
-    for (int k = 0; k < 7 && rc == GBDPCG_SUCCESS; ++k) {
-        if ((k == 2 || k == 3) && cluster == 1) continue;  // no cluster barrier in a one-CTA cluster
+    if (cudaMalloc(&sink, sizeof(float)) != cudaSuccess || cudaMemset(sink, 0, sizeof(float)) != cudaSuccess)
+        rc = probe_fail(GBDPCG_ERR_NO_MEMORY, "probe sink");
+    double loop = 0, t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const void *fns[10] = {(const void *)&probe_kernel<PROBE_LOOP, 1>, (const void *)&probe_kernel<PROBE_SYNCTHREADS, 1>,
+                           (const void *)&probe_kernel<PROBE_CLUSTER, 1>, (const void *)&probe_kernel<PROBE_DSMEM, 1>,
+                           (const void *)&probe_kernel<PROBE_REDUCE, 1>, (const void *)&probe_kernel<PROBE_REDUCE, 2>,
+                           (const void *)&probe_kernel<PROBE_REDUCE, 3>, (const void *)&probe_kernel<PROBE_REDUCE_TX, 1>,
+                           (const void *)&probe_kernel<PROBE_REDUCE_TX, 2>, (const void *)&probe_kernel<PROBE_REDUCE_TX, 3>};
+    for (int k = 0; k < 10 && rc == GBDPCG_SUCCESS; ++k) {
+        // no cluster barrier in a one-CTA cluster; the transaction-counted reduction is for C >= 2
+        if ((k == 2 || k == 3 || k >= 7) && cluster == 1) continue;
         rc = time_probe(fns[k], cluster, threads, clusters, reps, sink, k == 0 ? &loop : &t[k]);
     }
+    float flag = 0.f;
+    if (rc == GBDPCG_SUCCESS && cudaMemcpy(&flag, sink, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = probe_fail(GBDPCG_ERR_CUDA, "probe read-back");
+    if (rc == GBDPCG_SUCCESS && flag == 1.f) rc = probe_fail(GBDPCG_ERR_CUDA, "probe: a reduction wait timed out");
     if (sink) cudaFree(sink);
     if (prev >= 0 && prev != device) cudaSetDevice(prev);
     if (rc) return rc;
@@ -162,6 +190,7 @@ int gbdpcg_probe_primitives(int device, uint32_t cluster, uint32_t threads, uint
     out->cluster_barrier_ns = cluster > 1 ? net(t[2]) : 0.0;
     out->dsmem_store_barrier_ns = cluster > 1 ? net(t[3]) : 0.0;
     for (int q = 0; q < 3; ++q) out->allreduce_ns[q] = net(t[4 + q]);
+    for (int q = 0; q < 3; ++q) out->allreduce_tx_ns[q] = cluster > 1 ? net(t[7 + q]) : 0.0;
     return GBDPCG_SUCCESS;
 }
 

@@ -74,7 +74,7 @@ class Probe(ctypes.Structure):
     """gbdpcg_probe: ns per repetition of each synchronisation primitive."""
     _fields_ = [("loop_ns", ctypes.c_double), ("syncthreads_ns", ctypes.c_double),
                 ("cluster_barrier_ns", ctypes.c_double), ("dsmem_store_barrier_ns", ctypes.c_double),
-                ("allreduce_ns", ctypes.c_double * 3)]
+                ("allreduce_ns", ctypes.c_double * 3), ("allreduce_tx_ns", ctypes.c_double * 3)]
 
 
 def probe_primitives(device=0, cluster=1, threads=128, clusters=1, reps=100000) -> dict:
@@ -83,7 +83,8 @@ def probe_primitives(device=0, cluster=1, threads=128, clusters=1, reps=100000) 
     _check(lib().gbdpcg_probe_primitives(device, cluster, threads, clusters, reps, ctypes.byref(p)),
            "gbdpcg_probe_primitives")
     return {"loop_ns": p.loop_ns, "syncthreads_ns": p.syncthreads_ns, "cluster_barrier_ns": p.cluster_barrier_ns,
-            "dsmem_store_barrier_ns": p.dsmem_store_barrier_ns, "allreduce_ns": list(p.allreduce_ns)}
+            "dsmem_store_barrier_ns": p.dsmem_store_barrier_ns, "allreduce_ns": list(p.allreduce_ns),
+            "allreduce_tx_ns": list(p.allreduce_tx_ns)}
 
 
 class System(ctypes.Structure):

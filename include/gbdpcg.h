@@ -67,6 +67,8 @@ enum {
     GBDPCG_MAX_ITER = 1,    /* pcg_max_iter passes without meeting it (the reference's
                                d_max_iter_exit, include/pcg.cuh:101,212) */
     GBDPCG_BREAKDOWN = 2,   /* p^T S p or r^T Phi^-1 r not finite */
+    GBDPCG_TIMEOUT = 3,     /* a wait inside the cluster solver's reductions gave up after about a
+                               second; the system's outputs are not valid */
     GBDPCG_REJECTED = -1    /* the system did not fit the launch it was planned into */
 };
 
@@ -422,7 +424,11 @@ typedef struct {
     double syncthreads_ns;          /* __syncthreads */
     double cluster_barrier_ns;      /* barrier.cluster arrive (release) + wait (acquire) */
     double dsmem_store_barrier_ns;  /* one store into the next CTA's shared memory + the cluster barrier */
-    double allreduce_ns[3];         /* the solver's cluster-wide reduction of 1, 2, 3 values */
+    double allreduce_ns[3];         /* cluster-wide reduction of 1, 2, 3 values behind a cluster barrier
+                                       (the form of the single-reduction and refinement kernels) */
+    double allreduce_tx_ns[3];      /* the same reduction by transaction-counted stores (st.async onto
+                                       the receiving CTAs' mbarriers; the form of the cluster kernels
+                                       for cluster >= 2; 0 for cluster = 1) */
 } gbdpcg_probe;
 GBDPCG_API int gbdpcg_probe_primitives(int device, uint32_t cluster, uint32_t threads, uint32_t clusters,
                                        uint32_t reps, gbdpcg_probe *out);

@@ -68,5 +68,7 @@ def test_probe_primitives(gb, handle, C, threads):
         assert p["cluster_barrier_ns"] > 0 and p["dsmem_store_barrier_ns"] > 0
         # a reduction contains a cluster barrier
         assert p["allreduce_ns"][0] >= 0.5 * p["cluster_barrier_ns"]
+        # the transaction-counted form completes (a wait that gave up raises)
+        assert all(x > 0 for x in p["allreduce_tx_ns"])
     with pytest.raises(gb.GbdpcgError):
         gb.probe_primitives(0, 17, threads, 1, 10)

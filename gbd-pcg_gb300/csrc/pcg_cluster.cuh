@@ -285,6 +285,9 @@ __device__ __forceinline__ void hyb_matvec(const T (&Mr)[RPT][2 * NP], const T *
     }
 }
 
+// Rounds of loads the tensor-memory staging keeps in flight ahead of its stores.
+constexpr int kTmemDepth = 3;
+
 // Columns of one row's block in tensor memory (a multiple of 8: x8 moves).
 template <int NP>
 __host__ __device__ constexpr int tmem_cols() { return (NP + 7) / 8 * 8; }
@@ -928,38 +931,40 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 for (int q = 0; q < RPT; ++q)
                     Sr[q][j] = (act && (uint32_t)j < n) ? __ldg(Sk + (n + j) * n + i + q) : T(0);
             __syncwarp();  // tcgen05 stores are warp-wide
-            // one 8-column piece at a time (the loads of a piece are in flight together)
-#pragma unroll 1
-            for (int bi = 0; bi < 2; ++bi) {
-                const int b = 2 * bi;
-                const bool present = act && (b != 0 || k > 0) && (b != 2 || k + 1 < N);
-#pragma unroll 1
-                for (int q = 0; q < RPT; ++q) {
-#pragma unroll 1
-                    for (int cc = 0; cc < NPT / 8; ++cc) {
-                        float v[8];
-#pragma unroll
-                        for (int u = 0; u < 8; ++u) {
-                            const uint32_t j = 8 * cc + u;
-                            v[u] = (present && j < n) ? __ldg(Sk + (b * n + j) * n + i + q) : 0.f;
-                        }
-                        tmem_st8(trow + (q * 3 + bi) * NPT + 8 * cc, v);
-                    }
-                }
-            }
-            // Phi^-1 (compact, n^2 per knot) at columns (3q + 2) NPT
-            const T *Pk = P + (size_t)k * n * n;
-#pragma unroll 1
-            for (int q = 0; q < RPT; ++q) {
-#pragma unroll 1
-                for (int cc = 0; cc < NPT / 8; ++cc) {
-                    float v[8];
+            // The off-diagonal S blocks and Phi^-1 go to TMEM in 8-column pieces
+            // ("rounds": 2 blocks x RPT rows x NPT/8 pieces of S, then RPT x NPT/8
+            // of Phi^-1), each a tcgen05.st of 8 loaded values.  The loads run
+            // kTmemDepth rounds ahead of the stores, so that several rounds' loads
+            // are in flight while a store waits for its values.
+            {
+                constexpr int NC = NPT / 8, RS = 2 * RPT * NC, RR = RS + RPT * NC;
+                const T *Pk = P + (size_t)k * n * n;
+                const bool pres0 = act && k > 0, pres2 = act && k + 1 < N;
+                auto load_round = [&](int r, float (&v)[8]) {
+                    const bool is_s = r < RS;
+                    const int rr = is_s ? r % (RPT * NC) : r - RS;
+                    const int bi = is_s ? r / (RPT * NC) : 0, q = rr / NC, cc = rr % NC;
+                    const bool present = is_s ? (bi == 0 ? pres0 : pres2) : act;
+                    const T *src = is_s ? Sk + (size_t)(2 * bi) * n * n + i + q : Pk + i + q;
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
                         const uint32_t j = 8 * cc + u;
-                        v[u] = (act && j < n) ? __ldg(Pk + j * n + i + q) : 0.f;
+                        v[u] = (present && j < n) ? __ldg(src + (size_t)j * n) : 0.f;
                     }
-                    tmem_st8(trow + (q * 3 + 2) * NPT + 8 * cc, v);
+                };
+                auto col_of = [&](int r) -> uint32_t {
+                    const bool is_s = r < RS;
+                    const int rr = is_s ? r % (RPT * NC) : r - RS;
+                    const int bi = is_s ? r / (RPT * NC) : 2, q = rr / NC, cc = rr % NC;
+                    return (uint32_t)((q * 3 + bi) * NPT + 8 * cc);
+                };
+                float ring[kTmemDepth][8];
+#pragma unroll
+                for (int r = 0; r < kTmemDepth && r < RR; ++r) load_round(r, ring[r]);
+#pragma unroll
+                for (int r = 0; r < RR; ++r) {
+                    tmem_st8(trow + col_of(r), ring[r % kTmemDepth]);
+                    if (r + kTmemDepth < RR) load_round(r + kTmemDepth, ring[r % kTmemDepth]);
                 }
             }
             tmem_wait_st();

@@ -99,7 +99,8 @@ int get_registry(int device, Registry **out) {
                                      variants_np14,     variants_np16,     variants_np24,
                                      variants_np32,     variants_np6_ext,  variants_np8_ext,
                                      variants_np12_ext, variants_np14_ext, variants_np16_ext,
-                                     variants_np24_ext, variants_np32_ext};
+                                     variants_np24_ext, variants_np32_ext,
+                                     variants_stream_small, variants_stream_large};
     for (auto fn : fns) {
         const int c = fn(buf);
         for (int i = 0; i < c; ++i) {
@@ -205,14 +206,21 @@ struct Pref {
     int st, rpt;
 };
 
+// A launch shape of the streamed storage may give a thread several row groups,
+// so its CTA needs no thread per row (any CTA size holds the system).
+bool streamed(int st) { return st == 5; }  // pcg_cluster.cuh ST_STREAM
+
 std::vector<Pref> storage_prefs(bool f64, bool ptri, uint32_t storage) {
+    if (storage == GBDPCG_STORAGE_STREAM) return f64 || ptri ? std::vector<Pref>{{5, 1}} : std::vector<Pref>{{5, 2}, {5, 1}};
     if (storage == GBDPCG_STORAGE_REGISTERS) return {{0, 1}, {0, 2}};
     if (storage == GBDPCG_STORAGE_SHARED) return {{2, 1}};
     if (storage == GBDPCG_STORAGE_SPLIT) return ptri ? std::vector<Pref>{} : std::vector<Pref>{{1, 2}, {1, 1}};
     if (storage == GBDPCG_STORAGE_HYBRID) return ptri ? std::vector<Pref>{} : std::vector<Pref>{{3, 2}, {3, 1}};
     if (storage == GBDPCG_STORAGE_TMEM) return ptri || f64 ? std::vector<Pref>{} : std::vector<Pref>{{4, 2}};
-    if (f64) return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{0, 1}, {1, 1}, {2, 1}};
-    return ptri ? std::vector<Pref>{{0, 1}, {2, 1}} : std::vector<Pref>{{1, 2}, {0, 1}, {1, 1}, {2, 1}, {3, 2}, {3, 1}};
+    // AUTO: rows on chip where they fit; streamed rows for larger systems
+    if (f64) return ptri ? std::vector<Pref>{{0, 1}, {2, 1}, {5, 1}} : std::vector<Pref>{{0, 1}, {1, 1}, {2, 1}, {5, 1}};
+    return ptri ? std::vector<Pref>{{0, 1}, {2, 1}, {5, 1}}
+                : std::vector<Pref>{{1, 2}, {0, 1}, {1, 1}, {2, 1}, {3, 2}, {3, 1}, {5, 2}, {5, 1}};
 }
 
 // A tuned shape for one system, if its variant exists and holds the system.
@@ -223,7 +231,7 @@ bool tuned_shape(Registry *reg, bool f64, int acc, int np, bool ptri, uint32_t n
     if (!vi) return false;
     const uint32_t K = (N + tc.C - 1) / tc.C;
     const uint32_t thr = (K * n + tc.rpt - 1) / tc.rpt;
-    if (thr > tc.threads || tc.threads > (uint32_t)vi->max_threads) return false;
+    if ((!streamed(tc.st) && thr > tc.threads) || tc.threads > (uint32_t)vi->max_threads) return false;
     if (vi->v.smem_bytes(K, tc.C, tc.threads / 32) > (size_t)reg->max_smem_optin) return false;
     out->vi = vi;
     out->C = tc.C;
@@ -297,15 +305,19 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
                 if (C > 8 && (C & (C - 1))) continue;  // large clusters: powers of two only
                 const uint32_t K = (N + C - 1) / C;
                 const uint32_t thr = (K * n + pf.rpt - 1) / pf.rpt;
-                if (thr > cap) continue;
-                if (vi->v.smem_bytes(K, C, 32) > (size_t)reg->max_smem_optin) continue;
+                if (thr > cap && !streamed(pf.st)) continue;
+                // CTA sizes are rounded to 64 threads so that systems of similar
+                // size share a launch (streamed rows: up to the cap, in row groups)
+                uint32_t threads = std::min<uint32_t>(cap, std::max<uint32_t>(64, (thr + 63) / 64 * 64));
+                if (threads < thr && !streamed(pf.st)) threads = (thr + 31) / 32 * 32;
+                // shared memory at the largest CTA the class may get (streamed rows:
+                // at this CTA, whose vectors are what bound the system)
+                const uint32_t chk_warps = streamed(pf.st) ? threads / 32 : 32;
+                if (vi->v.smem_bytes(K, C, chk_warps) > (size_t)reg->max_smem_optin) continue;
                 s.vi = vi;
                 s.C = C;
                 s.K = K;
-                // CTA sizes are rounded to 64 threads so that systems of similar
-                // size share a launch
-                s.threads = std::min<uint32_t>(cap, std::max<uint32_t>(64, (thr + 63) / 64 * 64));
-                if (s.threads < thr) s.threads = (thr + 31) / 32 * 32;
+                s.threads = threads;
                 *out = s;
                 return GBDPCG_SUCCESS;
             }
@@ -396,7 +408,7 @@ int check_cfg(const gbdpcg_config *cfg, uint32_t layout) {
     if (!cfg) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "config is NULL");
     if (layout > GBDPCG_PINV_BLOCKDIAG) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad pinv_layout");
     if (cfg->exit_mode > GBDPCG_EXIT_RELRES || cfg->dot_precision > GBDPCG_DOT_FLOAT2 ||
-        cfg->algorithm > GBDPCG_ALGO_RECURRENCE || cfg->storage > GBDPCG_STORAGE_TMEM ||
+        cfg->algorithm > GBDPCG_ALGO_RECURRENCE || cfg->storage > GBDPCG_STORAGE_STREAM ||
         cfg->cluster_size > 16 || cfg->max_threads > 1024 || cfg->zero_guess > 1 ||
         !(cfg->inner_tol >= 0) || cfg->inner_tol >= 1)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad config field");
@@ -1506,6 +1518,7 @@ std::vector<Candidate> tune_candidates(gbdpcg_plan_s *p, const PlanClass &base,
                         : p->cfg.storage == GBDPCG_STORAGE_SPLIT   ? 1
                         : p->cfg.storage == GBDPCG_STORAGE_HYBRID  ? 3
                         : p->cfg.storage == GBDPCG_STORAGE_TMEM    ? 4
+                        : p->cfg.storage == GBDPCG_STORAGE_STREAM  ? 5
                                                                    : -1;
     static const uint32_t kC[] = {1, 2, 3, 4, 5, 6, 7, 8, 16};
     for (auto &vi : reg->list) {
@@ -1529,7 +1542,8 @@ std::vector<Candidate> tune_candidates(gbdpcg_plan_s *p, const PlanClass &base,
                 kmax = std::max(kmax, K);
                 thr = std::max(thr, (K * n + v.rpt - 1) / v.rpt);
             }
-            const uint32_t threads = (thr + 31) / 32 * 32;
+            uint32_t threads = (thr + 31) / 32 * 32;
+            if (streamed(v.st)) threads = std::min(threads, cap / 32 * 32);  // row groups beyond the cap
             if (!ok || threads > cap) continue;
             if (v.smem_bytes(kmax, C, threads / 32) > (size_t)reg->max_smem_optin) continue;
             Candidate cd;

@@ -53,7 +53,9 @@ __host__ __device__ constexpr size_t round_up(size_t x, size_t m) { return (x + 
 // block of S and Phi^-1 (block-diagonal) in shared memory; ST_TMEM the
 // diagonal block of S in registers, its two off-diagonal blocks and Phi^-1
 // (block-diagonal) in tensor memory.
-enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2, ST_HYB = 3, ST_TMEM = 4 };
+// ST_STREAM (pcg_stream.cuh): no storage; the rows are read from global memory
+// in every product.
+enum : int { ST_REG = 0, ST_REG_S = 1, ST_SMEM = 2, ST_HYB = 3, ST_TMEM = 4, ST_STREAM = 5 };
 
 // A CTA of the tensor-memory storage allocates all of its SM's tensor memory;
 // it asks for more than half an SM's shared memory so that no second such CTA

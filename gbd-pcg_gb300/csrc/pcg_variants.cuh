@@ -3,6 +3,7 @@
 #pragma once
 #include "pcg_cluster.cuh"
 #include "pcg_refine.cuh"
+#include "pcg_stream.cuh"
 #include "pcg_variants.h"
 
 #define GBDPCG_VARIANT(T, A, NP, PTRI, ST, RPT)                                               \
@@ -95,6 +96,20 @@
 #define GBDPCG_VARIANTS_HYB_RPT2(NP)                                                          \
     out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_HYB, 2);                            \
     out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_HYB, 2);
+// Streamed rows (read from global memory in every product): FP32 with a compact
+// Phi^-1 (one or two rows per thread) or a cbtd one, FP64 with either.
+#define GBDPCG_VARIANT_STREAM(T, A, NP, PTRI, RPT)                                            \
+    ::gbdpcg::KernelVariant {                                                                 \
+        sizeof(T) == 8, ::gbdpcg::acc_code<T, A>(), NP, PTRI, ::gbdpcg::ST_STREAM, RPT, 0,    \
+            (const void *)&::gbdpcg::pcg_stream_kernel<T, A, NP, PTRI, RPT>,                  \
+            &::gbdpcg::SmemPlanStream<T, A, NP, PTRI>::bytes                                  \
+    }
+#define GBDPCG_VARIANTS_STREAM(NP)                                                            \
+    out[c++] = GBDPCG_VARIANT_STREAM(float, float, NP, false, 1);                             \
+    out[c++] = GBDPCG_VARIANT_STREAM(float, float, NP, false, 2);                             \
+    out[c++] = GBDPCG_VARIANT_STREAM(float, float, NP, true, 1);                              \
+    out[c++] = GBDPCG_VARIANT_STREAM(double, double, NP, false, 1);                           \
+    out[c++] = GBDPCG_VARIANT_STREAM(double, double, NP, true, 1);
 // Tensor-memory storage (diagonal S block in registers, off-diagonal blocks in
 // TMEM, Phi^-1 in shared memory), two rows per thread, standard and recurrence forms.
 #define GBDPCG_VARIANTS_TMEM(NP)                                                              \

@@ -11,7 +11,8 @@ struct KernelVariant {
     int np;      // compile-time block-size bound (n <= np)
     int ptri;    // Phi^-1 block-tridiagonal (cbtd) instead of block-diagonal
     int st;      // storage: 0 S and Phi^-1 in registers, 1 S in registers and Phi^-1 in
-                 // shared memory, 2 both in shared memory
+                 // shared memory, 2 both in shared memory, 3 hybrid, 4 tensor memory,
+                 // 5 streamed from global memory
     int rpt;     // matrix rows per thread (2 needs an even n)
     int alg;     // 0 two reductions per iteration, 1 single reduction (block-diagonal Phi^-1),
                  // 2 FP32 inner PCG with FP64 refinement, 3 recurrence form (three barriers
@@ -36,6 +37,8 @@ int variants_np14_ext(KernelVariant *out);
 int variants_np16_ext(KernelVariant *out);
 int variants_np24_ext(KernelVariant *out);
 int variants_np32_ext(KernelVariant *out);
+int variants_stream_small(KernelVariant *out);  // streamed rows, NP 6..14
+int variants_stream_large(KernelVariant *out);  // streamed rows, NP 16..32
 
 const void *plain_kernel_ptr(bool f64);
 size_t plain_smem_bytes(bool f64, uint32_t n, uint32_t N);

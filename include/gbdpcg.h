@@ -17,10 +17,12 @@
  * present as padding and never read.  A block-diagonal Phi^-1 may instead be
  * given compactly: n^2 per knot, column-major.  Vectors are n*N, knot-major.
  *
- * Supported sizes: 1 <= n <= 32 on the cluster solver (any N up to what 16
- * CTAs hold); larger n, and systems past that with a cbtd Phi^-1, run the
- * plain algorithm (one CTA per knot, all N co-resident); past both a call
- * returns GBDPCG_ERR_UNSUPPORTED before launching anything.
+ * Supported sizes: 1 <= n <= 32 on the cluster solver: with the rows on chip
+ * up to what 16 CTAs hold, with streamed rows up to the knots whose vectors
+ * (three per knot) fit 16 CTAs' shared memory (n = 14 FP32: about 21000 knots;
+ * n = 24 FP64: about 6000); larger n runs the plain algorithm (one CTA per
+ * knot, all N co-resident); past those a call returns GBDPCG_ERR_UNSUPPORTED
+ * before launching anything.
  *
  * Groups of entry points: single solves (host arrays, device pointers),
  * batched plans (graph replay, autotuner and its table, end-to-end pipelines
@@ -107,14 +109,18 @@ enum {
  * block and Phi^-1 in shared memory (more rows per SM; FP32, block-diagonal
  * Phi^-1); TMEM: the diagonal block of S in registers, its off-diagonal
  * blocks in the SM's tensor memory, Phi^-1 in shared memory (the most rows
- * per SM; FP32, block-diagonal Phi^-1, even n; one CTA per SM) */
+ * per SM; FP32, block-diagonal Phi^-1, even n; one CTA per SM); STREAM: no
+ * storage, the rows are read from global memory (L2 or HBM) in every
+ * product, so a cluster holds any system whose vectors fit its shared memory
+ * (three vectors of its knots; AUTO's last choice before the plain algorithm) */
 enum {
     GBDPCG_STORAGE_AUTO = 0,
     GBDPCG_STORAGE_REGISTERS = 1,
     GBDPCG_STORAGE_SHARED = 2,
     GBDPCG_STORAGE_SPLIT = 3,
     GBDPCG_STORAGE_HYBRID = 4,
-    GBDPCG_STORAGE_TMEM = 5
+    GBDPCG_STORAGE_TMEM = 5,
+    GBDPCG_STORAGE_STREAM = 6
 };
 
 typedef struct {

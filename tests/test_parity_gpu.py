@@ -478,11 +478,11 @@ def test_maximum_sizes(gb, oracle_mod, handle, dts, n, N, seed):
 
 
 def test_too_large_is_reported(gb, handle):
-    """n = 14, N = 20000: no cluster shape holds it (1250 knots a CTA) and the
-    plain kernel's 20000 CTAs cannot be co-resident, so the call returns
-    UNSUPPORTED before any launch, and the handle stays usable.  (n = 6,
-    N = 4096 with a cbtd Phi^-1 is past both limits too.)"""
-    n, N = 14, 20000
+    """n = 14, N = 40000: even with streamed rows no cluster shape holds it
+    (2500 knots a CTA: three vectors of 140 KB each exceed a CTA's shared
+    memory) and the plain kernel's 40000 CTAs cannot be co-resident, so the
+    call returns UNSUPPORTED before any launch, and the handle stays usable."""
+    n, N = 14, 40000
     S = np.zeros(3 * n * n * N, np.float32)
     P = np.zeros_like(S)
     g = np.ones(n * N, np.float32)

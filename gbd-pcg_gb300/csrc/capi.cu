@@ -262,11 +262,35 @@ uint32_t lone_cluster_pref(bool f64_rows, uint32_t N) {
     return std::min<uint32_t>(16, p);
 }
 
+// Whether the plain algorithm's N CTAs of 64 threads can all be resident at
+// once (its cooperative launch needs that).
+bool plain_fits(Registry *reg, bool f64, uint32_t n, uint32_t N) {
+    const size_t smem = plain_smem_bytes(f64, n, N);
+    if (smem > (size_t)reg->max_smem_optin) return false;
+    const void *func = plain_kernel_ptr(f64);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, func, 64, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return (int64_t)per_sm * reg->sm_count >= (int64_t)N;
+}
+
 // c_pref > 1 (lone systems, cluster size not pinned): clusters from c_pref up
-// are tried first, then the smallest that fits.
+// are tried first, then the smallest that fits.  `lone`: a single system
+// solved by itself.  For such a system with a cbtd Phi^-1 that no on-chip
+// shape holds, AUTO prefers the plain algorithm (all SMs, one CTA per knot)
+// to streamed rows (one cluster of at most 16 SMs) whenever the plain
+// kernel's CTAs fit at once; batches take streamed rows, which keep the whole
+// batch in one persistent launch.
 int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layout,
                  const gbdpcg_config &cfg, Shape *out, bool refine = false,
-                 const TuneChoice *tuned = nullptr, uint32_t c_pref = 1) {
+                 const TuneChoice *tuned = nullptr, uint32_t c_pref = 1, bool lone = false) {
     Shape s;
     const int np = np_for(n);
     if (refine) {
@@ -295,6 +319,12 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
     for (uint32_t from : {first_lo, 1u}) {
         for (const Pref &pf : storage_prefs(f64 && !refine, ptri, cfg.storage)) {
             if (pf.rpt > 1 && (n % pf.rpt) != 0) continue;
+            if (streamed(pf.st) && lone && ptri && cfg.storage == GBDPCG_STORAGE_AUTO &&
+                cfg.algorithm == GBDPCG_ALGO_AUTO && cfg.cluster_size == 0 && plain_fits(reg, f64, n, N)) {
+                s.plain = true;
+                *out = s;
+                return GBDPCG_SUCCESS;
+            }
             VariantInfo *vi = find_variant(reg, f64 && !refine, acc, np, ptri, pf.st, pf.rpt, alg);
             if (!vi) continue;
             uint32_t cap = cfg.max_threads ? cfg.max_threads : (uint32_t)vi->max_threads;
@@ -506,7 +536,7 @@ int solve_one(gbdpcg_handle_s *h, bool f64, const SysDesc &d0, const gbdpcg_conf
     d.result = 0;
     Shape sh;
     rc = choose_shape(h->reg, f64, d.n, d.N, layout, cfg, &sh, refine, nullptr,
-                      lone_cluster_pref(f64 && !refine, d.N));
+                      lone_cluster_pref(f64 && !refine, d.N), true);
     if (rc) return rc;
     h->d_last = d_res;
     h->last_stream = stream;

@@ -555,13 +555,27 @@ def adjoint_config(gbdpcg, h, dev, tune_flags=None, count=1024, n=14, N=64):
     t_f = timeit(pf.execute)
     t_a = timeit(pa.execute)
     res_a = pa.results()
+    # forward + adjoint in one launch per class (gbdpcg_plan_create_fwd_adj):
+    # the rows are staged once for both solves
+    pairs = [{"S": f["S"], "Pinv": f["Pinv"], "gamma": f["gamma"], "lambda": torch.zeros_like(f["lambda"]),
+              "lambda_target": a["star"], "grad_gamma": torch.empty_like(f["lambda"]),
+              "grad_S": torch.empty_like(f["S"]), "n": n, "N": N} for f, a in zip(fwd, adj)]
+    pj = gbdpcg.Plan.forward_adjoint(h, pairs, gbdpcg.PINV_BLOCKDIAG, cfg)
+    if tune_flags is not None:
+        pj.autotune(flags=tune_flags)
+    t_j = timeit(pj.execute)
+    res_j = pj.results()
     out = {"systems": count, "n": n, "N": N, "forward_ms": t_f, "adjoint_ms": t_a,
            "forward_plus_adjoint_over_forward": (t_f + t_a) / t_f,
            "adjoint_all_converged": all(r.status == 0 for r in res_a),
+           "fused_ms": t_j, "fused_over_forward": t_j / t_f,
+           "fused_all_converged": all(r.status == 0 for r in res_j),
            "autotuned": tune_flags is not None,
-           "note": "adjoint = PCG solve of S mu = lambda - lambda* plus the fused dS, dgamma epilogue"}
+           "note": "adjoint = PCG solve of S mu = lambda - lambda* plus the dS, dgamma epilogue; fused = "
+                   "forward and adjoint solves and the epilogue in one launch (gbdpcg_plan_create_fwd_adj)"}
     pf.close()
     pa.close()
+    pj.close()
     return out
 
 

@@ -603,6 +603,10 @@ struct gbdpcg_plan_s {
     cudaStream_t build_stream = nullptr;  // highest priority: the Phi^-1 builds of solve_host
     std::vector<cudaStream_t> piece_streams;
     std::vector<cudaEvent_t> piece_events;  // [copied i], [solved i], start, [built i]
+    // forward + adjoint pairs (gbdpcg_plan_create_fwd_adj): results [0, count)
+    // are the forward solves', [count, 2 count) the adjoint solves'
+    bool fused = false;
+    uint32_t nresults = 0;
     // timeline (gbdpcg_plan_timeline): one record per work-list item, and the
     // SM of every CTA of every launch (launch c's CTAs from cta_off[c])
     bool timeline = false;
@@ -623,7 +627,8 @@ struct gbdpcg_plan_s {
 
 namespace {
 
-TuneKey tune_key(const gbdpcg_plan_s *p, bool adjoint, uint32_t n, uint32_t N) {
+// adjoint: 0 forward solves, 1 adjoint solves, 2 forward + adjoint pairs
+TuneKey tune_key(const gbdpcg_plan_s *p, uint8_t adjoint, uint32_t n, uint32_t N) {
     TuneKey k;
     memset(&k, 0, sizeof(k));
     k.f64 = p->f64;
@@ -1021,8 +1026,15 @@ int gbdpcg_adjoint_dev_f32(gbdpcg_handle_t h, const float *d_S, const float *d_P
 }
 
 // ---- plans
-int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *systems, uint32_t count,
-                       uint32_t pinv_layout, const gbdpcg_config *cfg, gbdpcg_plan_t *plan) {
+}  // extern "C"
+
+namespace {
+
+// Builds a plan.  With `fa`, every system is a forward + adjoint pair (the
+// forward fields are in `systems`, the adjoint's outputs and lambda* in fa).
+int plan_create_impl(gbdpcg_handle_t h, int dtype, const gbdpcg_system *systems, uint32_t count,
+                     uint32_t pinv_layout, const gbdpcg_config *cfg, gbdpcg_plan_t *plan,
+                     const gbdpcg_fwd_adj_system *fa) {
     if (!h || !systems || !plan || count == 0)
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer or empty batch");
     if (dtype < 0 || dtype > 2) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "dtype must be 0, 1 or 2");
@@ -1038,6 +1050,9 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
     p->layout = pinv_layout;
     p->cfg = *cfg;
     p->count = count;
+    p->fused = fa != nullptr;
+    p->nresults = fa ? 2 * count : count;
+    if (fa && p->refine) return fail(GBDPCG_ERR_UNSUPPORTED, "no adjoint of a refined solve");
     const bool adjoint = systems[0].lambda_fwd != nullptr;
     std::map<std::tuple<const void *, uint32_t, uint32_t>, uint32_t> class_of;
     std::vector<uint64_t> prefix(count);
@@ -1059,6 +1074,17 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
             d.dS = s.dS;
         }
         if (p->refine) d.flags |= SYS_REFINE;
+        if (fa) {
+            const gbdpcg_fwd_adj_system &f = fa[i];
+            if (!f.lambda_target || !f.grad_gamma || !f.grad_S)
+                return fail(GBDPCG_ERR_INVALID_ARGUMENT, "system " + std::to_string(i) + " is incomplete");
+            d.flags |= SYS_FWD_ADJ;
+            d.lstar = f.lambda_target;
+            d.mu = f.grad_gamma;
+            d.dS = f.grad_S;
+            d.lam_fwd = f.lambda;  // the epilogue's forward solution is the lambda output
+            d.result_adj = count + i;
+        }
         prefix[i] = p->total_knots;
         p->total_knots += s.N;
         p->descs.push_back(d);
@@ -1066,7 +1092,7 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
         const TuneChoice *tc = nullptr;
         TuneChoice tcv;
         if (use_table) {
-            auto tt = h->tune.find(tune_key(p.get(), adjoint, s.n, s.N));
+            auto tt = h->tune.find(tune_key(p.get(), fa ? 2 : (adjoint ? 1 : 0), s.n, s.N));
             if (tt != h->tune.end()) {
                 tcv = tt->second;
                 tc = &tcv;
@@ -1074,6 +1100,9 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
         }
         rc = choose_shape(h->reg, p->f64, s.n, s.N, pinv_layout, *cfg, &sh, p->refine, tc);
         if (rc) return rc;
+        if (fa && (sh.plain || streamed(sh.vi->v.st)))
+            return fail(GBDPCG_ERR_UNSUPPORTED, "a forward + adjoint pair needs the rows on chip (system " +
+                                                    std::to_string(i) + ")");
         if (sh.plain) {
             if (adjoint) return fail(GBDPCG_ERR_UNSUPPORTED, "adjoint needs n <= 32");
             p->plain_items.push_back(i);
@@ -1093,11 +1122,11 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
     }
     tune_lock.unlock();
     if ((rc = p->d_descs.ensure(sizeof(SysDesc) * count))) return rc;
-    if ((rc = p->d_results.ensure(sizeof(SysResult) * count))) return rc;
+    if ((rc = p->d_results.ensure(sizeof(SysResult) * p->nresults))) return rc;
     if ((rc = p->d_prefix.ensure(sizeof(uint64_t) * count))) return rc;
     GB_CUDA(cudaMemcpy(p->d_descs.p, p->descs.data(), sizeof(SysDesc) * count, cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(p->d_prefix.p, prefix.data(), sizeof(uint64_t) * count, cudaMemcpyHostToDevice));
-    GB_CUDA(cudaMemset(p->d_results.p, 0, sizeof(SysResult) * count));
+    GB_CUDA(cudaMemset(p->d_results.p, 0, sizeof(SysResult) * p->nresults));
     if ((rc = plan_layout(p.get()))) return rc;
     const size_t nc = p->classes.size();
     const uint32_t ns = (uint32_t)std::min<size_t>(std::max<uint32_t>(1, std::min<uint32_t>(cfg->streams, 32)),
@@ -1114,6 +1143,28 @@ int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *system
     }
     *plan = p.release();
     return GBDPCG_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_system *systems, uint32_t count,
+                       uint32_t pinv_layout, const gbdpcg_config *cfg, gbdpcg_plan_t *plan) {
+    return plan_create_impl(h, dtype, systems, count, pinv_layout, cfg, plan, nullptr);
+}
+
+int gbdpcg_plan_create_fwd_adj(gbdpcg_handle_t h, int dtype, const gbdpcg_fwd_adj_system *systems,
+                               uint32_t count, uint32_t pinv_layout, const gbdpcg_config *cfg,
+                               gbdpcg_plan_t *plan) {
+    if (!systems || count == 0) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer or empty batch");
+    if (dtype != 0 && dtype != 1) return fail(GBDPCG_ERR_UNSUPPORTED, "forward + adjoint pairs are float or double");
+    std::vector<gbdpcg_system> fwd(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const gbdpcg_fwd_adj_system &f = systems[i];
+        fwd[i] = gbdpcg_system{f.S, f.Pinv, f.gamma, f.lambda, nullptr, nullptr, f.n, f.N};
+    }
+    return plan_create_impl(h, dtype, fwd.data(), count, pinv_layout, cfg, plan, systems);
 }
 
 int gbdpcg_plan_execute(gbdpcg_plan_t p, gbdpcg_stream_t stream_) {
@@ -1412,11 +1463,11 @@ int gbdpcg_plan_build_block_jacobi(gbdpcg_plan_t p, gbdpcg_stream_t stream) {
 int gbdpcg_plan_results(gbdpcg_plan_t p, gbdpcg_result *results, gbdpcg_stream_t stream) {
     if (!p || !results) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
     HandleScope scope(p->h->device);
-    std::vector<SysResult> r(p->count);
-    GB_CUDA(cudaMemcpyAsync(r.data(), p->d_results.p, sizeof(SysResult) * p->count,
+    std::vector<SysResult> r(p->nresults);
+    GB_CUDA(cudaMemcpyAsync(r.data(), p->d_results.p, sizeof(SysResult) * p->nresults,
                             cudaMemcpyDeviceToHost, (cudaStream_t)stream));
     GB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
-    for (uint32_t i = 0; i < p->count; ++i) to_public(r[i], &results[i]);
+    for (uint32_t i = 0; i < p->nresults; ++i) to_public(r[i], &results[i]);
     return GBDPCG_SUCCESS;
 }
 
@@ -1607,7 +1658,8 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
     HandleScope scope(p->h->device);
     cudaStream_t st = (cudaStream_t)stream_;
     if (reps == 0) reps = 2;
-    const bool adjoint = (p->descs[0].flags & SYS_ADJOINT) != 0;
+    const bool adjoint = (p->descs[0].flags & (SYS_ADJOINT | SYS_FWD_ADJ)) != 0;
+    const bool fused = p->fused;  // also a mu output per system
     const size_t sv = (p->f64 || p->refine) ? 8 : 4;  // lambda element (refinement: double)
     const size_t sS = p->f64 ? 8 : 4;                 // dS element (adjoint: the plan's type)
     // scratch for the largest class: lambda (and dS) of each of its systems
@@ -1616,7 +1668,7 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
         size_t b = 0;
         for (uint32_t i : pc.items) {
             const size_t n = p->descs[i].n, N = p->descs[i].N;
-            b += round_up(n * N * sv, 256) + (adjoint ? round_up(3 * n * n * N * sS, 256) : 0);
+            b += round_up(n * N * sv, 256) * (fused ? 2 : 1) + (adjoint ? round_up(3 * n * n * N * sS, 256) : 0);
         }
         need = std::max(need, b);
     }
@@ -1626,7 +1678,7 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
     if ((rc = d_td.ensure(sizeof(SysDesc) * p->count))) return rc;
     if ((rc = d_ord.ensure(sizeof(uint32_t) * p->count))) return rc;
     if ((rc = d_q.ensure(sizeof(uint32_t)))) return rc;
-    if ((rc = d_res.ensure(sizeof(SysResult) * p->count))) return rc;
+    if ((rc = d_res.ensure(sizeof(SysResult) * p->nresults))) return rc;
     cudaEvent_t e0, e1;
     GB_CUDA(cudaEventCreate(&e0));
     cudaError_t ce = cudaEventCreate(&e1);
@@ -1674,6 +1726,11 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
             if (adjoint) {
                 d.dS = base + off;
                 off += round_up(3 * n * n * N * sS, 256);
+            }
+            if (fused) {
+                d.lam_fwd = d.lambda;
+                d.mu = base + off;
+                off += round_up(n * N * sv, 256);
             }
         }
         GB_CUDA(cudaMemcpyAsync(d_td.p, td.data(), sizeof(SysDesc) * p->count, cudaMemcpyHostToDevice, st));
@@ -1729,7 +1786,7 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
         pc.sh = best.sh;
         pc.kmax = best.kmax;
         TuneChoice ch{best.sh.vi->v.st, best.sh.vi->v.rpt, best.sh.vi->v.alg, best.sh.C, best.sh.threads};
-        for (uint32_t i : pc.items) learned.emplace_back(tune_key(p, adjoint, p->descs[i].n, p->descs[i].N), ch);
+        for (uint32_t i : pc.items) learned.emplace_back(tune_key(p, fused ? 2 : (adjoint ? 1 : 0), p->descs[i].n, p->descs[i].N), ch);
         for (uint32_t i : pc.items) td[i] = p->descs[i];
     }
     GB_CUDA(cudaStreamSynchronize(st));

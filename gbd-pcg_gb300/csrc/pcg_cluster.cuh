@@ -1051,18 +1051,31 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         __syncthreads();
         stamp.staged();
 
-        // ---- r = gamma - S lambda0   (include/pcg.cuh:119-126)
+        // Phase 0 solves S lambda = gamma.  With SYS_FWD_ADJ, phase 1 then solves
+        // the adjoint system S mu = lambda - lambda* from mu = 0 on the rows
+        // still on chip (S is symmetric), with lambda re-read from its output.
+        const bool fused = (d.flags & SYS_FWD_ADJ) != 0;
+        T *lam_out = static_cast<T *>(d.lambda);
+        const T *lstar = static_cast<const T *>(d.lstar);
         T gam[RPT], lam[RPT], r[RPT], p[RPT], z[RPT], y[RPT];
+        uint32_t iters_all = 0;
+        for (uint32_t phase = 0;; ++phase) {
+        if (phase == 1) {  // the forward solve's windows and halos start the adjoint at zero
+            for (uint32_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
+        }
+        const T *lam_init = phase == 0 ? lam0 : nullptr;
+        // ---- r = gamma - S lambda0   (include/pcg.cuh:119-126)
 #pragma unroll
         for (int q = 0; q < RPT; ++q) {
-            gam[q] = act ? gamma[(size_t)k * n + i + q] : T(0);
-            lam[q] = (act && lam0) ? lam0[(size_t)k * n + i + q] : T(0);
+            const size_t row = (size_t)k * n + i + q;
+            gam[q] = act ? (phase == 0 ? gamma[row] : lam_out[row] - lstar[row]) : T(0);
+            lam[q] = (act && lam_init) ? lam_init[row] : T(0);
             if (act) my_p[q] = lam[q];
         }
-        if (lam0) {
+        if (lam_init) {
             for (uint32_t t = tid; t < 2 * n; t += nthr) {
-                if (t < n && has_left) vp[t] = lam0[(size_t)(kb - 1) * n + t];
-                if (t >= n && has_right) vp[(nk + 1) * NP + (t - n)] = lam0[(size_t)ke * n + (t - n)];
+                if (t < n && has_left) vp[t] = lam_init[(size_t)(kb - 1) * n + t];
+                if (t >= n && has_right) vp[(nk + 1) * NP + (t - n)] = lam_init[(size_t)ke * n + (t - n)];
             }
         }
         __syncthreads();
@@ -1254,10 +1267,10 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
 
         // ---- outputs   (include/pcg.cuh:212-217)
         stamp.solved();
-        T *lam_out = static_cast<T *>(d.lambda);
+        T *sol_out = phase == 0 ? lam_out : static_cast<T *>(d.mu);
         if (act) {
 #pragma unroll
-            for (int q = 0; q < RPT; ++q) lam_out[(size_t)k * n + i + q] = lam[q];
+            for (int q = 0; q < RPT; ++q) sol_out[(size_t)k * n + i + q] = lam[q];
         }
         if (rank == 0 && tid == 0) {
             if (C > 1)  // a reduction wait of some CTA of the cluster gave up
@@ -1271,11 +1284,16 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             res.gg = (double)gg;
             res.outer = 0;
             res.pad = 0;
-            lp.results[d.result] = res;
+            lp.results[phase == 0 ? d.result : d.result_adj] = res;
         }
+        iters_all += iter;
+        if (phase == 0 && fused) continue;
+        break;
+        }  // phase
 
         // ---- adjoint epilogue: dS = -1/2 (mu lam^T + lam mu^T) on the block pattern
-        if (d.flags & SYS_ADJOINT) {
+        // (after a forward + adjoint pair too: lam_fwd is then the lambda output)
+        if (d.flags & (SYS_ADJOINT | SYS_FWD_ADJ)) {
             const T *lf = static_cast<const T *>(d.lam_fwd);
             T *dS = static_cast<T *>(d.dS);
             group_sync(cluster, C);  // vp / vr free in every CTA
@@ -1318,7 +1336,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 }
             }
         }
-        stamp.done(lp, item, iter);
+        stamp.done(lp, item, iters_all);
     }
     if (C > 1) cluster.sync();  // every transaction-counted store into this CTA has landed
     if constexpr (S_TM) {  // every TMEM access of the CTA is done
@@ -1408,7 +1426,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
         const uint32_t n = d.n, N = d.N;
         const uint32_t K = (N + C - 1) / C;
         if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (size_t)K * n > (size_t)nthr * RPT ||
-            (RPT > 1 && (n % RPT) != 0) || (d.flags & (SYS_PINV_TRI | SYS_ADJOINT))) {
+            (RPT > 1 && (n % RPT) != 0) || (d.flags & (SYS_PINV_TRI | SYS_ADJOINT | SYS_FWD_ADJ))) {
             if (rank == 0 && tid == 0) {
                 SysResult res = {};
                 res.status = -1;

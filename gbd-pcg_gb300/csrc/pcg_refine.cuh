@@ -83,7 +83,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
         const uint32_t n = d.n, N = d.N;
         const uint32_t K = (N + C - 1) / C;
         if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (size_t)K * n > (size_t)nthr * RPT ||
-            (RPT > 1 && (n % RPT) != 0) || (d.flags & (SYS_PINV_TRI | SYS_ADJOINT))) {
+            (RPT > 1 && (n % RPT) != 0) || (d.flags & (SYS_PINV_TRI | SYS_ADJOINT | SYS_FWD_ADJ))) {
             if (rank == 0 && tid == 0) {
                 SysResult res = {};
                 res.status = -1;

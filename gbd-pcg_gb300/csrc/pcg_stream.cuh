@@ -123,7 +123,9 @@ __global__ void __launch_bounds__(kStreamThreads, 1) pcg_stream_kernel(const Lau
         const SysDesc d = lp.descs ? lp.descs[lp.order ? lp.order[item] : item] : lp.one;
         const uint32_t n = d.n, N = d.N;
         const uint32_t K = (N + C - 1) / C;
-        if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (RPT > 1 && (n % RPT) != 0)) {
+        // (a forward + adjoint pair runs on the on-chip storages only)
+        if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (RPT > 1 && (n % RPT) != 0) ||
+            (d.flags & SYS_FWD_ADJ)) {
             if (rank == 0 && tid == 0) {
                 SysResult res = {};
                 res.status = -1;

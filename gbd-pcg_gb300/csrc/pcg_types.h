@@ -18,6 +18,8 @@ enum : uint32_t {
     SYS_ADJOINT = 4u,         // epilogue writes dS = -1/2 (mu lam^T + lam mu^T) and dgamma = mu
     SYS_LAMBDA0_ZERO = 8u,    // initial guess is zero (lambda0 pointer unused)
     SYS_REFINE = 16u,         // FP64 outer iterative refinement around the PCG
+    SYS_FWD_ADJ = 32u,        // forward solve, then in the same launch the adjoint solve
+                              // S mu = lambda - lambda* and the dS, dgamma epilogue
 };
 
 enum : int32_t {
@@ -44,6 +46,10 @@ struct SysDesc {
     uint32_t flags;
     uint32_t result;      // index into the result array
     uint32_t max_outer;   // refinement: outer steps
+    const void *lstar;    // forward + adjoint: lambda* of L = 1/2 ||lambda - lambda*||^2
+    void *mu;             // forward + adjoint: dL/dgamma = mu (n N)
+    uint32_t result_adj;  // forward + adjoint: index of the adjoint solve's result
+    uint32_t pad_;
 };
 
 struct SysResult {

@@ -64,6 +64,13 @@ class PackedSystem(ctypes.Structure):
                 ("Pinv_off", ctypes.c_uint64), ("vec_off", ctypes.c_uint64)]
 
 
+class FwdAdjSystem(ctypes.Structure):
+    """gbdpcg_fwd_adj_system: a forward solve and the adjoint of L = 1/2 ||lambda - lambda*||^2."""
+    _fields_ = [("S", ctypes.c_void_p), ("Pinv", ctypes.c_void_p), ("gamma", ctypes.c_void_p),
+                ("lambda_", ctypes.c_void_p), ("lambda_target", ctypes.c_void_p), ("grad_gamma", ctypes.c_void_p),
+                ("grad_S", ctypes.c_void_p), ("n", ctypes.c_uint32), ("N", ctypes.c_uint32)]
+
+
 class Stamp(ctypes.Structure):
     """gbdpcg_stamp: one system's timeline (GPU global clock, ns)."""
     _fields_ = [("t_pop", ctypes.c_uint64), ("t_staged", ctypes.c_uint64), ("t_solved", ctypes.c_uint64),
@@ -115,6 +122,7 @@ _SIGS = {
     "gbdpcg_solve_plain_noalloc_f32": ([_P, _P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_adjoint_dev_f32": ([_P, _P, _P, _U, _P, _P, _P, _P, _U, _U, _P, _P, _P], _I),
     "gbdpcg_plan_create": ([_P, _I, _P, _U, _U, _P, _P], _I),
+    "gbdpcg_plan_create_fwd_adj": ([_P, _I, _P, _U, _U, _P, _P], _I),
     "gbdpcg_plan_execute": ([_P, _P], _I),
     "gbdpcg_plan_create_packed": ([_P, _I, _P, _U, _P, _P, _P, _P, _U, _P, _P], _I),
     "gbdpcg_plan_execute_host": ([_P, _P, _P, _P, _P, _P, _P], _I),
@@ -339,6 +347,28 @@ class Plan:
         self.p = ctypes.c_void_p()
         _check(lib().gbdpcg_plan_create(handle.h, dtype, ctypes.cast(arr, ctypes.c_void_p), len(systems),
                                         layout, ctypes.byref(cfg), ctypes.byref(self.p)), "gbdpcg_plan_create")
+
+    @classmethod
+    def forward_adjoint(cls, handle, systems, layout=PINV_BLOCKDIAG, cfg=None, dtype=None):
+        """A plan of forward + adjoint pairs (gbdpcg_plan_create_fwd_adj): dicts
+        with S, Pinv, gamma, lambda, lambda_target, grad_gamma, grad_S, n, N.
+        results() returns 2 count results: the forward solves', then the
+        adjoint solves'."""
+        cfg = cfg or config()
+        self = cls.__new__(cls)
+        self.handle = handle
+        self.p = ctypes.c_void_p()
+        if dtype is None:
+            dtype = 1 if systems[0]["S"].dtype.itemsize == 8 else 0
+        arr = (FwdAdjSystem * len(systems))()
+        for i, s in enumerate(systems):
+            arr[i] = FwdAdjSystem(_tp(s["S"]), _tp(s["Pinv"]), _tp(s["gamma"]), _tp(s["lambda"]),
+                                  _tp(s["lambda_target"]), _tp(s["grad_gamma"]), _tp(s["grad_S"]), s["n"], s["N"])
+        self.count = 2 * len(systems)
+        _check(lib().gbdpcg_plan_create_fwd_adj(handle.h, dtype, ctypes.cast(arr, ctypes.c_void_p), len(systems),
+                                                layout, ctypes.byref(cfg), ctypes.byref(self.p)),
+               "gbdpcg_plan_create_fwd_adj")
+        return self
 
     def execute(self, stream=None):
         _check(lib().gbdpcg_plan_execute(self.p, _stream(stream)), "gbdpcg_plan_execute")

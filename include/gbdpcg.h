@@ -289,6 +289,32 @@ GBDPCG_API int gbdpcg_plan_create(gbdpcg_handle_t h, int dtype, const gbdpcg_sys
                        uint32_t pinv_layout, const gbdpcg_config *cfg, gbdpcg_plan_t *plan);
 GBDPCG_API int gbdpcg_plan_execute(gbdpcg_plan_t plan, gbdpcg_stream_t stream);
 
+/* Forward solve and adjoint of the loss L = 1/2 ||lambda - lambda*||^2 in one
+ * launch (no reference counterpart).  Each cluster solves S lambda = gamma,
+ * writes lambda, then, with the matrix rows still on chip, solves the adjoint
+ * system S mu = lambda - lambda* (S is symmetric) from mu = 0 and writes
+ * dL/dgamma = mu and the block-tridiagonal dL/dS = -1/2 (mu_i lambda_j^T +
+ * lambda_i mu_j^T) in cbtd layout: the same results as a forward plan
+ * followed by an adjoint plan (gbdpcg_system.lambda_fwd), without staging the
+ * rows twice.  Device pointers of the plan's element type (dtype 0 float,
+ * 1 double).  The plan reports 2 count results (gbdpcg_plan_results): the
+ * forward solves', then the adjoint solves'.  Systems must fit the on-chip
+ * storages (else GBDPCG_ERR_UNSUPPORTED). */
+typedef struct {
+    const void *S;
+    const void *Pinv;
+    const void *gamma;
+    void *lambda;              /* forward solution (out; the initial guess unless cfg->zero_guess) */
+    const void *lambda_target; /* lambda* */
+    void *grad_gamma;          /* dL/dgamma = mu (out) */
+    void *grad_S;              /* dL/dS, cbtd, padding blocks zero (out) */
+    uint32_t n;
+    uint32_t N;
+} gbdpcg_fwd_adj_system;
+GBDPCG_API int gbdpcg_plan_create_fwd_adj(gbdpcg_handle_t h, int dtype, const gbdpcg_fwd_adj_system *systems,
+                                          uint32_t count, uint32_t pinv_layout, const gbdpcg_config *cfg,
+                                          gbdpcg_plan_t *plan);
+
 /* A system of a packed batch: element offsets into four device arenas
  * (S, Pinv, gamma, lambda; gamma and lambda share vec_off). */
 typedef struct {
@@ -328,7 +354,8 @@ GBDPCG_API int gbdpcg_plan_solve_host(gbdpcg_plan_t plan, const void *h_S, const
                                       gbdpcg_result *h_results, gbdpcg_stream_t stream);
 /* Builds every system's block-Jacobi Phi^-1 into its Pinv pointer (stream-ordered). */
 GBDPCG_API int gbdpcg_plan_build_block_jacobi(gbdpcg_plan_t plan, gbdpcg_stream_t stream);
-/* Waits for the stream and copies `count` results out. */
+/* Waits for the stream and copies the plan's results out: `count` of them
+ * (2 count for a forward + adjoint plan). */
 GBDPCG_API int gbdpcg_plan_results(gbdpcg_plan_t plan, gbdpcg_result *results, gbdpcg_stream_t stream);
 /* Number of launches (cluster classes + plain systems) the plan makes per execution. */
 GBDPCG_API int gbdpcg_plan_launch_count(gbdpcg_plan_t plan, uint32_t *launches);

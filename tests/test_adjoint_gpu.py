@@ -151,3 +151,74 @@ def test_batched_adjoint_plan(gb, oracle_mod, handle):
         lam64, mu64, dS64 = _dense_grads(O, sy, lam_star)
         assert rel(a["lambda"].cpu().numpy(), mu64) < 1e-4
         assert rel(a["dS"].cpu().numpy(), dS64) < 2e-4
+
+
+@pytest.mark.parametrize("layout,algorithm,dts", [(1, "auto", "f32"), (0, "auto", "f32"), (1, "recurrence", "f32"),
+                                                  (1, "auto", "f64")])
+def test_fused_forward_adjoint_matches_two_plans(gb, oracle_mod, layout, algorithm, dts):
+    """gbdpcg_plan_create_fwd_adj: forward solve and adjoint solve with the dS,
+    dgamma epilogue in one launch give the bits of a forward plan followed by
+    an adjoint plan (same launch shapes: a fresh handle, no tuning table), on
+    the batched-adjoint systems (n = 14, N = 64), and the results of both
+    solves."""
+    import torch
+    O = oracle_mod
+    n, N, B = 14, 64, 12
+    dt = np.float64 if dts == "f64" else np.float32
+    td = torch.float64 if dts == "f64" else torch.float32
+    d = torch.device("cuda:0")
+    h = gb.Handle(0)
+    algo = gb.ALGO_RECURRENCE if algorithm == "recurrence" else gb.ALGO_AUTO
+    cfg = gb.config(max_iter=500, exit_tol=1e-7, exit_mode=gb.EXIT_RELRES, zero_guess=1, algorithm=algo)
+    fwd, adj, fused = [], [], []
+    for b in range(B):
+        sy, lam_star = _sys(O, n, N, 100 + b)
+        S = torch.from_numpy(sy.cbtd(dt)).to(d)
+        P = torch.from_numpy(O.block_jacobi(sy.D, "compact" if layout == 1 else "cbtd").astype(dt)).to(d)
+        g = torch.from_numpy(sy.gamma.astype(dt)).to(d)
+        star = torch.from_numpy(lam_star.astype(dt)).to(d)
+        fwd.append({"S": S, "Pinv": P, "gamma": g, "lambda": torch.zeros(n * N, dtype=td, device=d), "n": n, "N": N,
+                    "star": star})
+        fused.append({"S": S, "Pinv": P, "gamma": g, "lambda": torch.zeros(n * N, dtype=td, device=d),
+                      "lambda_target": star, "grad_gamma": torch.empty(n * N, dtype=td, device=d),
+                      "grad_S": torch.full_like(S, float("nan")), "n": n, "N": N})
+    pf = gb.Plan(h, [{k: v for k, v in f.items() if k != "star"} for f in fwd], layout, cfg)
+    pf.execute()
+    rf = pf.results()
+    for f in fwd:
+        gl = f["lambda"] - f["star"]
+        adj.append({"S": f["S"], "Pinv": f["Pinv"], "gamma": gl, "lambda": torch.empty_like(gl),
+                    "lambda_fwd": f["lambda"], "dS": torch.empty_like(f["S"]), "n": n, "N": N})
+    pa = gb.Plan(h, adj, layout, cfg)
+    pa.execute()
+    ra = pa.results()
+    pj = gb.Plan.forward_adjoint(h, fused, layout, cfg)
+    assert [l["storage"] for l in pj.launches()] == [l["storage"] for l in pf.launches()]
+    pj.execute()
+    rj = pj.results()
+    torch.cuda.synchronize()
+    assert len(rj) == 2 * B
+    for b in range(B):
+        assert rj[b].status == rf[b].status == gb.CONVERGED and rj[b].iters == rf[b].iters
+        assert rj[B + b].status == ra[b].status == gb.CONVERGED and rj[B + b].iters == ra[b].iters
+        assert fused[b]["lambda"].cpu().numpy().tobytes() == fwd[b]["lambda"].cpu().numpy().tobytes()
+        assert fused[b]["grad_gamma"].cpu().numpy().tobytes() == adj[b]["lambda"].cpu().numpy().tobytes()
+        assert fused[b]["grad_S"].cpu().numpy().tobytes() == adj[b]["dS"].cpu().numpy().tobytes()
+    for p in (pf, pa, pj):
+        p.close()
+    h.close()
+
+
+def test_fused_forward_adjoint_rejects_streamed_sizes(gb, handle):
+    """A pair whose rows do not fit on chip (n = 14, N = 20000) is refused at
+    plan creation, before anything is launched."""
+    import torch
+    n, N = 14, 20000
+    d = torch.device("cuda:0")
+    t = torch.zeros(3 * n * n * N, device=d)
+    v = torch.zeros(n * N, device=d)
+    with pytest.raises(gb.GbdpcgError) as e:
+        gb.Plan.forward_adjoint(handle, [{"S": t, "Pinv": t, "gamma": v, "lambda": v, "lambda_target": v,
+                                          "grad_gamma": v, "grad_S": t, "n": n, "N": N}], gb.PINV_BLOCKDIAG,
+                                gb.config())
+    assert e.value.code == gb.ERR_UNSUPPORTED

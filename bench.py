@@ -36,8 +36,8 @@ Printed JSON line (rank 0):
              n = 14, N = 32 system; roofline.latency repeats the floors
 --impl reference: times the reference's CPU path on the host cores — the
 reference ships none, so the oracle's C port of its PCG (all host threads).
---only around-solve | block-jacobi | single-system | single-system-n128 | timeline:
-that section alone.
+--only around-solve | block-jacobi | single-system | single-system-n128 | timeline |
+adjoint: that section alone.
 """
 from __future__ import annotations
 
@@ -72,7 +72,7 @@ def parse():
     ap.add_argument("--systems", type=int, default=4096)
     ap.add_argument("--no-extras", action="store_true", help="skip the baselines and the other configurations")
     ap.add_argument("--only", default=None, choices=["around-solve", "block-jacobi", "single-system",
-                                                     "single-system-n128", "timeline"],
+                                                     "single-system-n128", "timeline", "adjoint"],
                     help="time one section alone and print its JSON (profiling): the kernels either side of "
                          "the solve, the block-Jacobi build over the batch, or the n = 14, N = 128 seeds "
                          "beside the rebuilt reference kernel")
@@ -834,6 +834,11 @@ def main():
     hbm = peaks.get("hbm_gbs", 6800.0)
     if args.only == "around-solve":
         print(json.dumps({"around_solve": around_solve_kernels(gbdpcg, dev, hbm, N=args.knots)}), flush=True)
+        return
+    if args.only == "adjoint":
+        h1 = gbdpcg.Handle(local)
+        print(json.dumps({"adjoint": adjoint_config(gbdpcg, h1, dev, gbdpcg.TUNE_RECURRENCE)}), flush=True)
+        h1.close()
         return
     if args.only == "single-system":
         h1 = gbdpcg.Handle(local)

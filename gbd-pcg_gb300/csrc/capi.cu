@@ -100,7 +100,10 @@ int get_registry(int device, Registry **out) {
                                      variants_np32,     variants_np6_ext,  variants_np8_ext,
                                      variants_np12_ext, variants_np14_ext, variants_np16_ext,
                                      variants_np24_ext, variants_np32_ext,
-                                     variants_stream_small, variants_stream_large};
+                                     variants_stream_small, variants_stream_large,
+                                     variants_fa_np6,   variants_fa_np8,   variants_fa_np12,
+                                     variants_fa_np14,  variants_fa_np16,  variants_fa_np24,
+                                     variants_fa_np32};
     for (auto fn : fns) {
         const int c = fn(buf);
         for (int i = 0; i < c; ++i) {
@@ -127,11 +130,13 @@ int get_registry(int device, Registry **out) {
 
 // acc: dot accumulation of FP32 systems (0 float, 1 double, 2 float-float);
 // FP64 systems always accumulate in double.
+// fa: a variant that also runs forward + adjoint pairs (for such plans only).
 VariantInfo *find_variant(Registry *reg, bool f64, int acc, int np, bool ptri, int st, int rpt,
-                          int alg) {
+                          int alg, bool fa = false) {
     for (auto &vi : reg->list)
         if (vi.v.f64 == (int)f64 && vi.v.acc == (f64 ? 1 : acc) && vi.v.np == np &&
-            vi.v.ptri == (int)ptri && vi.v.st == st && vi.v.rpt == rpt && vi.v.alg == alg)
+            vi.v.ptri == (int)ptri && vi.v.st == st && vi.v.rpt == rpt && vi.v.alg == alg &&
+            vi.v.fa == (int)fa)
             return &vi;
     return nullptr;
 }
@@ -225,9 +230,9 @@ std::vector<Pref> storage_prefs(bool f64, bool ptri, uint32_t storage) {
 
 // A tuned shape for one system, if its variant exists and holds the system.
 bool tuned_shape(Registry *reg, bool f64, int acc, int np, bool ptri, uint32_t n, uint32_t N,
-                 const TuneChoice &tc, Shape *out) {
+                 const TuneChoice &tc, Shape *out, bool fa = false) {
     if (tc.rpt < 1 || n % tc.rpt || tc.C < 1 || tc.C > 16 || tc.threads == 0 || tc.threads % 32) return false;
-    VariantInfo *vi = find_variant(reg, f64, acc, np, ptri, tc.st, tc.rpt, tc.alg);
+    VariantInfo *vi = find_variant(reg, f64, acc, np, ptri, tc.st, tc.rpt, tc.alg, fa);
     if (!vi) return false;
     const uint32_t K = (N + tc.C - 1) / tc.C;
     const uint32_t thr = (K * n + tc.rpt - 1) / tc.rpt;
@@ -290,7 +295,8 @@ bool plain_fits(Registry *reg, bool f64, uint32_t n, uint32_t N) {
 // batch in one persistent launch.
 int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layout,
                  const gbdpcg_config &cfg, Shape *out, bool refine = false,
-                 const TuneChoice *tuned = nullptr, uint32_t c_pref = 1, bool lone = false) {
+                 const TuneChoice *tuned = nullptr, uint32_t c_pref = 1, bool lone = false,
+                 bool fa = false) {
     Shape s;
     const int np = np_for(n);
     if (refine) {
@@ -314,7 +320,7 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
         return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm needs a block-diagonal Phi^-1");
     if (alg == 1 && acc == 2)
         return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm has no float-float accumulation");
-    if (tuned && tuned_shape(reg, f64 && !refine, acc, np, ptri, n, N, *tuned, out)) return GBDPCG_SUCCESS;
+    if (tuned && tuned_shape(reg, f64 && !refine, acc, np, ptri, n, N, *tuned, out, fa)) return GBDPCG_SUCCESS;
     const uint32_t first_lo = (cfg.cluster_size == 0 && c_pref > 1) ? c_pref : 1;
     for (uint32_t from : {first_lo, 1u}) {
         for (const Pref &pf : storage_prefs(f64 && !refine, ptri, cfg.storage)) {
@@ -325,7 +331,7 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
                 *out = s;
                 return GBDPCG_SUCCESS;
             }
-            VariantInfo *vi = find_variant(reg, f64 && !refine, acc, np, ptri, pf.st, pf.rpt, alg);
+            VariantInfo *vi = find_variant(reg, f64 && !refine, acc, np, ptri, pf.st, pf.rpt, alg, fa);
             if (!vi) continue;
             uint32_t cap = cfg.max_threads ? cfg.max_threads : (uint32_t)vi->max_threads;
             cap = std::min<uint32_t>(cap, (uint32_t)vi->max_threads);
@@ -1098,7 +1104,7 @@ int plan_create_impl(gbdpcg_handle_t h, int dtype, const gbdpcg_system *systems,
                 tc = &tcv;
             }
         }
-        rc = choose_shape(h->reg, p->f64, s.n, s.N, pinv_layout, *cfg, &sh, p->refine, tc);
+        rc = choose_shape(h->reg, p->f64, s.n, s.N, pinv_layout, *cfg, &sh, p->refine, tc, 1, false, fa != nullptr);
         if (rc) return rc;
         if (fa && (sh.plain || streamed(sh.vi->v.st)))
             return fail(GBDPCG_ERR_UNSUPPORTED, "a forward + adjoint pair needs the rows on chip (system " +
@@ -1158,7 +1164,7 @@ int gbdpcg_plan_create_fwd_adj(gbdpcg_handle_t h, int dtype, const gbdpcg_fwd_ad
                                uint32_t count, uint32_t pinv_layout, const gbdpcg_config *cfg,
                                gbdpcg_plan_t *plan) {
     if (!systems || count == 0) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer or empty batch");
-    if (dtype != 0 && dtype != 1) return fail(GBDPCG_ERR_UNSUPPORTED, "forward + adjoint pairs are float or double");
+    if (dtype != 0) return fail(GBDPCG_ERR_UNSUPPORTED, "forward + adjoint pairs are float systems");
     std::vector<gbdpcg_system> fwd(count);
     for (uint32_t i = 0; i < count; ++i) {
         const gbdpcg_fwd_adj_system &f = systems[i];
@@ -1602,10 +1608,16 @@ std::vector<Candidate> tune_candidates(gbdpcg_plan_s *p, const PlanClass &base,
                         : p->cfg.storage == GBDPCG_STORAGE_STREAM  ? 5
                                                                    : -1;
     static const uint32_t kC[] = {1, 2, 3, 4, 5, 6, 7, 8, 16};
+    // what the plan's systems need of a kernel: the single-reduction kernel has
+    // no adjoint epilogue, the streamed one no forward + adjoint pair (a kernel
+    // that rejects a system finishes at once and would look fastest)
+    const bool adjoint = (p->descs[items[0]].flags & SYS_ADJOINT) != 0;
     for (auto &vi : reg->list) {
         const KernelVariant &v = vi.v;
         if (v.f64 != bv.f64 || v.acc != bv.acc || v.np != bv.np || v.ptri != bv.ptri) continue;
         if (std::find(algs.begin(), algs.end(), v.alg) == algs.end()) continue;
+        if ((v.alg == 1 && (adjoint || p->fused)) || (streamed(v.st) && p->fused)) continue;
+        if (v.fa != (int)p->fused) continue;  // pairs run on the variants built for them
         if (want_st >= 0 && v.st != want_st) continue;
         bool rows_ok = true;
         for (uint32_t i : items) rows_ok &= p->descs[i].n % v.rpt == 0;

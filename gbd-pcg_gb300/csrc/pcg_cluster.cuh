@@ -795,7 +795,10 @@ __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uin
 // recurrence too would remove a fourth, but in FP32 that recurrence drifts
 // and the iteration stalls.)  Same passes on well-conditioned systems;
 // iterates differ at roundoff level.
-template <typename T, typename A, int NP, bool PTRI, int ST, int RPT, bool REC>
+// FA: the variant also runs forward + adjoint pairs (SYS_FWD_ADJ: a second
+// solve phase on the rows still on chip); only such variants compile the
+// phase loop, so the others' code is that of a single solve.
+template <typename T, typename A, int NP, bool PTRI, int ST, int RPT, bool REC, bool FA = false>
 __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threads), 1)
     pcg_cluster_kernel(const LaunchParams lp) {
     using Plan = SmemPlan<T, A, NP, PTRI, ST>;
@@ -871,7 +874,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         const uint32_t n = d.n, N = d.N;
         const uint32_t K = (N + C - 1) / C;
         if (n == 0 || N == 0 || n > (uint32_t)NP || K > lp.kmax || (size_t)K * n > (size_t)nthr * RPT ||
-            (RPT > 1 && (n % RPT) != 0)) {
+            (RPT > 1 && (n % RPT) != 0) || (!FA && (d.flags & SYS_FWD_ADJ))) {
             if (rank == 0 && tid == 0) {
                 SysResult res = {};
                 res.status = -1;
@@ -1054,7 +1057,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         // Phase 0 solves S lambda = gamma.  With SYS_FWD_ADJ, phase 1 then solves
         // the adjoint system S mu = lambda - lambda* from mu = 0 on the rows
         // still on chip (S is symmetric), with lambda re-read from its output.
-        const bool fused = (d.flags & SYS_FWD_ADJ) != 0;
+        const bool fused = FA && (d.flags & SYS_FWD_ADJ) != 0;
         T *lam_out = static_cast<T *>(d.lambda);
         const T *lstar = static_cast<const T *>(d.lstar);
         T gam[RPT], lam[RPT], r[RPT], p[RPT], z[RPT], y[RPT];
@@ -1287,7 +1290,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             lp.results[phase == 0 ? d.result : d.result_adj] = res;
         }
         iters_all += iter;
-        if (phase == 0 && fused) continue;
+        if constexpr (FA) {
+            if (phase == 0 && fused) continue;
+        }
         break;
         }  // phase
 

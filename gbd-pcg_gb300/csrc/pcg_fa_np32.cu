@@ -1,0 +1,11 @@
+// Cluster-kernel variants for blocks of size n <= 32 that also run forward +
+// adjoint pairs (a translation unit of their own, compiled in parallel).
+#include "pcg_variants.cuh"
+
+namespace gbdpcg {
+int variants_fa_np32(KernelVariant *out) {
+    int c = 0;
+    GBDPCG_VARIANTS_FA(32)
+    return c;
+}
+}  // namespace gbdpcg

@@ -1,0 +1,12 @@
+// Cluster-kernel variants for blocks of size n <= 8 that also run forward +
+// adjoint pairs (a translation unit of their own, compiled in parallel).
+#include "pcg_variants.cuh"
+
+namespace gbdpcg {
+int variants_fa_np8(KernelVariant *out) {
+    int c = 0;
+    GBDPCG_VARIANTS_FA(8)
+    GBDPCG_VARIANTS_FA_RPT2(8)
+    return c;
+}
+}  // namespace gbdpcg

@@ -296,10 +296,10 @@ GBDPCG_API int gbdpcg_plan_execute(gbdpcg_plan_t plan, gbdpcg_stream_t stream);
  * dL/dgamma = mu and the block-tridiagonal dL/dS = -1/2 (mu_i lambda_j^T +
  * lambda_i mu_j^T) in cbtd layout: the same results as a forward plan
  * followed by an adjoint plan (gbdpcg_system.lambda_fwd), without staging the
- * rows twice.  Device pointers of the plan's element type (dtype 0 float,
- * 1 double).  The plan reports 2 count results (gbdpcg_plan_results): the
- * forward solves', then the adjoint solves'.  Systems must fit the on-chip
- * storages (else GBDPCG_ERR_UNSUPPORTED). */
+ * rows twice.  FP32 systems (dtype 0), device pointers.  The plan reports
+ * 2 count results (gbdpcg_plan_results): the forward solves', then the
+ * adjoint solves'.  Systems must fit the on-chip storages (else
+ * GBDPCG_ERR_UNSUPPORTED). */
 typedef struct {
     const void *S;
     const void *Pinv;

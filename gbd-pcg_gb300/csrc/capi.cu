@@ -130,7 +130,7 @@ int get_registry(int device, Registry **out) {
 
 // acc: dot accumulation of FP32 systems (0 float, 1 double, 2 float-float);
 // FP64 systems always accumulate in double.
-// fa: a variant that also runs forward + adjoint pairs (for such plans only).
+// fa: a variant that runs forward + adjoint pairs (for such plans only).
 VariantInfo *find_variant(Registry *reg, bool f64, int acc, int np, bool ptri, int st, int rpt,
                           int alg, bool fa = false) {
     for (auto &vi : reg->list)

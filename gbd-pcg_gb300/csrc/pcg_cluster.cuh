@@ -34,6 +34,7 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "accum.cuh"
 #include "tmem.cuh"
@@ -67,6 +68,10 @@ constexpr size_t kTmemExclusiveSmem = 120 * 1024;
 // 32..47 the two mbarriers of the transaction-counted reductions, word 12 the
 // CTA's reduction-timeout flag.
 constexpr size_t kItemBytes = 64;
+// Word 13 of the item area: 1 while the next pass of the persistent loop is
+// the adjoint pass of a forward + adjoint pair (SYS_FWD_ADJ), which takes the
+// same item again instead of popping a new one.
+constexpr int kAdjPassWord = 13;
 
 // Reduction slots: [2 buffers][3 values][C ranks x 32 warps]
 constexpr int kMaxValues = 3;
@@ -777,6 +782,55 @@ __device__ __forceinline__ void solver_allreduce(A (&v)[NQ], A *slots, A *wscr, 
         cluster_allreduce_tx<A, NQ>(v, slots, wscr, buf, tx, C, rank, extra_bytes);
 }
 
+// The output fields of work item `item`'s descriptor, read again from memory
+// after the iteration (volatile loads: the compiler cannot reuse the copy it
+// read when the item was taken, so none of them has to stay in a register
+// through the iteration).
+struct OutFields {
+    void *lambda, *mu, *dS;
+    const void *lam_fwd;
+    uint32_t flags, result, result_adj;
+};
+template <typename F>
+__device__ __forceinline__ F ld_volatile(const F *p) {
+    static_assert(sizeof(F) == 8 || sizeof(F) == 4, "one word");
+    if constexpr (sizeof(F) == 8) {
+        uint64_t v;
+        asm volatile("ld.volatile.global.u64 %0, [%1];" : "=l"(v) : "l"(p));
+        F f;
+        memcpy(&f, &v, 8);
+        return f;
+    } else {
+        uint32_t v;
+        asm volatile("ld.volatile.global.u32 %0, [%1];" : "=r"(v) : "l"(p));
+        F f;
+        memcpy(&f, &v, 4);
+        return f;
+    }
+}
+__device__ __forceinline__ OutFields reload_outputs(const LaunchParams &lp, uint32_t item) {
+    OutFields o;
+    if (!lp.descs) {
+        o.lambda = lp.one.lambda;
+        o.mu = lp.one.mu;
+        o.dS = lp.one.dS;
+        o.lam_fwd = lp.one.lam_fwd;
+        o.flags = lp.one.flags;
+        o.result = lp.one.result;
+        o.result_adj = lp.one.result_adj;
+        return o;
+    }
+    const SysDesc *g = lp.descs + (lp.order ? lp.order[item] : item);
+    o.lambda = ld_volatile(&g->lambda);
+    o.mu = ld_volatile(&g->mu);
+    o.dS = ld_volatile(&g->dS);
+    o.lam_fwd = ld_volatile(&g->lam_fwd);
+    o.flags = ld_volatile(&g->flags);
+    o.result = ld_volatile(&g->result);
+    o.result_adj = ld_volatile(&g->result_adj);
+    return o;
+}
+
 __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uint32_t C) {
     if (C > 1)
         cluster.sync();
@@ -795,9 +849,9 @@ __device__ __forceinline__ void group_sync(const cg::cluster_group &cluster, uin
 // recurrence too would remove a fourth, but in FP32 that recurrence drifts
 // and the iteration stalls.)  Same passes on well-conditioned systems;
 // iterates differ at roundoff level.
-// FA: the variant also runs forward + adjoint pairs (SYS_FWD_ADJ: a second
-// solve phase on the rows still on chip); only such variants compile the
-// phase loop, so the others' code is that of a single solve.
+// FA: the variant also runs forward + adjoint pairs (SYS_FWD_ADJ) as two
+// passes over the same item; without it every check of the adjoint pass is a
+// compile-time false and the code is that of single solves.
 template <typename T, typename A, int NP, bool PTRI, int ST, int RPT, bool REC, bool FA = false>
 __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threads), 1)
     pcg_cluster_kernel(const LaunchParams lp) {
@@ -832,6 +886,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     // transaction-counted reductions (C >= 2): two mbarriers of one arrival each,
     // initialised and made visible to the cluster before any CTA sends to them
     TxReduce tx{reinterpret_cast<uint64_t *>(s_item + 8), 0u, s_item + 12};
+    if constexpr (FA) {
+        if (tid == 0) s_item[kAdjPassWord] = 0u;
+    }
     if (C > 1) {
         if (tid == 0) {
             mbar_init(tx.bar, 1);
@@ -841,6 +898,11 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         }
         cluster.sync();
     }
+    // this pass is the adjoint pass of a pair (read where needed, not held)
+    auto adj_pass = [&]() {
+        if constexpr (FA) return *reinterpret_cast<volatile uint32_t *>(s_item + kAdjPassWord) != 0u;
+        else return false;
+    };
     // tensor memory: warp 0 allocates every column (the CTA is alone on its SM);
     // warp w reaches lanes (w % 4) * 32 + lane, its rows at columns (w / 4) * 3 RPT NPT
     uint32_t tbase = 0, trow = 0;
@@ -855,10 +917,11 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     Stamper stamp(lp, rank);
     for (uint32_t pass = 0;; ++pass) {
-        // ---- pull the next system (cluster leader pops, broadcasts by DSMEM)
+        // ---- pull the next system (cluster leader pops, broadcasts by DSMEM);
+        // the adjoint pass of a pair keeps the item it has
         uint32_t item;
         if (lp.queue) {
-            if (rank == 0 && tid == 0) {
+            if (rank == 0 && tid == 0 && !adj_pass()) {
                 const uint32_t it = atomicAdd(lp.queue, 1u);
                 for (uint32_t c = 0; c < C; ++c) *cluster.map_shared_rank(s_item, c) = it;
             }
@@ -904,14 +967,16 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         const uint32_t halo_in = ((has_left ? n : 0u) + (has_right ? n : 0u)) * (uint32_t)sizeof(T);
         // this CTA's block rows of S and Phi^-1 into L2 at once: the staging
         // loads below then wait on L2, not on HBM, round after round
-        if (tid == 0 && nk > 0) {
+        if (tid == 0 && nk > 0 && !adj_pass()) {
             prefetch_l2_range(S + (size_t)kb * blkS, (size_t)nk * blkS * sizeof(T));
             prefetch_l2_range(P + (size_t)kb * blkP, (size_t)nk * blkP * sizeof(T));
         }
 
         for (uint32_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
 
-        // ---- matrices: registers or shared memory
+        // ---- matrices: registers or shared memory.  An adjoint pass finds the
+        // rows of shared and tensor memory as the forward pass left them and
+        // reloads only those held in registers (from L2).
         T Sr[S_REG || S_HYB || S_TM ? RPT : 1][S_REG ? 3 * NP : (S_HYB ? 2 * NP : (S_TM ? NP : 1))];
         T Pr[P_REG ? RPT : 1][P_REG ? NBP * NP : 1];
         if constexpr (S_REG || S_HYB) {
@@ -927,7 +992,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                                                 ? __ldg(Sk + (b * n + j) * n + i + q)
                                                 : T(0);
             }
-            if constexpr (S_HYB) stage_block(ms, R, S + (size_t)kb * blkS + 2 * n * n, nk, n, blkS, tid, nthr);
+            if constexpr (S_HYB)
+                if (!adj_pass()) stage_block(ms, R, S + (size_t)kb * blkS + 2 * n * n, nk, n, blkS, tid, nthr);
         } else if constexpr (S_TM) {
             const T *Sk = S + (size_t)k * blkS;
 #pragma unroll
@@ -940,8 +1006,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             // ("rounds": 2 blocks x RPT rows x NPT/8 pieces of S, then RPT x NPT/8
             // of Phi^-1), each a tcgen05.st of 8 loaded values.  The loads run
             // kTmemDepth rounds ahead of the stores, so that several rounds' loads
-            // are in flight while a store waits for its values.
-            {
+            // are in flight while a store waits for its values.  (Not again in
+            // an adjoint pass: the forward pass left them there.)
+            if (!adj_pass()) {
                 constexpr int NC = NPT / 8, RS = 2 * RPT * NC, RR = RS + RPT * NC;
                 const T *Pk = P + (size_t)k * n * n;
                 const bool pres0 = act && k > 0, pres2 = act && k + 1 < N;
@@ -975,7 +1042,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             tmem_wait_st();
         } else {
             const T *Sg = S + (size_t)kb * blkS;
-            stage_rows(ms, R, Sg, nk, n, blkS, tid, nthr);
+            if (!adj_pass()) stage_rows(ms, R, Sg, nk, n, blkS, tid, nthr);
         }
         if constexpr (S_TM) {
             // Phi^-1 went to tensor memory with the off-diagonal S blocks
@@ -995,7 +1062,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             }
         } else {
             const T *Pg = P + (size_t)kb * blkP;
-            stage_rows(mp, R, Pg, nk, n, blkP, tid, nthr);
+            if (!adj_pass()) stage_rows(mp, R, Pg, nk, n, blkP, tid, nthr);
         }
         const int sb0 = (k == 0) ? 1 : 0, sb1 = (k + 1 == N) ? 2 : 3;
         auto matS = [&](const T *x, T(&y)[RPT]) {
@@ -1054,24 +1121,18 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
         __syncthreads();
         stamp.staged();
 
-        // Phase 0 solves S lambda = gamma.  With SYS_FWD_ADJ, phase 1 then solves
-        // the adjoint system S mu = lambda - lambda* from mu = 0 on the rows
-        // still on chip (S is symmetric), with lambda re-read from its output.
-        const bool fused = FA && (d.flags & SYS_FWD_ADJ) != 0;
-        T *lam_out = static_cast<T *>(d.lambda);
-        const T *lstar = static_cast<const T *>(d.lstar);
+        // ---- r = gamma - S lambda0   (include/pcg.cuh:119-126); the adjoint pass
+        // of a pair solves S mu = lambda - lambda* from mu = 0 (lambda: the
+        // forward pass's output)
         T gam[RPT], lam[RPT], r[RPT], p[RPT], z[RPT], y[RPT];
-        uint32_t iters_all = 0;
-        for (uint32_t phase = 0;; ++phase) {
-        if (phase == 1) {  // the forward solve's windows and halos start the adjoint at zero
-            for (uint32_t e = tid; e < zero_elems; e += nthr) vp[e] = T(0);
-        }
-        const T *lam_init = phase == 0 ? lam0 : nullptr;
-        // ---- r = gamma - S lambda0   (include/pcg.cuh:119-126)
+        const bool adj0 = adj_pass();
+        const T *lam_init = adj0 ? nullptr : lam0;
 #pragma unroll
         for (int q = 0; q < RPT; ++q) {
             const size_t row = (size_t)k * n + i + q;
-            gam[q] = act ? (phase == 0 ? gamma[row] : lam_out[row] - lstar[row]) : T(0);
+            gam[q] = act ? (adj0 ? static_cast<const T *>(d.lambda)[row] - static_cast<const T *>(d.lstar)[row]
+                                 : gamma[row])
+                         : T(0);
             lam[q] = (act && lam_init) ? lam_init[row] : T(0);
             if (act) my_p[q] = lam[q];
         }
@@ -1270,10 +1331,15 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
 
         // ---- outputs   (include/pcg.cuh:212-217)
         stamp.solved();
-        T *sol_out = phase == 0 ? lam_out : static_cast<T *>(d.mu);
+        const bool adj = adj_pass();
+        // the output fields: read again now when pairs are possible, else as taken
+        OutFields dd;
+        if constexpr (FA) dd = reload_outputs(lp, item);
+        else dd = OutFields{d.lambda, d.mu, d.dS, d.lam_fwd, d.flags, d.result, d.result_adj};
+        T *lam_out = static_cast<T *>(adj ? dd.mu : dd.lambda);
         if (act) {
 #pragma unroll
-            for (int q = 0; q < RPT; ++q) sol_out[(size_t)k * n + i + q] = lam[q];
+            for (int q = 0; q < RPT; ++q) lam_out[(size_t)k * n + i + q] = lam[q];
         }
         if (rank == 0 && tid == 0) {
             if (C > 1)  // a reduction wait of some CTA of the cluster gave up
@@ -1287,20 +1353,14 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
             res.gg = (double)gg;
             res.outer = 0;
             res.pad = 0;
-            lp.results[phase == 0 ? d.result : d.result_adj] = res;
+            lp.results[adj ? dd.result_adj : dd.result] = res;
         }
-        iters_all += iter;
-        if constexpr (FA) {
-            if (phase == 0 && fused) continue;
-        }
-        break;
-        }  // phase
 
         // ---- adjoint epilogue: dS = -1/2 (mu lam^T + lam mu^T) on the block pattern
-        // (after a forward + adjoint pair too: lam_fwd is then the lambda output)
-        if (d.flags & (SYS_ADJOINT | SYS_FWD_ADJ)) {
-            const T *lf = static_cast<const T *>(d.lam_fwd);
-            T *dS = static_cast<T *>(d.dS);
+        // (after an adjoint solve, or the adjoint pass of a pair)
+        if ((dd.flags & SYS_ADJOINT) || adj) {
+            const T *lf = static_cast<const T *>(dd.lam_fwd);
+            T *dS = static_cast<T *>(dd.dS);
             group_sync(cluster, C);  // vp / vr free in every CTA
             T lfi[RPT];
 #pragma unroll
@@ -1341,7 +1401,13 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 }
             }
         }
-        stamp.done(lp, item, iters_all);
+        stamp.done(lp, item, iter);
+        if constexpr (FA) {
+            if ((dd.flags & SYS_FWD_ADJ) && lp.queue) {  // a pair: the adjoint pass next, then a new item
+                __syncthreads();  // every thread has read this pass's word
+                if (tid == 0) s_item[kAdjPassWord] = adj ? 0u : 1u;
+            }
+        }
     }
     if (C > 1) cluster.sync();  // every transaction-counted store into this CTA has landed
     if constexpr (S_TM) {  // every TMEM access of the CTA is done

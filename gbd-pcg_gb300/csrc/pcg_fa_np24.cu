@@ -1,4 +1,4 @@
-// Cluster-kernel variants for blocks of size n <= 24 that also run forward +
+// Cluster-kernel variants for blocks of size n <= 24 that run forward +
 // adjoint pairs (a translation unit of their own, compiled in parallel).
 #include "pcg_variants.cuh"
 

@@ -19,7 +19,7 @@ struct KernelVariant {
                  // per iteration)
     const void *func;
     size_t (*smem_bytes)(uint32_t kmax, uint32_t C, uint32_t nwarps);
-    int fa = 0;  // also runs forward + adjoint pairs (SYS_FWD_ADJ)
+    int fa = 0;  // runs forward + adjoint pairs (SYS_FWD_ADJ), for such plans only
 };
 
 // Each returns the number of variants written to `out` (at most kMaxVariantsPerNP).
@@ -39,7 +39,7 @@ int variants_np16_ext(KernelVariant *out);
 int variants_np24_ext(KernelVariant *out);
 int variants_np32_ext(KernelVariant *out);
 int variants_stream_small(KernelVariant *out);  // streamed rows, NP 6..14
-int variants_fa_np6(KernelVariant *out);  // forward + adjoint variants, one unit per NP
+int variants_fa_np6(KernelVariant *out);  // forward + adjoint pair variants, one unit per NP
 int variants_fa_np8(KernelVariant *out);
 int variants_fa_np12(KernelVariant *out);
 int variants_fa_np14(KernelVariant *out);

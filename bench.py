@@ -569,6 +569,8 @@ def adjoint_config(gbdpcg, h, dev, tune_flags=None, count=1024, n=14, N=64):
            "forward_plus_adjoint_over_forward": (t_f + t_a) / t_f,
            "adjoint_all_converged": all(r.status == 0 for r in res_a),
            "fused_ms": t_j, "fused_over_forward": t_j / t_f,
+           "shapes": {k: [[l["cluster"], l["threads"], l["storage"], l["rows_per_thread"], l["algorithm"],
+                           l["systems"]] for l in pl.launches()] for k, pl in (("forward", pf), ("fused", pj))},
            "fused_all_converged": all(r.status == 0 for r in res_j),
            "autotuned": tune_flags is not None,
            "note": "adjoint = PCG solve of S mu = lambda - lambda* plus the dS, dgamma epilogue; fused = "

@@ -97,8 +97,9 @@
     out[c++] = GBDPCG_VARIANT(float, float, NP, false, ST_HYB, 2);                            \
     out[c++] = GBDPCG_VARIANT_REC(float, float, NP, false, ST_HYB, 2);
 // Variants that run forward + adjoint pairs (FP32, native accumulation): the
-// storages the planner chooses by default and the recurrence form the
-// autotuner adds, with a compact or a cbtd Phi^-1.
+// storages the planner and the autotuner choose from (registers, split,
+// shared, hybrid, tensor memory), standard and recurrence forms, with a
+// compact or a cbtd Phi^-1.
 #define GBDPCG_VARIANT_FA(NP, PTRI, ST, RPT, REC)                                             \
     ::gbdpcg::KernelVariant {                                                                 \
         0, 0, NP, PTRI, ST, RPT, REC ? 3 : 0,                                                 \
@@ -111,11 +112,17 @@
     out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_SMEM, 1, false);                               \
     out[c++] = GBDPCG_VARIANT_FA(NP, true, ST_REG, 1, false);                                 \
     out[c++] = GBDPCG_VARIANT_FA(NP, true, ST_SMEM, 1, false);                                \
+    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_HYB, 1, false);                                \
     out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_REG, 1, true);                                 \
-    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_SMEM, 1, true);
+    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_SMEM, 1, true);                                \
+    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_HYB, 1, true);
 #define GBDPCG_VARIANTS_FA_RPT2(NP)                                                           \
     out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_REG_S, 2, false);                              \
-    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_REG_S, 2, true);
+    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_HYB, 2, false);                                \
+    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_TMEM, 2, false);                               \
+    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_REG_S, 2, true);                               \
+    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_HYB, 2, true);                                 \
+    out[c++] = GBDPCG_VARIANT_FA(NP, false, ST_TMEM, 2, true);
 // Streamed rows (read from global memory in every product): FP32 with a compact
 // Phi^-1 (one or two rows per thread) or a cbtd one, FP64 with either.
 #define GBDPCG_VARIANT_STREAM(T, A, NP, PTRI, RPT)                                            \

@@ -2,7 +2,8 @@
 
 Workload (one "step"): 4096 independent block-tridiagonal Schur-complement
 systems, n drawn from {6, 12, 14, 24} (m = n/2), N uniform in [16, 128],
-per-system seeds 0..4095 (rank r of a multi-GPU run uses seeds r*4096 + i),
+per-system seeds 0..4095 (a multi-GPU run of W ranks solves seeds 0..4096 W - 1,
+split over the ranks by estimated cost with the library's partitioner),
 gamma ~ N(0, 1), lambda0 = 0, FP32, block-Jacobi Phi^-1 (built on the GPU),
 exit on the relative recursive residual ||r|| <= 1e-6 ||gamma||.  All systems
 are solved by one CUDA-graph replay of the persistent cluster launches.
@@ -92,15 +93,24 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
-def rank_seeds(rank, count):
-    """Seeds of the systems rank `rank` solves: each rank its own `count`
-    systems, disjoint from every other rank's (weak scaling, no exchange)."""
-    return range(rank * count, rank * count + count)
+def rank_seeds(rank, count, world=1):
+    """Seeds of the systems rank `rank` solves.  The job's batch is the
+    world*count systems of seeds 0 .. world*count-1 (weak scaling: `count` per
+    GPU); it is split over the ranks by estimated cost n^2 N with the
+    library's partitioner (gbdpcg_partition), each rank solving its own part
+    with no exchange of data.  One rank: seeds 0 .. count-1."""
+    if world <= 1:
+        return list(range(count))
+    from gbdpcg import distributed as D
+    from gbdpcg.workload import mixed_size
+    sizes = np.array([mixed_size(s) for s in range(world * count)], np.uint32)
+    part_of, _ = D.partition(sizes[:, 0], sizes[:, 1], world)
+    return D.rank_items(part_of, rank).tolist()
 
 
-def build_batch(rank, count, workers):
+def build_batch(rank, count, workers, world=1):
     from gbdpcg.workload import packed_batch
-    return packed_batch(rank_seeds(rank, count), np.float32, workers=workers, pinv_layout=1)
+    return packed_batch(rank_seeds(rank, count, world), np.float32, workers=workers, pinv_layout=1)
 
 
 def max_over_ranks(x, world, dev=None):
@@ -115,9 +125,9 @@ def max_over_ranks(x, world, dev=None):
     return float(t.item())
 
 
-def whole_job_rate(world, systems_per_rank, steps, seconds):
+def whole_job_rate(job_systems, steps, seconds):
     """Systems solved by all ranks per second of the slowest rank's time."""
-    return world * systems_per_rank * steps / seconds
+    return job_systems * steps / seconds
 
 
 def algorithmic_bytes(descs, iters, s=4):
@@ -853,8 +863,9 @@ def main():
         h1.close()
         return
 
-    descs, Sa, ga, nP = build_batch(rank, args.systems, max(1, (os.cpu_count() or 1) // max(1, world)))
-    count = len(descs)
+    descs, Sa, ga, nP = build_batch(rank, args.systems, max(1, (os.cpu_count() or 1) // max(1, world)), world)
+    count = len(descs)              # this rank's part of the job's batch
+    job_systems = world * args.systems
     dS = torch.from_numpy(Sa).to(dev)
     dg = torch.from_numpy(ga).to(dev)
     dP = torch.empty(nP, dtype=torch.float32, device=dev)
@@ -914,7 +925,7 @@ def main():
     clocks = clk.summary()
     ms = max_over_ranks(e0.elapsed_time(e1), world, dev)
     ms_step = ms / args.steps
-    value = whole_job_rate(world, count, args.steps, ms / 1e3)
+    value = whole_job_rate(job_systems, args.steps, ms / 1e3)
 
     # ---- end to end from pinned host buffers through the C ABI: the batched
     # pcg_solve (S and gamma in, Phi^-1 built on the device, lambda and the
@@ -975,9 +986,11 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, see config)",
         "config": {"workload": WORKLOAD, "algorithm": args.algorithm, "storage": args.storage,
-                   "cluster_size": args.cluster_size, "systems_per_gpu": count,
-                   "global_batch": count * world,
-                   "seeds": f"rank*{count} + [0, {count})", "l2": "inputs (1.1 GB/GPU) larger than L2",
+                   "cluster_size": args.cluster_size, "systems_per_gpu": args.systems,
+                   "global_batch": job_systems,
+                   "seeds": (f"[0, {job_systems})" + ("" if world == 1 else
+                             ", split over the ranks by estimated cost (gbdpcg_partition)")),
+                   "l2": "inputs (1.1 GB/GPU) larger than L2",
                    "parallelism": f"replicas{world} (independent systems per GPU)",
                    "launches_per_step": len(launches), "autotune": args.tune,
                    "autotune_s": round(tune_s, 2),
@@ -994,13 +1007,13 @@ def main():
                                     "achieved": compulsory / (ms_step / 1e3) / 1e9,
                                     "frac": compulsory / (ms_step / 1e3) / 1e9 / hbm},
                      "fp32_flops_per_step": flops, "fp32_tflops": flops / (ms_step / 1e3) / 1e12},
-        "e2e": {"value": whole_job_rate(world, count, 1, e2e_med), "unit": "solves/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": whole_job_rate(job_systems, 1, e2e_med), "unit": "solves/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": e2e_steps, "statistic": "median step",
-                "mean_step_value": whole_job_rate(world, count, e2e_steps, e2e_s),
+                "mean_step_value": whole_job_rate(job_systems, e2e_steps, e2e_s),
                 "path": "gbdpcg_plan_solve_host (batched pcg_solve): S, gamma in; Phi^-1 built on the GPU; "
                         "lambda and results out; pinned host memory",
-                "with_pinv_copied": {"value": whole_job_rate(world, count, 1, e2e_p_med), "unit": "solves/s",
-                                     "mean_step_value": whole_job_rate(world, count, e2e_steps, e2e_p_s),
+                "with_pinv_copied": {"value": whole_job_rate(job_systems, 1, e2e_p_med), "unit": "solves/s",
+                                     "mean_step_value": whole_job_rate(job_systems, e2e_steps, e2e_p_s),
                                      "h2d_bytes_per_step": h2d + hP.numel() * 4,
                                      "path": "gbdpcg_plan_execute_host (solvePCG with Pinv)"}},
         "gpu_launches": len(launches) * args.steps,

@@ -136,6 +136,7 @@ _SIGS = {
     "gbdpcg_plan_timeline": ([_P, _I], _I),
     "gbdpcg_plan_timeline_read": ([_P, _P, _U, _P, _P, _U, _P, _P], _I),
     "gbdpcg_probe_primitives": ([_I, _U, _U, _U, _U, _P], _I),
+    "gbdpcg_partition": ([_P, _P, _P, _U, _U, _P, _P], _I),
     "gbdpcg_form_schur_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
     "gbdpcg_form_schur_f64": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
     "gbdpcg_form_schur_pinv_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P, _P], _I),

@@ -58,6 +58,15 @@ def generate(n: int, N: int, seed: int, ill: bool = False, rng=None) -> System:
     return System(n, N, D, O, gamma, seed)
 
 
+def mixed_size(seed: int, sizes=(6, 12, 14, 24), nmin=16, nmax=128):
+    """(n, N) of generate_mixed(seed) without building the system (the same
+    first two draws)."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.choice(np.asarray(sizes)))
+    N = int(rng.integers(nmin, nmax + 1))
+    return n, N
+
+
 def generate_mixed(seed: int, sizes=(6, 12, 14, 24), nmin=16, nmax=128) -> System:
     """One system of the mixed batch: n from `sizes`, N uniform in [nmin, nmax],
     then the generator above, all from default_rng(seed)."""

@@ -315,6 +315,18 @@ GBDPCG_API int gbdpcg_plan_create_fwd_adj(gbdpcg_handle_t h, int dtype, const gb
                                           uint32_t count, uint32_t pinv_layout, const gbdpcg_config *cfg,
                                           gbdpcg_plan_t *plan);
 
+/* Split of one batch of independent systems over `parts` GPUs or ranks (no
+ * reference counterpart: the reference solves one system per call; this is
+ * the batch-level split of a multi-GPU deployment).  System i is estimated to
+ * cost n[i]^2 N[i] iters[i] (iters NULL: 1 each); systems go, in decreasing
+ * cost, to the part with the least cost so far (ties: the lowest index).
+ * Writes part_of[count] and, if non-NULL, part_cost[parts].  Host code only:
+ * no CUDA call, no GPU needed.  Each part is then solved by its own plan on
+ * its own device, with no exchange of data between parts, and the results are
+ * gathered in input order by the caller. */
+GBDPCG_API int gbdpcg_partition(const uint32_t *n, const uint32_t *N, const float *iters, uint32_t count,
+                                uint32_t parts, uint32_t *part_of, double *part_cost);
+
 /* A system of a packed batch: element offsets into four device arenas
  * (S, Pinv, gamma, lambda; gamma and lambda share vec_off). */
 typedef struct {

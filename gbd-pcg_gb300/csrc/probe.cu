@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/gbdpcg.h"
 #include "pcg_cluster.cuh"
@@ -90,6 +91,47 @@ __global__ void probe_kernel(uint32_t reps, float *sink) {
     else if (v == 12345.678f)
         sink[0] = v;  // keeps the chain alive
     if (C > 1) cluster.sync();  // no CTA leaves while a peer may still store into it
+}
+
+// A wait that nothing completes, through the solver's own bounded waits: for
+// a cluster of C >= 2 CTAs, one transaction-counted reduction whose receivers
+// also expect 16 bytes of halo that no neighbour sends (every real partial
+// arrives); for C = 1, a wait on an mbarrier that expects 16 bytes nothing
+// sends.  Each CTA gives up after about a second (mbar_wait_bounded) and
+// writes its outcome to status[cta]: GBDPCG_TIMEOUT when the wait gave up.
+// Nothing waits without a limit, and no CTA leaves before the cluster's last
+// barrier, so no store is in flight into a CTA that has ended.
+__global__ void probe_timeout_kernel(int *status) {
+    const cg::cluster_group cluster = cg::this_cluster();
+    const uint32_t C = cluster.num_blocks(), rank = cluster.block_rank();
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const uint32_t nwarps = blockDim.x >> 5;
+    float *slots = reinterpret_cast<float *>(smem_raw);
+    float *wscr = slots + 2 * kMaxValues * slot_stride(C);
+    float *cell = wscr + nwarps * kMaxValues * 32;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(cell + 8);
+    uint32_t *timed_out = reinterpret_cast<uint32_t *>(bar + 2);
+    if (threadIdx.x == 0) {
+        *timed_out = 0u;
+        mbar_init(bar, 1);
+        mbar_init(bar + 1, 1);
+        mbar_init_fence();
+    }
+    if (C > 1)
+        cluster.sync();
+    else
+        __syncthreads();
+    TxReduce tx{bar, 0u, timed_out};
+    if (C > 1) {
+        float q[1] = {(float)rank};
+        cluster_allreduce_tx<float, 1>(q, slots, wscr, 0, tx, C, rank, 16u);
+    } else {
+        if (threadIdx.x == 0) mbar_arrive_expect_tx(bar, 16u);
+        mbar_wait_bounded(bar, 0u, timed_out);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) status[blockIdx.x] = *timed_out ? GBDPCG_TIMEOUT : GBDPCG_SUCCESS;
+    if (C > 1) cluster.sync();
 }
 
 size_t probe_smem(uint32_t C, uint32_t threads) {
@@ -191,6 +233,56 @@ int gbdpcg_probe_primitives(int device, uint32_t cluster, uint32_t threads, uint
     out->dsmem_store_barrier_ns = cluster > 1 ? net(t[3]) : 0.0;
     for (int q = 0; q < 3; ++q) out->allreduce_ns[q] = net(t[4 + q]);
     for (int q = 0; q < 3; ++q) out->allreduce_tx_ns[q] = cluster > 1 ? net(t[7 + q]) : 0.0;
+    return GBDPCG_SUCCESS;
+}
+
+int gbdpcg_probe_timeout(int device, uint32_t cluster, int *status, double *waited_ms) {
+    if (!status || !waited_ms) return probe_fail(GBDPCG_ERR_INVALID_ARGUMENT, "NULL pointer");
+    if (cluster < 1 || cluster > 16) return probe_fail(GBDPCG_ERR_INVALID_ARGUMENT, "cluster 1..16");
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != device && cudaSetDevice(device) != cudaSuccess)
+        return probe_fail(GBDPCG_ERR_INVALID_ARGUMENT, "bad device");
+    const uint32_t threads = 128;
+    const void *func = (const void *)&probe_timeout_kernel;
+    int *d_status = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMalloc(&d_status, cluster * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(d_status, 0xff, cluster * sizeof(int));
+    if (e == cudaSuccess && cluster > 8) e = cudaFuncSetAttribute(func, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(cluster);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = probe_smem(cluster, threads);
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void *args[] = {&d_status};
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, 0);
+    if (e == cudaSuccess) e = cudaLaunchKernelExC(&cfg, func, args);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    std::vector<int> st(cluster, -2);
+    if (e == cudaSuccess) e = cudaMemcpy(st.data(), d_status, cluster * sizeof(int), cudaMemcpyDeviceToHost);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (d_status) cudaFree(d_status);
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    if (e != cudaSuccess) return probe_fail(GBDPCG_ERR_CUDA, std::string("timeout probe: ") + cudaGetErrorString(e));
+    int worst = GBDPCG_TIMEOUT;
+    for (int x : st)
+        if (x != GBDPCG_TIMEOUT) worst = x;  // a CTA whose wait did not give up
+    *status = worst;
+    *waited_ms = (double)ms;
     return GBDPCG_SUCCESS;
 }
 

@@ -95,6 +95,14 @@ def probe_primitives(device=0, cluster=1, threads=128, clusters=1, reps=100000) 
             "allreduce_tx_ns": list(p.allreduce_tx_ns)}
 
 
+def probe_timeout(device=0, cluster=2) -> tuple:
+    """A wait that nothing completes, through the solver's bounded wait
+    (gbdpcg_probe_timeout): (status, ms waited)."""
+    st, ms = ctypes.c_int(0), ctypes.c_double(0)
+    _check(lib().gbdpcg_probe_timeout(device, cluster, ctypes.byref(st), ctypes.byref(ms)), "gbdpcg_probe_timeout")
+    return st.value, ms.value
+
+
 class System(ctypes.Structure):
     _fields_ = [("S", ctypes.c_void_p), ("Pinv", ctypes.c_void_p), ("gamma", ctypes.c_void_p),
                 ("lambda_", ctypes.c_void_p), ("lambda_fwd", ctypes.c_void_p), ("dS", ctypes.c_void_p),
@@ -136,6 +144,7 @@ _SIGS = {
     "gbdpcg_plan_timeline": ([_P, _I], _I),
     "gbdpcg_plan_timeline_read": ([_P, _P, _U, _P, _P, _U, _P, _P], _I),
     "gbdpcg_probe_primitives": ([_I, _U, _U, _U, _U, _P], _I),
+    "gbdpcg_probe_timeout": ([_I, _U, _P, _P], _I),
     "gbdpcg_partition": ([_P, _P, _P, _U, _U, _P, _P], _I),
     "gbdpcg_form_schur_f32": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),
     "gbdpcg_form_schur_f64": ([_P] * 7 + [_U, _U, _U, _P, _P, _P], _I),

@@ -477,6 +477,16 @@ typedef struct {
 } gbdpcg_probe;
 GBDPCG_API int gbdpcg_probe_primitives(int device, uint32_t cluster, uint32_t threads, uint32_t clusters,
                                        uint32_t reps, gbdpcg_probe *out);
+/* The cluster solver's failure path without a fault (no reference
+ * counterpart: the reference's grid barriers wait without a limit): one
+ * cluster of `cluster` CTAs (1..16) runs a wait that nothing completes, through
+ * the solver's own bounded mbarrier wait (for cluster >= 2, a cluster-wide
+ * reduction whose receivers also expect halo bytes no neighbour sends).  Every
+ * CTA gives up after about a second; *status = GBDPCG_TIMEOUT when all of them
+ * did (else the outcome of a CTA that did not), *waited_ms = the launch's
+ * duration.  The context stays usable.  Synchronous; allocates `cluster`
+ * words of device memory. */
+GBDPCG_API int gbdpcg_probe_timeout(int device, uint32_t cluster, int *status, double *waited_ms);
 /* Waits for the stream and copies the last execution's records (one per
  * system of the cluster launches, grouped by launch; at most `capacity`) and
  * the SM of each CTA (launch 0's CTAs first, in grid order; at most

@@ -1,6 +1,7 @@
 """The measurement entry points: a plan's per-system timeline
 (gbdpcg_plan_timeline / _read) and the latency probes of the synchronisation
-primitives (gbdpcg_probe_primitives)."""
+primitives (gbdpcg_probe_primitives) and of the bounded wait's failure path
+(gbdpcg_probe_timeout)."""
 import numpy as np
 import pytest
 
@@ -72,3 +73,27 @@ def test_probe_primitives(gb, handle, C, threads):
         assert all(x > 0 for x in p["allreduce_tx_ns"])
     with pytest.raises(gb.GbdpcgError):
         gb.probe_primitives(0, 17, threads, 1, 10)
+
+
+@pytest.mark.parametrize("C", [1, 2, 8])
+def test_bounded_wait_gives_up_and_the_context_stays_usable(gb, oracle_mod, handle, C):
+    """The solver's failure path, made without a fault: a wait that nothing
+    completes (for C >= 2 a cluster reduction whose receivers also expect halo
+    bytes no neighbour sends) gives up after about a second with
+    GBDPCG_TIMEOUT, and the same context then solves a batch (true relative
+    residual within 1e-4 by the oracle's FP64 product)."""
+    import torch
+    st, ms = gb.probe_timeout(0, C)
+    assert st == gb.TIMEOUT
+    assert 900.0 <= ms <= 10000.0
+    plan, systems = _plan(gb, oracle_mod, handle, range(8))
+    plan.execute()
+    torch.cuda.synchronize()
+    res = plan.results()
+    assert all(r.status == gb.CONVERGED for r in res)
+    for i, s in enumerate(systems):
+        sy = oracle_mod.generate_mixed(i)
+        assert oracle_mod.relres(sy.cbtd(np.float64), s["lambda"].cpu().numpy(), sy.gamma, sy.n, sy.N) <= 1e-4
+    with pytest.raises(gb.GbdpcgError):
+        gb.probe_timeout(0, 17)
+    plan.close()

@@ -477,32 +477,41 @@ __device__ __forceinline__ void warp_sum_n(A (&v)[NQ]) {
     }
 }
 
-// Sum of the M (32 or 64) values at p (A-typed, 16-byte aligned) with vector
-// loads into four accumulator chains (element j into chain j mod 4), then
-// (c0+c1)+(c2+c3).
+// Sum of the first `used` of the M (32 or 64) values at p (A-typed, 16-byte
+// aligned; values from `used` on are zero) with vector loads into four
+// accumulator chains (element j into chain j mod 4), then (c0+c1)+(c2+c3).
+// Whole groups of four are read up to `used`; the groups after it would only
+// add zeros to chains that started at +0, which leaves their bits unchanged,
+// so they are skipped (a warp-uniform bound).
 template <typename A, int M>
-__device__ __forceinline__ A sum_slots(const A *p) {
+__device__ __forceinline__ A sum_slots(const A *p, uint32_t used = M) {
     static_assert(M % 4 == 0, "four chains");
     A c0 = A(0), c1 = A(0), c2 = A(0), c3 = A(0);
     if constexpr (std::is_same<A, f2acc>::value) {
 #pragma unroll
         for (int j = 0; j < M / 4; ++j) {
-            const float4 t0 = reinterpret_cast<const float4 *>(p)[2 * j];
-            const float4 t1 = reinterpret_cast<const float4 *>(p)[2 * j + 1];
-            c0 += f2acc(t0.x, t0.y); c1 += f2acc(t0.z, t0.w); c2 += f2acc(t1.x, t1.y); c3 += f2acc(t1.z, t1.w);
+            if ((uint32_t)(4 * j) < used) {
+                const float4 t0 = reinterpret_cast<const float4 *>(p)[2 * j];
+                const float4 t1 = reinterpret_cast<const float4 *>(p)[2 * j + 1];
+                c0 += f2acc(t0.x, t0.y); c1 += f2acc(t0.z, t0.w); c2 += f2acc(t1.x, t1.y); c3 += f2acc(t1.z, t1.w);
+            }
         }
     } else if constexpr (sizeof(A) == 4) {
 #pragma unroll
         for (int j = 0; j < M / 4; ++j) {
-            const float4 t = reinterpret_cast<const float4 *>(p)[j];
-            c0 += t.x; c1 += t.y; c2 += t.z; c3 += t.w;
+            if ((uint32_t)(4 * j) < used) {
+                const float4 t = reinterpret_cast<const float4 *>(p)[j];
+                c0 += t.x; c1 += t.y; c2 += t.z; c3 += t.w;
+            }
         }
     } else {
 #pragma unroll
         for (int j = 0; j < M / 4; ++j) {
-            const double2 t0 = reinterpret_cast<const double2 *>(p)[2 * j];
-            const double2 t1 = reinterpret_cast<const double2 *>(p)[2 * j + 1];
-            c0 += t0.x; c1 += t0.y; c2 += t1.x; c3 += t1.y;
+            if ((uint32_t)(4 * j) < used) {
+                const double2 t0 = reinterpret_cast<const double2 *>(p)[2 * j];
+                const double2 t1 = reinterpret_cast<const double2 *>(p)[2 * j + 1];
+                c0 += t0.x; c1 += t0.y; c2 += t1.x; c3 += t1.y;
+            }
         }
     }
     return (c0 + c1) + (c2 + c3);
@@ -514,7 +523,7 @@ __device__ __forceinline__ A sum32(const A *p) {
 }
 
 // The slots of one reduction value, summed identically in every thread: up
-// to 32 slots (zero beyond `total`) with vector loads and four chains, and up
+// to 32 slots (zero beyond `total`, not read) with vector loads and four chains, and up
 // to 64 that way too for float accumulators; more with a strided sum per lane
 // and a warp butterfly.  (Double and float-float additions are many times
 // dearer than float ones on GB300, so for them every thread adding 64 slots
@@ -523,10 +532,10 @@ template <typename A, int NQ>
 __device__ __forceinline__ void sum_all_slots(A (&v)[NQ], const A *sl, uint32_t stride, uint32_t total) {
     if (total <= 32) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) v[q] = sum_slots<A, 32>(sl + q * stride);
+        for (int q = 0; q < NQ; ++q) v[q] = sum_slots<A, 32>(sl + q * stride, total);
     } else if (std::is_same<A, float>::value && total <= 64) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) v[q] = sum_slots<A, 64>(sl + q * stride);
+        for (int q = 0; q < NQ; ++q) v[q] = sum_slots<A, 64>(sl + q * stride, total);
     } else {
         const uint32_t lane = threadIdx.x & 31;
 #pragma unroll
@@ -1436,7 +1445,8 @@ struct SmemPlanSR {
 // Single-reduction (Chronopoulos-Gear) PCG with a block-diagonal Phi^-1: the
 // vectors s = S p and u = Phi^-1 r are carried by recurrences so that
 // gamma = r.u, delta = (S u).u (and r.r) are reduced together: one cluster
-// barrier per iteration instead of two.
+// reduction per iteration instead of two (transaction-counted for C >= 2, the
+// neighbours' boundary w travelling on the same mbarrier).
 //   r0 = gamma - S x0, u0 = M r0, w0 = S u0, g0 = r0.u0, d0 = w0.u0,
 //   alpha0 = g0/d0, beta0 = 0; per pass
 //   p = u + beta p; s = w + beta s; x += alpha p; r -= alpha s; u = M r;
@@ -1476,6 +1486,17 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
     const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
 
     for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
+    // transaction-counted reductions (C >= 2), as in pcg_cluster_kernel
+    TxReduce tx{reinterpret_cast<uint64_t *>(s_item + 8), 0u, s_item + 12};
+    if (C > 1) {
+        if (tid == 0) {
+            mbar_init(tx.bar, 1);
+            mbar_init(tx.bar + 1, 1);
+            *tx.timed_out = 0u;
+            mbar_init_fence();
+        }
+        cluster.sync();
+    }
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     Stamper stamp(lp, rank);
     for (uint32_t pass = 0;; ++pass) {
@@ -1523,6 +1544,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
         const uint32_t R = (K * n + 1) & ~1u;  // row stride of staged matrices (even)
         const bool has_left = nk > 0 && kb > 0, has_right = nk > 0 && ke < N;
         const bool first_knot = act && lk == 0 && kb > 0, last_knot = act && lk + 1 == nk && ke < N;
+        // halo bytes the neighbours send to this CTA with each reduction (n values each)
+        const uint32_t halo_in = ((has_left ? n : 0u) + (has_right ? n : 0u)) * (uint32_t)sizeof(T);
         if (tid == 0 && nk > 0) {  // this CTA's rows into L2 before they are staged
             prefetch_l2_range(S + (size_t)kb * blkS, (size_t)nk * blkS * sizeof(T));
             prefetch_l2_range(P + (size_t)kb * blkP, (size_t)nk * blkP * sizeof(T));
@@ -1582,7 +1605,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
             const T *M = mh + side * NP * NP + row;
             const T *rw = vr + (side ? (nk + 1) * NP : 0);
             T acc = T(0);
-            for (uint32_t j = 0; j < n; ++j) acc = fma_rn(M[j * n], rw[j], acc);
+#pragma unroll
+            for (int j = 0; j < NP; ++j)  // unrolled to NP: every load issued ahead of the chain
+                if ((uint32_t)j < n) acc = fma_rn(M[j * n], rw[j], acc);
             return acc;
         };
         T *my_u = vu + (lk + 1) * NP + i;
@@ -1647,16 +1672,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
 #pragma unroll
             for (int q = 0; q < RPT; ++q) w[q] = T(0);
         }
-        if (first_knot) {
-            T *dst = cluster.map_shared_rank(wh0, rank - 1) + NP + i;
-#pragma unroll
-            for (int q = 0; q < RPT; ++q) dst[q] = w[q];
-        }
-        if (last_knot) {
-            T *dst = cluster.map_shared_rank(wh0, rank + 1) + i;
-#pragma unroll
-            for (int q = 0; q < RPT; ++q) dst[q] = w[q];
-        }
+        // boundary w into the neighbours' halo buffer 0, counted on their reduction buffer 0
+        if (first_knot) push_halo_tx<T, RPT>(wh0 + NP + i, rank - 1, w, tx, 0);
+        if (last_knot) push_halo_tx<T, RPT>(wh0 + i, rank + 1, w, tx, 0);
         A g, dlt, gg;
         {
             A v3[3] = {A(0), A(0), A(0)};
@@ -1666,7 +1684,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
                 acc_madd(v3[1], w[q], u[q]);
                 acc_madd(v3[2], gam[q], gam[q]);
             }
-            cluster_allreduce<A, 3>(v3, slots, wscr, 0, cluster, C, rank);
+            solver_allreduce<A, 3>(v3, slots, wscr, 0, tx, cluster, C, rank, halo_in);
             g = v3[0];
             dlt = v3[1];
             gg = v3[2];
@@ -1723,16 +1741,10 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) w[q] = T(0);
             }
-            if (first_knot) {
-                T *dst = cluster.map_shared_rank(wh_next, rank - 1) + NP + i;
-#pragma unroll
-                for (int q = 0; q < RPT; ++q) dst[q] = w[q];
-            }
-            if (last_knot) {
-                T *dst = cluster.map_shared_rank(wh_next, rank + 1) + i;
-#pragma unroll
-                for (int q = 0; q < RPT; ++q) dst[q] = w[q];
-            }
+            // halo buffer b travels with reduction buffer b: (iter + 1) & 1
+            const int buf = (int)((iter + 1) & 1);
+            if (first_knot) push_halo_tx<T, RPT>(wh_next + NP + i, rank - 1, w, tx, buf);
+            if (last_knot) push_halo_tx<T, RPT>(wh_next + i, rank + 1, w, tx, buf);
             A dn;
             {
                 A v3[3] = {A(0), A(0), A(0)};
@@ -1742,7 +1754,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
                     acc_madd(v3[1], w[q], u[q]);
                     if (relres) acc_madd(v3[2], r[q], r[q]);
                 }
-                cluster_allreduce<A, 3>(v3, slots, wscr, (iter + 1) & 1, cluster, C, rank);
+                solver_allreduce<A, 3>(v3, slots, wscr, buf, tx, cluster, C, rank, halo_in);
                 g_new = v3[0];
                 dn = v3[1];
                 rr = v3[2];
@@ -1764,6 +1776,9 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
             for (int q = 0; q < RPT; ++q) lam_out[(size_t)k * n + i + q] = lam[q];
         }
         if (rank == 0 && tid == 0) {
+            if (C > 1)  // a reduction wait of some CTA of the cluster gave up
+                for (uint32_t c = 0; c < C; ++c)
+                    if (*cluster.map_shared_rank(tx.timed_out, c)) status = ST_TIMEOUT;
             SysResult res;
             res.iters = iter;
             res.status = status;
@@ -1776,6 +1791,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
         }
         stamp.done(lp, item, iter);
     }
+    if (C > 1) cluster.sync();  // every transaction-counted store into this CTA has landed
 }
 
 }  // namespace gbdpcg

@@ -84,7 +84,8 @@ def parse():
     ap.add_argument("--cluster-size", type=int, default=0, help="pin the CTAs per system (profiling; 0: chosen)")
     ap.add_argument("--host-pieces", type=int, default=0,
                     help="pieces the end-to-end path pipelines copies and solves in (0: automatic)")
-    ap.add_argument("--tune", default="shapes+recurrence", choices=["off", "shapes", "shapes+recurrence", "shapes+algorithms"],
+    ap.add_argument("--tune", default="shapes+recurrence+plan",
+                    choices=["off", "shapes", "shapes+recurrence", "shapes+recurrence+plan", "shapes+algorithms"],
                     help="autotune the plan before timing (untimed set-up, like building the plan)")
     return ap.parse_args()
 
@@ -885,6 +886,7 @@ def main():
         return
     tune_s = 0.0
     tune_flags = {"off": None, "shapes": 0, "shapes+recurrence": gbdpcg.TUNE_RECURRENCE,
+                  "shapes+recurrence+plan": gbdpcg.TUNE_RECURRENCE | gbdpcg.TUNE_WHOLE_PLAN,
                   "shapes+algorithms": gbdpcg.TUNE_RECURRENCE | gbdpcg.TUNE_SINGLE_REDUCTION}[args.tune]
     if tune_flags is not None:
         t0 = time.perf_counter()

@@ -655,10 +655,15 @@ int timeline_buffers(gbdpcg_plan_s *p);
 // longest first and the classes by their largest system, builds the device
 // work list, sizes each persistent grid to the clusters that fit at once, and
 // drops a captured graph (the next execution captures the new launches).
-int plan_layout(gbdpcg_plan_s *p) {
+// Merges the classes that share a launch shape, orders each class's systems
+// by decreasing cost n^2 N (the queue hands out the longest first) and the
+// classes by their largest system, and sizes each grid to the clusters that
+// fit at once; `order` receives the work list of all classes.
+int layout_classes(const std::vector<SysDesc> &descs, std::vector<PlanClass> &classes,
+                   std::vector<uint32_t> &order) {
     std::vector<PlanClass> merged;
     std::map<std::tuple<const void *, uint32_t, uint32_t>, size_t> index;
-    for (auto &pc : p->classes) {
+    for (auto &pc : classes) {
         auto key = std::make_tuple((const void *)pc.sh.vi, pc.sh.C, pc.sh.threads);
         auto it = index.find(key);
         if (it == index.end()) {
@@ -670,17 +675,17 @@ int plan_layout(gbdpcg_plan_s *p) {
             m.kmax = std::max(m.kmax, pc.kmax);
         }
     }
-    p->classes.swap(merged);
-    auto cost = [&](uint32_t i) { return (double)p->descs[i].n * p->descs[i].n * p->descs[i].N; };
-    for (auto &pc : p->classes)
+    classes.swap(merged);
+    auto cost = [&](uint32_t i) { return (double)descs[i].n * descs[i].n * descs[i].N; };
+    for (auto &pc : classes)
         std::stable_sort(pc.items.begin(), pc.items.end(),
                          [&](uint32_t a, uint32_t b) { return cost(a) > cost(b); });
-    std::stable_sort(p->classes.begin(), p->classes.end(),
+    std::stable_sort(classes.begin(), classes.end(),
                      [&](const PlanClass &a, const PlanClass &b) {
                          return cost(a.items[0]) > cost(b.items[0]);
                      });
-    std::vector<uint32_t> order;
-    for (auto &pc : p->classes) {
+    order.clear();
+    for (auto &pc : classes) {
         pc.order_off = (uint32_t)order.size();
         order.insert(order.end(), pc.items.begin(), pc.items.end());
         int active = 0;
@@ -691,6 +696,12 @@ int plan_layout(gbdpcg_plan_s *p) {
                                                     std::to_string(pc.sh.C) + ")");
         pc.grid_clusters = std::min<uint32_t>((uint32_t)pc.items.size(), (uint32_t)active);
     }
+    return GBDPCG_SUCCESS;
+}
+
+int plan_layout(gbdpcg_plan_s *p) {
+    std::vector<uint32_t> order;
+    if (int lrc = layout_classes(p->descs, p->classes, order)) return lrc;
     int rc;
     if ((rc = p->d_order.ensure(sizeof(uint32_t) * std::max<size_t>(1, order.size())))) return rc;
     if ((rc = p->d_queues.ensure(sizeof(uint32_t) * std::max<size_t>(1, p->classes.size())))) return rc;
@@ -1282,11 +1293,27 @@ int build_pieces(gbdpcg_plan_s *p) {
         if (L[i].S_off <= L[i - 1].S_off || L[i].Pinv_off <= L[i - 1].Pinv_off || L[i].vec_off <= L[i - 1].vec_off)
             return GBDPCG_SUCCESS;
     const size_t s = p->dtype ? 8 : 4;
-    // equal shares of S bytes
+    // shares of S bytes, equal but for the last two pieces (3/4 and 1/2 of the
+    // others): the solve of the last piece is the one no copy hides, so a
+    // shorter last piece ends the pipeline sooner
+    std::vector<double> bound(k);
+    {
+        std::vector<double> w(k, 1.0);
+        if (k >= 4) {
+            w[k - 2] = 0.75;
+            w[k - 1] = 0.5;
+        }
+        double sum = 0, acc = 0;
+        for (double x : w) sum += x;
+        for (uint32_t j = 0; j < k; ++j) {
+            bound[j] = acc / sum;  // piece j starts at this share
+            acc += w[j];
+        }
+    }
     std::vector<uint32_t> cut = {0};
     const double total = (double)p->bytes_S;
     for (uint32_t i = 1; i < count && cut.size() < k; ++i)
-        if ((double)L[i].S_off * s >= total * cut.size() / k) cut.push_back(i);
+        if ((double)L[i].S_off * s >= total * bound[cut.size()]) cut.push_back(i);
     cut.push_back(count);
     gbdpcg_config cfg = p->cfg;
     cfg.host_pieces = 1;
@@ -1658,13 +1685,138 @@ std::vector<Candidate> tune_candidates(gbdpcg_plan_s *p, const PlanClass &base,
     return out;
 }
 
+// The whole-plan pass of the autotuner (GBDPCG_TUNE_WHOLE_PLAN).  Each class
+// was tuned alone, with the whole GPU to itself; in the plan the classes run
+// side by side on several streams, where what counts is how many SM-seconds a
+// class takes rather than how soon it finishes alone (a shape that finishes
+// first by spreading thin clusters over every SM can lose to one that packs
+// its systems densely).  So the plan is timed as it will run, every class
+// launched on the plan's streams with its systems solving from zero into
+// scratch, and each class in turn (the longest alone first) tries its other
+// shapes that came within 30% of its best alone; a change is kept when the
+// whole plan gets faster by more than 1%.  The plan's own lambda and results
+// are not written.
+int tune_whole_plan(gbdpcg_plan_s *p, const std::vector<std::vector<std::pair<float, Candidate>>> &timed,
+                    uint32_t reps, cudaStream_t st, cudaEvent_t e0, cudaEvent_t e1, bool log) {
+    const size_t sv = (p->f64 || p->refine) ? 8 : 4;
+    size_t need = 0;
+    for (const auto &d : p->descs) need += round_up((size_t)d.n * d.N * sv, 256);
+    DevBuf scratch, d_wd, d_ord, d_q, d_res;
+    int rc;
+    if ((rc = scratch.ensure(std::max<size_t>(need, 256)))) return rc;
+    if ((rc = d_wd.ensure(sizeof(SysDesc) * p->count))) return rc;
+    if ((rc = d_ord.ensure(sizeof(uint32_t) * p->count))) return rc;
+    if ((rc = d_q.ensure(sizeof(uint32_t) * p->classes.size()))) return rc;
+    if ((rc = d_res.ensure(sizeof(SysResult) * p->nresults))) return rc;
+    std::vector<SysDesc> wd = p->descs;
+    size_t off = 0;
+    for (auto &d : wd) {
+        d.lambda = scratch.as<char>() + off;
+        d.lambda0 = nullptr;
+        d.flags |= SYS_LAMBDA0_ZERO;
+        off += round_up((size_t)d.n * d.N * sv, 256);
+    }
+    GB_CUDA(cudaMemcpyAsync(d_wd.p, wd.data(), sizeof(SysDesc) * p->count, cudaMemcpyHostToDevice, st));
+    const uint32_t ns = (uint32_t)p->streams.size();
+    const uint32_t treps = std::max<uint32_t>(reps, 4);  // the fastest of several runs: steps differ by ~1%
+    auto time_plan = [&](std::vector<PlanClass> cls, float *ms) -> int {
+        std::vector<uint32_t> order;
+        int lrc = layout_classes(p->descs, cls, order);
+        if (lrc) return lrc;
+        GB_CUDA(cudaMemcpyAsync(d_ord.p, order.data(), sizeof(uint32_t) * order.size(), cudaMemcpyHostToDevice,
+                                st));
+        const uint32_t nc = (uint32_t)cls.size();
+        float best = 1e30f;
+        for (uint32_t r = 0; r <= treps; ++r) {
+            GB_CUDA(cudaMemsetAsync(d_q.p, 0, sizeof(uint32_t) * nc, st));
+            GB_CUDA(cudaEventRecord(e0, st));
+            GB_CUDA(cudaEventRecord(p->events[0], st));
+            for (uint32_t c = 0; c < nc; ++c) {
+                cudaStream_t s = p->streams[c % ns];
+                if (c < ns) GB_CUDA(cudaStreamWaitEvent(s, p->events[0], 0));
+                const PlanClass &pc = cls[c];
+                LaunchParams lp;
+                memset(&lp, 0, sizeof(lp));
+                lp.descs = d_wd.as<SysDesc>();
+                lp.order = d_ord.as<uint32_t>() + pc.order_off;
+                lp.count = (uint32_t)pc.items.size();
+                lp.kmax = pc.kmax;
+                lp.queue = d_q.as<uint32_t>() + c;
+                lp.results = d_res.as<SysResult>();
+                lp.launch_id = c;
+                if ((lrc = launch_cluster(pc.sh, lp, pc.grid_clusters, s))) return lrc;
+            }
+            for (uint32_t s = 0; s < std::min(ns, nc); ++s) {
+                GB_CUDA(cudaEventRecord(p->events[1 + s], p->streams[s]));
+                GB_CUDA(cudaStreamWaitEvent(st, p->events[1 + s], 0));
+            }
+            GB_CUDA(cudaEventRecord(e1, st));
+            GB_CUDA(cudaEventSynchronize(e1));
+            float t = 0;
+            GB_CUDA(cudaEventElapsedTime(&t, e0, e1));
+            if (r > 0) best = std::min(best, t);
+        }
+        *ms = best;
+        return GBDPCG_SUCCESS;
+    };
+    std::vector<PlanClass> cur = p->classes;
+    float t_best = 0;
+    if ((rc = time_plan(cur, &t_best))) return rc;
+    if (log) fprintf(stderr, "gbdpcg tune: whole plan %.4f ms (classes tuned alone)\n", t_best);
+    // the longest classes alone first
+    std::vector<size_t> idx(cur.size());
+    for (size_t i = 0; i < idx.size(); ++i) idx[i] = i;
+    auto alone = [&](size_t i) {
+        float b = 1e30f;
+        for (auto &t : timed[i]) b = std::min(b, t.first);
+        return b;
+    };
+    std::stable_sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return alone(a) > alone(b); });
+    for (size_t i : idx) {
+        const float best_alone = alone(i);
+        std::vector<std::pair<float, Candidate>> alts = timed[i];
+        std::stable_sort(alts.begin(), alts.end(),
+                         [](const std::pair<float, Candidate> &a, const std::pair<float, Candidate> &b) {
+                             return a.first < b.first;
+                         });
+        int tried = 0;
+        for (const auto &a : alts) {
+            if (a.first > 1.3f * best_alone || tried >= 4) break;
+            const Candidate &cd = a.second;
+            if (cd.sh.vi == cur[i].sh.vi && cd.sh.C == cur[i].sh.C && cd.sh.threads == cur[i].sh.threads) continue;
+            ++tried;
+            std::vector<PlanClass> trial = cur;
+            trial[i].sh = cd.sh;
+            trial[i].kmax = cd.kmax;
+            float t = 0;
+            if (time_plan(trial, &t) != GBDPCG_SUCCESS) {
+                cudaGetLastError();
+                GB_CUDA(cudaStreamSynchronize(st));
+                continue;
+            }
+            if (log) {
+                const KernelVariant &v = cd.sh.vi->v;
+                fprintf(stderr, "gbdpcg tune: whole plan %.4f ms with class %zu (%zu systems) at st=%d rpt=%d alg=%d C=%u threads=%u%s\n",
+                        t, i, cur[i].items.size(), v.st, v.rpt, v.alg, cd.sh.C, cd.sh.threads, t < 0.99f * t_best ? " (kept)" : "");
+            }
+            if (t < 0.99f * t_best) {
+                t_best = t;
+                cur[i] = trial[i];
+            }
+        }
+    }
+    GB_CUDA(cudaStreamSynchronize(st));
+    p->classes = cur;
+    return GBDPCG_SUCCESS;
+}
+
 }  // namespace
 
 extern "C" {
 
 int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_stream_t stream_) {
     if (!p) return fail(GBDPCG_ERR_INVALID_ARGUMENT, "plan is NULL");
-    if (flags & ~(uint32_t)(GBDPCG_TUNE_RECURRENCE | GBDPCG_TUNE_SINGLE_REDUCTION))
+    if (flags & ~(uint32_t)(GBDPCG_TUNE_RECURRENCE | GBDPCG_TUNE_SINGLE_REDUCTION | GBDPCG_TUNE_WHOLE_PLAN))
         return fail(GBDPCG_ERR_INVALID_ARGUMENT, "unknown tune flag");
     if (p->classes.empty()) return GBDPCG_SUCCESS;
     HandleScope scope(p->h->device);
@@ -1724,7 +1876,10 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
         fprintf(stderr, "gbdpcg tune: systems=%zu n=%u-%u N=%u-%u | np=%d st=%d rpt=%d alg=%d acc=%d C=%u threads=%u grid=%u | %.4f ms%s\n",
                 pc.items.size(), nmin, nmax, Nmin, Nmax, v.np, v.st, v.rpt, v.alg, v.acc, sh.C, sh.threads, grid, ms, tag);
     };
-    for (auto &pc : p->classes) {
+    // every timed shape of each class, for the whole-plan pass
+    std::vector<std::vector<std::pair<float, Candidate>>> timed(p->classes.size());
+    for (size_t ci = 0; ci < p->classes.size(); ++ci) {
+        PlanClass &pc = p->classes[ci];
         // this class's systems solve from zero into the scratch buffers
         size_t off = 0;
         char *base = scratch.as<char>();
@@ -1779,6 +1934,7 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
         best.sh = pc.sh;
         best.kmax = pc.kmax;
         best.grid = pc.grid_clusters;
+        timed[ci].emplace_back(best_ms, best);
         for (const Candidate &cd : tune_candidates(p, pc, pc.items, flags)) {
             if (cd.sh.vi == pc.sh.vi && cd.sh.C == pc.sh.C && cd.sh.threads == pc.sh.threads) continue;
             float ms = 0;
@@ -1790,6 +1946,7 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
                 continue;
             }
             log_shape(pc, cd.sh, cd.grid, ms, "");
+            timed[ci].emplace_back(ms, cd);
             if (ms < best_ms * 0.98f) {
                 best_ms = ms;
                 best = cd;
@@ -1797,11 +1954,17 @@ int gbdpcg_plan_autotune(gbdpcg_plan_t p, uint32_t flags, uint32_t reps, gbdpcg_
         }
         pc.sh = best.sh;
         pc.kmax = best.kmax;
-        TuneChoice ch{best.sh.vi->v.st, best.sh.vi->v.rpt, best.sh.vi->v.alg, best.sh.C, best.sh.threads};
-        for (uint32_t i : pc.items) learned.emplace_back(tune_key(p, fused ? 2 : (adjoint ? 1 : 0), p->descs[i].n, p->descs[i].N), ch);
         for (uint32_t i : pc.items) td[i] = p->descs[i];
     }
     GB_CUDA(cudaStreamSynchronize(st));
+    if ((flags & GBDPCG_TUNE_WHOLE_PLAN) && !adjoint && !fused && p->classes.size() > 1 &&
+        (rc = tune_whole_plan(p, timed, reps, st, e0, e1, log))) return rc;
+    for (auto &pc : p->classes) {
+        const Shape &sh = pc.sh;
+        TuneChoice ch{sh.vi->v.st, sh.vi->v.rpt, sh.vi->v.alg, sh.C, sh.threads};
+        for (uint32_t i : pc.items)
+            learned.emplace_back(tune_key(p, fused ? 2 : (adjoint ? 1 : 0), p->descs[i].n, p->descs[i].N), ch);
+    }
     {
         std::lock_guard<std::mutex> lk(p->h->tune_mu);
         for (auto &kv : learned) p->h->tune[kv.first] = kv.second;

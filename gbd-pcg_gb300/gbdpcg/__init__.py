@@ -28,7 +28,7 @@ CONVERGED, MAX_ITER, BREAKDOWN, TIMEOUT, REJECTED = 0, 1, 2, 3, -1
 EXIT_REFERENCE, EXIT_RELRES = 0, 1
 PINV_CBTD, PINV_BLOCKDIAG = 0, 1
 ALGO_AUTO, ALGO_CLUSTER, ALGO_PLAIN, ALGO_SINGLE_REDUCTION, ALGO_RECURRENCE = 0, 1, 2, 3, 4
-TUNE_RECURRENCE, TUNE_SINGLE_REDUCTION = 1, 2
+TUNE_RECURRENCE, TUNE_SINGLE_REDUCTION, TUNE_WHOLE_PLAN = 1, 2, 4
 DOT_NATIVE, DOT_FP64, DOT_FLOAT2 = 0, 1, 2
 STORAGE_AUTO, STORAGE_REGISTERS, STORAGE_SHARED, STORAGE_SPLIT, STORAGE_HYBRID, STORAGE_TMEM = 0, 1, 2, 3, 4, 5
 STORAGE_STREAM = 6

@@ -511,8 +511,14 @@ GBDPCG_API int gbdpcg_plan_timeline_read(gbdpcg_plan_t plan, gbdpcg_stamp *stamp
  * `reps` timed launches per shape (0 means 2).  Synchronous. */
 enum {
     GBDPCG_TUNE_RECURRENCE = 1,      /* with GBDPCG_ALGO_AUTO also try the recurrence form */
-    GBDPCG_TUNE_SINGLE_REDUCTION = 2 /* with GBDPCG_ALGO_AUTO and a compact Phi^-1 also try the
-                                        single-reduction (Chronopoulos-Gear) form */
+    GBDPCG_TUNE_SINGLE_REDUCTION = 2, /* with GBDPCG_ALGO_AUTO and a compact Phi^-1 also try the
+                                         single-reduction (Chronopoulos-Gear) form */
+    GBDPCG_TUNE_WHOLE_PLAN = 4        /* then time the whole plan as it runs (its classes side by
+                                         side on the plan's streams, solving into scratch) and let
+                                         each class, the longest first, take another of its shapes
+                                         within 30% of its best alone when that makes the whole
+                                         plan faster by more than 1% (forward plans of two or more
+                                         classes) */
 };
 GBDPCG_API int gbdpcg_plan_autotune(gbdpcg_plan_t plan, uint32_t flags, uint32_t reps, gbdpcg_stream_t stream);
 /* The handle's tuning table as text, one line per (n, N) entry:

@@ -38,7 +38,10 @@ def _cfg(gb, **kw):
     return gb.config(max_iter=300, exit_tol=1e-6, exit_mode=gb.EXIT_RELRES, **kw)
 
 
-def test_autotuned_plan_matches_oracle(gb, oracle_mod, handle):
+@pytest.mark.parametrize("flags", ["shapes", "whole-plan"])
+def test_autotuned_plan_matches_oracle(gb, oracle_mod, handle, flags):
+    """Tuned shapes solve like the oracle; the whole-plan pass (the plan timed
+    as it runs, solving into scratch) leaves the plan's buffers alone too."""
     import torch
     O = oracle_mod
     d = torch.device("cuda:0")
@@ -48,7 +51,7 @@ def test_autotuned_plan_matches_oracle(gb, oracle_mod, handle):
     before = plan.launches()
     for s in systems:
         s["lambda"].fill_(7.0)  # the tuner must not touch the plan's buffers
-    after = plan.autotune(reps=1)
+    after = plan.autotune(reps=1, flags=0 if flags == "shapes" else gb.TUNE_WHOLE_PLAN)
     assert sum(l["systems"] for l in after) == len(systems)
     assert len(after) <= len(before)
     for l in after:

@@ -735,9 +735,13 @@ struct TxReduce {
 // cluster_allreduce: warp sums with sum32 into slot [rank*W + w] of every CTA,
 // then every thread sums the slots.  `extra_bytes`: halo values the
 // neighbours send on the same buffer (push_halo_tx) before this call.
+// In two halves, so that work that needs neither the sums nor the halos can
+// run while the partials travel: cluster_allreduce_tx_send stores this
+// warp's partials into every CTA's slots, cluster_allreduce_tx_finish waits
+// for this CTA's bytes and sums the slots.
 template <typename A, int NQ>
-__device__ __forceinline__ void cluster_allreduce_tx(A (&v)[NQ], A *slots, A *wscr, int buf, TxReduce &tx,
-                                                     uint32_t C, uint32_t rank, uint32_t extra_bytes = 0) {
+__device__ __forceinline__ void cluster_allreduce_tx_send(A (&v)[NQ], A *slots, A *wscr, int buf, TxReduce &tx,
+                                                          uint32_t C, uint32_t rank, uint32_t extra_bytes = 0) {
     static_assert(NQ <= kMaxValues, "slot array holds kMaxValues values");
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nwarps = blockDim.x >> 5;
@@ -757,11 +761,25 @@ __device__ __forceinline__ void cluster_allreduce_tx(A (&v)[NQ], A *slots, A *ws
         for (int q = 0; q < NQ; ++q)
             st_async(rsl + (uint32_t)((q * stride + my) * sizeof(A)), sum32(ws + q * 32), rbar);
     }
+}
+
+template <typename A, int NQ>
+__device__ __forceinline__ void cluster_allreduce_tx_finish(A (&v)[NQ], A *slots, int buf, TxReduce &tx,
+                                                            uint32_t C) {
+    const uint32_t stride = (uint32_t)slot_stride(C);
+    const A *sl = slots + (size_t)buf * stride * kMaxValues;
     mbar_wait_bounded(tx.bar + buf, (tx.parity >> buf) & 1u, tx.timed_out);
     tx.parity ^= 1u << buf;
-    sum_all_slots<A, NQ>(v, sl, stride, total);
+    sum_all_slots<A, NQ>(v, sl, stride, C * (blockDim.x >> 5));
 #pragma unroll
     for (int q = 0; q < NQ; ++q) v[q] = acc_normalize(v[q]);
+}
+
+template <typename A, int NQ>
+__device__ __forceinline__ void cluster_allreduce_tx(A (&v)[NQ], A *slots, A *wscr, int buf, TxReduce &tx,
+                                                     uint32_t C, uint32_t rank, uint32_t extra_bytes = 0) {
+    cluster_allreduce_tx_send<A, NQ>(v, slots, wscr, buf, tx, C, rank, extra_bytes);
+    cluster_allreduce_tx_finish<A, NQ>(v, slots, buf, tx, C);
 }
 
 // Halo values for a neighbouring CTA, sent like the reduction partials: RPT
@@ -1247,6 +1265,13 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 }
                 if (first_knot) push_halo_tx<T, RPT>(vp + (K + 1) * NP + i, rank - 1, z, tx, 1);
                 if (last_knot) push_halo_tx<T, RPT>(vp + i, rank + 1, z, tx, 1);
+                // w = S z is needed only after the reduction, and only the rows
+                // next to a neighbour read its halo: the other warps form w
+                // while the partials and halos travel (once this CTA's z rows
+                // are all in the window), the rest after the wait.  Either
+                // way, before the exit test, so that its loads and FMAs
+                // interleave with the slot sums.
+                T w[RPT];
                 {
                     A v2[2] = {A(0), A(0)};
 #pragma unroll
@@ -1254,7 +1279,17 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                         acc_madd(v2[0], r[q], z[q]);
                         if (relres) acc_madd(v2[1], r[q], r[q]);
                     }
-                    solver_allreduce<A, 2>(v2, slots, wscr, 1, tx, cluster, C, rank, halo_in);
+                    if (C > 1) {
+                        cluster_allreduce_tx_send<A, 2>(v2, slots, wscr, 1, tx, C, rank, halo_in);
+                        __syncthreads();  // this CTA's z rows are in the window
+                        const bool halo_rows = __any_sync(0xffffffffu, first_knot || last_knot);
+                        if (!halo_rows) matS_rows(w);
+                        cluster_allreduce_tx_finish<A, 2>(v2, slots, 1, tx, C);
+                        if (halo_rows) matS_rows(w);
+                    } else {
+                        cluster_allreduce<A, 2>(v2, slots, wscr, 1, cluster, C, rank);
+                        matS_rows(w);
+                    }
                     eta_new = v2[0];
                     rr = v2[1];
                 }
@@ -1263,8 +1298,6 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                 if (relres ? (rr <= thr) : (acc_abs(eta_new) < tol)) { status = ST_CONVERGED; break; }
                 const T beta = acc_ratio<T>(eta_new, eta);
                 eta = eta_new;
-                T w[RPT];
-                matS_rows(w);
 #pragma unroll
                 for (int q = 0; q < RPT; ++q) {
                     p[q] = fma_rn(beta, p[q], z[q]);

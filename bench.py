@@ -391,8 +391,9 @@ def n128_seed_sweep(gbdpcg, h, dev, reps=20, seeds=range(10)):
 def timeline_summary(stamps, cta_sm, launches, sm_count):
     """Reads one execution's timeline (gbdpcg_plan_timeline_read): per launch
     class, the share of each system's time spent staging its rows, the us per
-    PCG iteration, and how long the class's clusters sat idle after the
-    class's last system started; over the step, the fraction of SM-time with
+    PCG iteration, the mean time between two systems of one cluster (taking
+    the next from the queue), and how long the class's clusters sat idle
+    after the class's last system started; over the step, the fraction of SM-time with
     no CTA of the solver resident and busy, and the step's tail (from the last
     moment 90% of the SMs were busy to the end)."""
     ok = stamps["iters"] > 0
@@ -402,6 +403,7 @@ def timeline_summary(stamps, cta_sm, launches, sm_count):
     T = t_end - t0
     cta_base = np.concatenate([[0], np.cumsum([l["ctas"] for l in launches if l["cluster"] > 0])])
     classes = []
+    all_gaps = []
     for c, l in enumerate(launches):
         if l["cluster"] == 0:
             continue
@@ -416,6 +418,13 @@ def timeline_summary(stamps, cta_sm, launches, sm_count):
         last_done = {}
         for rec in s:
             last_done[int(rec["cluster"])] = max(last_done.get(int(rec["cluster"]), 0), int(rec["t_done"]))
+        # between two systems of one cluster: from the first's results written
+        # to the second taken from the queue (the pop and its cluster barrier)
+        gaps = []
+        for cl in np.unique(s["cluster"]):
+            r = np.sort(s[s["cluster"] == cl], order="t_pop")
+            gaps.extend((r["t_pop"][1:].astype(np.int64) - r["t_done"][:-1].astype(np.int64)).tolist())
+        all_gaps.extend(gaps)
         idle_cta_ns = sum(c_end - v for v in last_done.values()) * l["cluster"]
         classes.append({"launch": c, "cluster": l["cluster"], "threads": l["threads"], "storage": l["storage"],
                         "rows_per_thread": l["rows_per_thread"], "algorithm": l["algorithm"],
@@ -423,7 +432,8 @@ def timeline_summary(stamps, cta_sm, launches, sm_count):
                         "staging_share": float(stage.sum() / busy.sum()),
                         "us_per_iteration_median": float(np.median(per_iter) / 1e3),
                         "start_ms": (int(s["t_pop"].min()) - t0) / 1e6, "end_ms": (c_end - t0) / 1e6,
-                        "tail_idle_cta_ms": idle_cta_ns / 1e6})
+                        "tail_idle_cta_ms": idle_cta_ns / 1e6,
+                        "between_systems_us_mean": float(np.mean(gaps) / 1e3) if gaps else 0.0})
     # busy SMs over the step: an SM is busy while a CTA of a cluster is solving a system
     ev = []
     for rec in st:
@@ -453,6 +463,7 @@ def timeline_summary(stamps, cta_sm, launches, sm_count):
     return {"step_ms": T / 1e6, "sm_busy_frac": busy_sm_ns / (sm_count * T), "tail_ms": (t_end - last_full) / 1e6,
             "tail_share": (t_end - last_full) / T,
             "staging_share": float(((st["t_staged"] - st["t_pop"]).sum()) / (st["t_done"] - st["t_pop"]).sum()),
+            "between_systems_share": float(sum(all_gaps) / (st["t_done"] - st["t_pop"]).sum()),
             "classes": classes}
 
 

@@ -517,10 +517,6 @@ __device__ __forceinline__ A sum_slots(const A *p, uint32_t used = M) {
     return (c0 + c1) + (c2 + c3);
 }
 
-template <typename A>
-__device__ __forceinline__ A sum32(const A *p) {
-    return sum_slots<A, 32>(p);
-}
 
 // The slots of one reduction value, summed identically in every thread: up
 // to 32 slots (zero beyond `total`, not read) with vector loads and four chains, and up
@@ -549,10 +545,11 @@ __device__ __forceinline__ void sum_all_slots(A (&v)[NQ], const A *sl, uint32_t 
 }
 
 // Cluster-wide sum of NQ values, identical in every thread of the cluster.
-//   1. each lane stores its values in its warp's scratch row; after a warp
-//      barrier, lanes 0..max(C,1)-1 each re-read the 32 values (vector loads,
-//      four chains: no shuffle chain) and store the warp's sums into slot
-//      [rank*W + w] of CTA `lane` (DSMEM stores; local when C == 1);
+//   1. a warp butterfly (xor shuffles, the NQ values interleaved) gives every
+//      lane of a warp the warp's sums, the same bits in every lane (each step
+//      adds the same two values, in either order); lanes 0..max(C,1)-1 store
+//      them into slot [rank*W + w] of CTA `lane` (DSMEM stores; local when
+//      C == 1);
 //   2. one barrier (barrier.cluster, or __syncthreads when C == 1), whose
 //      release/acquire makes the stores — and any halo pushes the caller made
 //      before this call — visible;
@@ -562,25 +559,30 @@ __device__ __forceinline__ void sum_all_slots(A (&v)[NQ], const A *sl, uint32_t 
 // Every thread of every CTA reads the same slots in the same order, so all hold
 // the same bits.  `buf` alternates between call sites so that a slot array is
 // rewritten only after a barrier that every reader has passed.  Slots
-// [buf][q][C*32] are zeroed at kernel start; wscr is [warp][q][32].
+// [buf][q][C*32] are zeroed at kernel start.  (The butterfly's five dependent
+// shuffle rounds, with the values of a reduction interleaved, beat re-reading
+// the warp's 32 values from shared memory by one lane: one value 162 against
+// 192 ns, two 224 against 326, three 300 against 504, for a 256-thread CTA.)
+// `wscr` is not used (kept for the callers' shared-memory layout).
 template <typename A, int NQ>
 __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, A *wscr, int buf,
                                                   const cg::cluster_group &cluster, uint32_t C,
                                                   uint32_t rank) {
     static_assert(NQ <= kMaxValues, "slot array holds kMaxValues values");
+    (void)wscr;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nwarps = blockDim.x >> 5;
     const uint32_t stride = (uint32_t)slot_stride(C);
     A *sl = slots + (size_t)buf * stride * kMaxValues;
-    A *ws = wscr + (size_t)warp * kMaxValues * 32;
+    A t[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) ws[q * 32 + lane] = v[q];
-    __syncwarp();
+    for (int q = 0; q < NQ; ++q) t[q] = v[q];
+    warp_sum_n<A, NQ>(t);
     const uint32_t my = rank * nwarps + warp, total = C * nwarps;
     if (lane < C) {
         A *dst = (C == 1) ? sl : cluster.map_shared_rank(sl, lane);
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) dst[q * stride + my] = sum32(ws + q * 32);
+        for (int q = 0; q < NQ; ++q) dst[q * stride + my] = t[q];
     }
     if (C == 1)
         __syncthreads();
@@ -732,8 +734,8 @@ struct TxReduce {
 // Cluster-wide sum of NQ values, identical in every thread of the cluster, for
 // C >= 2 (C == 1 uses cluster_allreduce, whose barrier is __syncthreads).
 // Same slots, same summation order and same result bits as
-// cluster_allreduce: warp sums with sum32 into slot [rank*W + w] of every CTA,
-// then every thread sums the slots.  `extra_bytes`: halo values the
+// cluster_allreduce: warp sums by the butterfly into slot [rank*W + w] of
+// every CTA, then every thread sums the slots.  `extra_bytes`: halo values the
 // neighbours send on the same buffer (push_halo_tx) before this call.
 // In two halves, so that work that needs neither the sums nor the halos can
 // run while the partials travel: cluster_allreduce_tx_send stores this
@@ -746,20 +748,20 @@ __device__ __forceinline__ void cluster_allreduce_tx_send(A (&v)[NQ], A *slots, 
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nwarps = blockDim.x >> 5;
     const uint32_t stride = (uint32_t)slot_stride(C);
+    (void)wscr;
     A *sl = slots + (size_t)buf * stride * kMaxValues;
-    A *ws = wscr + (size_t)warp * kMaxValues * 32;
+    A t[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) ws[q * 32 + lane] = v[q];
-    __syncwarp();
+    for (int q = 0; q < NQ; ++q) t[q] = v[q];
+    warp_sum_n<A, NQ>(t);
     if (threadIdx.x == 0)
         mbar_arrive_expect_tx(tx.bar + buf, (uint32_t)(NQ * C * nwarps * sizeof(A)) + extra_bytes);
-    const uint32_t my = rank * nwarps + warp, total = C * nwarps;
+    const uint32_t my = rank * nwarps + warp;
     if (lane < C) {
         const uint32_t rbar = map_rank_u32(smem_u32(tx.bar + buf), lane);
         const uint32_t rsl = map_rank_u32(smem_u32(sl), lane);
 #pragma unroll
-        for (int q = 0; q < NQ; ++q)
-            st_async(rsl + (uint32_t)((q * stride + my) * sizeof(A)), sum32(ws + q * 32), rbar);
+        for (int q = 0; q < NQ; ++q) st_async(rsl + (uint32_t)((q * stride + my) * sizeof(A)), t[q], rbar);
     }
 }
 

@@ -477,67 +477,68 @@ __device__ __forceinline__ void warp_sum_n(A (&v)[NQ]) {
     }
 }
 
-// Sum of the first `used` of the M (32 or 64) values at p (A-typed, 16-byte
-// aligned; values from `used` on are zero) with vector loads into four
-// accumulator chains (element j into chain j mod 4), then (c0+c1)+(c2+c3).
-// Whole groups of four are read up to `used`; the groups after it would only
-// add zeros to chains that started at +0, which leaves their bits unchanged,
-// so they are skipped (a warp-uniform bound).
-template <typename A, int M>
-__device__ __forceinline__ A sum_slots(const A *p, uint32_t used = M) {
-    static_assert(M % 4 == 0, "four chains");
-    A c0 = A(0), c1 = A(0), c2 = A(0), c3 = A(0);
+// Pairwise sums of M slots at p (A-typed, 16-byte aligned; M = 4, 8, 16, 32
+// or 64): four or eight values from vector loads, added as a balanced tree,
+// then the halves added.  Straight-line code: every load is issued at once.
+template <typename A>
+__device__ __forceinline__ void load4(const A *p, A (&x)[4]) {
     if constexpr (std::is_same<A, f2acc>::value) {
-#pragma unroll
-        for (int j = 0; j < M / 4; ++j) {
-            if ((uint32_t)(4 * j) < used) {
-                const float4 t0 = reinterpret_cast<const float4 *>(p)[2 * j];
-                const float4 t1 = reinterpret_cast<const float4 *>(p)[2 * j + 1];
-                c0 += f2acc(t0.x, t0.y); c1 += f2acc(t0.z, t0.w); c2 += f2acc(t1.x, t1.y); c3 += f2acc(t1.z, t1.w);
-            }
-        }
+        const float4 t0 = reinterpret_cast<const float4 *>(p)[0];
+        const float4 t1 = reinterpret_cast<const float4 *>(p)[1];
+        x[0] = f2acc(t0.x, t0.y); x[1] = f2acc(t0.z, t0.w); x[2] = f2acc(t1.x, t1.y); x[3] = f2acc(t1.z, t1.w);
     } else if constexpr (sizeof(A) == 4) {
-#pragma unroll
-        for (int j = 0; j < M / 4; ++j) {
-            if ((uint32_t)(4 * j) < used) {
-                const float4 t = reinterpret_cast<const float4 *>(p)[j];
-                c0 += t.x; c1 += t.y; c2 += t.z; c3 += t.w;
-            }
-        }
+        const float4 t = reinterpret_cast<const float4 *>(p)[0];
+        x[0] = t.x; x[1] = t.y; x[2] = t.z; x[3] = t.w;
     } else {
-#pragma unroll
-        for (int j = 0; j < M / 4; ++j) {
-            if ((uint32_t)(4 * j) < used) {
-                const double2 t0 = reinterpret_cast<const double2 *>(p)[2 * j];
-                const double2 t1 = reinterpret_cast<const double2 *>(p)[2 * j + 1];
-                c0 += t0.x; c1 += t0.y; c2 += t1.x; c3 += t1.y;
-            }
-        }
+        const double2 t0 = reinterpret_cast<const double2 *>(p)[0];
+        const double2 t1 = reinterpret_cast<const double2 *>(p)[1];
+        x[0] = t0.x; x[1] = t0.y; x[2] = t1.x; x[3] = t1.y;
     }
-    return (c0 + c1) + (c2 + c3);
 }
 
+template <typename A, int M>
+__device__ __forceinline__ A tree_slots(const A *p) {
+    static_assert(M == 4 || M == 8 || M == 16 || M == 32 || M == 64, "a power of two from 4 to 64");
+    if constexpr (M == 4) {
+        A x[4];
+        load4<A>(p, x);
+        return (x[0] + x[1]) + (x[2] + x[3]);
+    } else {
+        return tree_slots<A, M / 2>(p) + tree_slots<A, M / 2>(p + M / 2);
+    }
+}
 
-// The slots of one reduction value, summed identically in every thread: up
-// to 32 slots (zero beyond `total`, not read) with vector loads and four chains, and up
-// to 64 that way too for float accumulators; more with a strided sum per lane
-// and a warp butterfly.  (Double and float-float additions are many times
-// dearer than float ones on GB300, so for them every thread adding 64 slots
-// costs more than the butterfly's shuffles.)
+// The slots of one reduction value, summed identically in every thread (the
+// slots from `total` on are zero; a warp-uniform branch picks the smallest
+// power of two from 4 that covers them): float, the pairwise tree of up to 64
+// slots; double and float-float, whose additions are many times dearer than
+// float ones on GB300, the tree up to 8 slots and otherwise lane l's slots l,
+// l+32, ... finished by a warp butterfly (5 additions a thread); float beyond
+// 64 slots the same way.
 template <typename A, int NQ>
 __device__ __forceinline__ void sum_all_slots(A (&v)[NQ], const A *sl, uint32_t stride, uint32_t total) {
-    if (total <= 32) {
+    constexpr bool F = std::is_same<A, float>::value;
+    if (total <= 4) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) v[q] = sum_slots<A, 32>(sl + q * stride, total);
-    } else if (std::is_same<A, float>::value && total <= 64) {
+        for (int q = 0; q < NQ; ++q) v[q] = tree_slots<A, 4>(sl + q * stride);
+    } else if (total <= 8) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) v[q] = sum_slots<A, 64>(sl + q * stride, total);
+        for (int q = 0; q < NQ; ++q) v[q] = tree_slots<A, 8>(sl + q * stride);
+    } else if (F && total <= 16) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) v[q] = tree_slots<A, 16>(sl + q * stride);
+    } else if (F && total <= 32) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) v[q] = tree_slots<A, 32>(sl + q * stride);
+    } else if (F && total <= 64) {
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) v[q] = tree_slots<A, 64>(sl + q * stride);
     } else {
         const uint32_t lane = threadIdx.x & 31;
 #pragma unroll
         for (int q = 0; q < NQ; ++q) {
-            A s = A(0);
-            for (uint32_t j = lane; j < total; j += 32) s += sl[q * stride + j];
+            A s = lane < total ? sl[q * stride + lane] : A(0);
+            for (uint32_t j = lane + 32; j < total; j += 32) s += sl[q * stride + j];
             v[q] = s;
         }
         warp_sum_n<A, NQ>(v);

@@ -322,8 +322,16 @@ int choose_shape(Registry *reg, bool f64, uint32_t n, uint32_t N, uint32_t layou
         return fail(GBDPCG_ERR_UNSUPPORTED, "the single-reduction algorithm has no float-float accumulation");
     if (tuned && tuned_shape(reg, f64 && !refine, acc, np, ptri, n, N, *tuned, out, fa)) return GBDPCG_SUCCESS;
     const uint32_t first_lo = (cfg.cluster_size == 0 && c_pref > 1) ? c_pref : 1;
+    std::vector<Pref> prefs = storage_prefs(f64 && !refine, ptri, cfg.storage);
+    // A lone FP32 system takes tensor-memory rows first where they fit: its
+    // CTAs have their SMs to themselves anyway (the exclusive tensor-memory
+    // allocation is what keeps that storage out of AUTO for batches), and its
+    // iteration is the shortest there (n = 14, N = 32: 1.1-1.3 us against
+    // 1.4-1.6 us with S in registers and Phi^-1 in shared memory).
+    if (lone && cfg.storage == GBDPCG_STORAGE_AUTO && !f64 && !refine && !ptri)
+        prefs.insert(prefs.begin(), Pref{4, 2});
     for (uint32_t from : {first_lo, 1u}) {
-        for (const Pref &pf : storage_prefs(f64 && !refine, ptri, cfg.storage)) {
+        for (const Pref &pf : prefs) {
             if (pf.rpt > 1 && (n % pf.rpt) != 0) continue;
             if (streamed(pf.st) && lone && ptri && cfg.storage == GBDPCG_STORAGE_AUTO &&
                 cfg.algorithm == GBDPCG_ALGO_AUTO && cfg.cluster_size == 0 && plain_fits(reg, f64, n, N)) {

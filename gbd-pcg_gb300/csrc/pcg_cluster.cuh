@@ -733,15 +733,26 @@ struct TxReduce {
 };
 
 // Cluster-wide sum of NQ values, identical in every thread of the cluster, for
-// C >= 2 (C == 1 uses cluster_allreduce, whose barrier is __syncthreads).
-// Same slots, same summation order and same result bits as
-// cluster_allreduce: warp sums by the butterfly into slot [rank*W + w] of
-// every CTA, then every thread sums the slots.  `extra_bytes`: halo values the
-// neighbours send on the same buffer (push_halo_tx) before this call.
+// C >= 2 (C == 1 uses cluster_allreduce, whose barrier is __syncthreads), in
+// two levels:
+//   1. the warp butterfly gives every warp its sums; lane 0 stores them into
+//      this CTA's local slots (`wscr`, [value][32], zero past the warps);
+//   2. after a CTA barrier, warp 0 sums the local slots (sum_all_slots over
+//      the W warps) and its lanes 0..C-1 send the CTA's sums into slot
+//      [rank] of CTA `lane` (st.async counted on that CTA's mbarrier); thread
+//      0 arms this CTA's mbarrier with the C values per reduced value it
+//      expects plus `extra_bytes` of halo values the neighbours send on the
+//      same buffer (push_halo_tx) before this call;
+//   3. every thread waits for its CTA's bytes and sums the C slots.
+// One CTA sends C values per reduced value instead of C W, and every thread
+// adds C slots instead of C W: the adds of the slot stage move to one warp.
+// The CTA barrier of step 2 also completes this CTA's stores into its own
+// shared memory made before the call (the recurrence form relies on that).
+// `wscr` is written by step 1 of the next call only after every warp has
+// passed step 3 of this one, which needs warp 0's sends, made after its read.
 // In two halves, so that work that needs neither the sums nor the halos can
-// run while the partials travel: cluster_allreduce_tx_send stores this
-// warp's partials into every CTA's slots, cluster_allreduce_tx_finish waits
-// for this CTA's bytes and sums the slots.
+// run while the partials travel: cluster_allreduce_tx_send (steps 1-2),
+// cluster_allreduce_tx_finish (step 3).
 template <typename A, int NQ>
 __device__ __forceinline__ void cluster_allreduce_tx_send(A (&v)[NQ], A *slots, A *wscr, int buf, TxReduce &tx,
                                                           uint32_t C, uint32_t rank, uint32_t extra_bytes = 0) {
@@ -749,20 +760,25 @@ __device__ __forceinline__ void cluster_allreduce_tx_send(A (&v)[NQ], A *slots, 
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nwarps = blockDim.x >> 5;
     const uint32_t stride = (uint32_t)slot_stride(C);
-    (void)wscr;
     A *sl = slots + (size_t)buf * stride * kMaxValues;
     A t[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) t[q] = v[q];
     warp_sum_n<A, NQ>(t);
-    if (threadIdx.x == 0)
-        mbar_arrive_expect_tx(tx.bar + buf, (uint32_t)(NQ * C * nwarps * sizeof(A)) + extra_bytes);
-    const uint32_t my = rank * nwarps + warp;
-    if (lane < C) {
-        const uint32_t rbar = map_rank_u32(smem_u32(tx.bar + buf), lane);
-        const uint32_t rsl = map_rank_u32(smem_u32(sl), lane);
+    if (lane == 0) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) st_async(rsl + (uint32_t)((q * stride + my) * sizeof(A)), t[q], rbar);
+        for (int q = 0; q < NQ; ++q) wscr[q * 32 + warp] = t[q];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        sum_all_slots<A, NQ>(t, wscr, 32, nwarps);
+        if (lane == 0) mbar_arrive_expect_tx(tx.bar + buf, (uint32_t)(NQ * C * sizeof(A)) + extra_bytes);
+        if (lane < C) {
+            const uint32_t rbar = map_rank_u32(smem_u32(tx.bar + buf), lane);
+            const uint32_t rsl = map_rank_u32(smem_u32(sl), lane);
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) st_async(rsl + (uint32_t)((q * stride + rank) * sizeof(A)), t[q], rbar);
+        }
     }
 }
 
@@ -773,7 +789,7 @@ __device__ __forceinline__ void cluster_allreduce_tx_finish(A (&v)[NQ], A *slots
     const A *sl = slots + (size_t)buf * stride * kMaxValues;
     mbar_wait_bounded(tx.bar + buf, (tx.parity >> buf) & 1u, tx.timed_out);
     tx.parity ^= 1u << buf;
-    sum_all_slots<A, NQ>(v, sl, stride, C * (blockDim.x >> 5));
+    sum_all_slots<A, NQ>(v, sl, stride, C);
 #pragma unroll
     for (int q = 0; q < NQ; ++q) v[q] = acc_normalize(v[q]);
 }
@@ -913,6 +929,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
     const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
 
     for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
+    for (uint32_t e = tid; e < (uint32_t)(kMaxValues * 32); e += nthr) wscr[e] = A(0);  // local slots
     // transaction-counted reductions (C >= 2): two mbarriers of one arrival each,
     // initialised and made visible to the cluster before any CTA sends to them
     TxReduce tx{reinterpret_cast<uint64_t *>(s_item + 8), 0u, s_item + 12};
@@ -1283,8 +1300,8 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, PTRI, ST, RPT>::max_threa
                         if (relres) acc_madd(v2[1], r[q], r[q]);
                     }
                     if (C > 1) {
+                        // its CTA barrier also completes this CTA's z rows in the window
                         cluster_allreduce_tx_send<A, 2>(v2, slots, wscr, 1, tx, C, rank, halo_in);
-                        __syncthreads();  // this CTA's z rows are in the window
                         const bool halo_rows = __any_sync(0xffffffffu, first_knot || last_knot);
                         if (!halo_rows) matS_rows(w);
                         cluster_allreduce_tx_finish<A, 2>(v2, slots, 1, tx, C);
@@ -1522,6 +1539,7 @@ __global__ void __launch_bounds__((RegBudget<T, A, NP, false, ST, RPT>::max_thre
     const uint32_t zero_elems = (uint32_t)((2 * Plan::vec(lp.kmax) + 2 * Plan::halo()) / sizeof(T));
 
     for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
+    for (uint32_t e = tid; e < (uint32_t)(kMaxValues * 32); e += nthr) wscr[e] = A(0);  // local slots
     // transaction-counted reductions (C >= 2), as in pcg_cluster_kernel
     TxReduce tx{reinterpret_cast<uint64_t *>(s_item + 8), 0u, s_item + 12};
     if (C > 1) {

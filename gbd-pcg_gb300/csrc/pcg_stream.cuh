@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(kStreamThreads, 1) pcg_stream_kernel(const Lau
         (uint32_t)((2 * Base::vec(lp.kmax) + Plan::own(lp.kmax) + 2 * Base::halo()) / sizeof(T));
 
     for (uint32_t e = tid; e < (uint32_t)(Base::slots(C) / sizeof(A)); e += nthr) slots[e] = A(0);
+    for (uint32_t e = tid; e < (uint32_t)(kMaxValues * 32); e += nthr) wscr[e] = A(0);  // local slots
     TxReduce tx{reinterpret_cast<uint64_t *>(s_item + 8), 0u, s_item + 12};
     if (C > 1) {
         if (tid == 0) {

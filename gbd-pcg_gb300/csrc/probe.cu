@@ -44,6 +44,7 @@ __global__ void probe_kernel(uint32_t reps, float *sink) {
     uint64_t *bar = reinterpret_cast<uint64_t *>(cell + 8);
     uint32_t *timed_out = reinterpret_cast<uint32_t *>(bar + 2);
     for (uint32_t e = threadIdx.x; e < 2 * kMaxValues * slot_stride(C); e += blockDim.x) slots[e] = 0.f;
+    for (uint32_t e = threadIdx.x; e < kMaxValues * 32; e += blockDim.x) wscr[e] = 0.f;  // local slots
     if (threadIdx.x == 0) {
         cell[0] = 0.f;
         *timed_out = 0u;
@@ -111,6 +112,7 @@ __global__ void probe_timeout_kernel(int *status) {
     float *cell = wscr + nwarps * kMaxValues * 32;
     uint64_t *bar = reinterpret_cast<uint64_t *>(cell + 8);
     uint32_t *timed_out = reinterpret_cast<uint32_t *>(bar + 2);
+    for (uint32_t e = threadIdx.x; e < kMaxValues * 32; e += blockDim.x) wscr[e] = 0.f;  // local slots
     if (threadIdx.x == 0) {
         *timed_out = 0u;
         mbar_init(bar, 1);

@@ -548,15 +548,13 @@ __device__ __forceinline__ void sum_all_slots(A (&v)[NQ], const A *sl, uint32_t 
 // Cluster-wide sum of NQ values, identical in every thread of the cluster.
 //   1. a warp butterfly (xor shuffles, the NQ values interleaved) gives every
 //      lane of a warp the warp's sums, the same bits in every lane (each step
-//      adds the same two values, in either order); lanes 0..max(C,1)-1 store
-//      them into slot [rank*W + w] of CTA `lane` (DSMEM stores; local when
-//      C == 1);
+//      adds the same two values, in either order); for C == 1 lane 0 stores
+//      them into slot [w] (for C >= 2, see below);
 //   2. one barrier (barrier.cluster, or __syncthreads when C == 1), whose
 //      release/acquire makes the stores — and any halo pushes the caller made
 //      before this call — visible;
-//   3. every thread sums the slots: up to 32 (64 for float; zero beyond C*W)
-//      with vector loads (sum_all_slots); beyond that, lane l sums slots l,
-//      l+32, ... and a warp butterfly finishes.
+//   3. every thread sums the slots in use (sum_all_slots: pairwise trees, or
+//      a strided sum and a warp butterfly).
 // Every thread of every CTA reads the same slots in the same order, so all hold
 // the same bits.  `buf` alternates between call sites so that a slot array is
 // rewritten only after a barrier that every reader has passed.  Slots
@@ -564,13 +562,16 @@ __device__ __forceinline__ void sum_all_slots(A (&v)[NQ], const A *sl, uint32_t 
 // shuffle rounds, with the values of a reduction interleaved, beat re-reading
 // the warp's 32 values from shared memory by one lane: one value 162 against
 // 192 ns, two 224 against 326, three 300 against 504, for a 256-thread CTA.)
-// `wscr` is not used (kept for the callers' shared-memory layout).
+// For C >= 2 the slot stage is in two levels, as in cluster_allreduce_tx:
+// the warps' sums go into the CTA's local slots (`wscr`, [value][32], zeroed
+// at kernel start), warp 0 sums them and stores the CTA's sums into slot
+// [rank] of every CTA before the cluster barrier, and every thread adds C
+// slots.
 template <typename A, int NQ>
 __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, A *wscr, int buf,
                                                   const cg::cluster_group &cluster, uint32_t C,
                                                   uint32_t rank) {
     static_assert(NQ <= kMaxValues, "slot array holds kMaxValues values");
-    (void)wscr;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nwarps = blockDim.x >> 5;
     const uint32_t stride = (uint32_t)slot_stride(C);
@@ -579,17 +580,33 @@ __device__ __forceinline__ void cluster_allreduce(A (&v)[NQ], A *slots, A *wscr,
 #pragma unroll
     for (int q = 0; q < NQ; ++q) t[q] = v[q];
     warp_sum_n<A, NQ>(t);
-    const uint32_t my = rank * nwarps + warp, total = C * nwarps;
-    if (lane < C) {
-        A *dst = (C == 1) ? sl : cluster.map_shared_rank(sl, lane);
+    if (C == 1) {
+        if (lane == 0) {
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) dst[q * stride + my] = t[q];
-    }
-    if (C == 1)
+            for (int q = 0; q < NQ; ++q) sl[q * stride + warp] = t[q];
+        }
         __syncthreads();
-    else
+        sum_all_slots<A, NQ>(v, sl, stride, nwarps);
+    } else {
+        // two levels, as cluster_allreduce_tx: the CTA's warp sums in its
+        // local slots (`wscr`), summed by warp 0, whose lanes store them into
+        // slot [rank] of every CTA; then the cluster barrier
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) wscr[q * 32 + warp] = t[q];
+        }
+        __syncthreads();
+        if (warp == 0) {
+            sum_all_slots<A, NQ>(t, wscr, 32, nwarps);
+            if (lane < C) {
+                A *dst = cluster.map_shared_rank(sl, lane);
+#pragma unroll
+                for (int q = 0; q < NQ; ++q) dst[q * stride + rank] = t[q];
+            }
+        }
         cluster.sync();
-    sum_all_slots<A, NQ>(v, sl, stride, total);
+        sum_all_slots<A, NQ>(v, sl, stride, C);
+    }
 #pragma unroll
     for (int q = 0; q < NQ; ++q) v[q] = acc_normalize(v[q]);
 }

@@ -62,6 +62,7 @@ __global__ void __launch_bounds__((RegBudget<float, double, NP, false, ST, RPT>:
     const uint32_t zero_d = (uint32_t)(SmemPlanRF<NP, ST>::dwin(lp.kmax) / sizeof(double));
 
     for (uint32_t e = tid; e < (uint32_t)(Plan::slots(C) / sizeof(double)); e += nthr) slots64[e] = 0.0;
+    for (uint32_t e = tid; e < (uint32_t)(kMaxValues * 32); e += nthr) wscr64[e] = 0.0;  // local slots
     const uint32_t cluster_id = blockIdx.x / C, nclusters = gridDim.x / C;
     Stamper stamp(lp, rank);
     for (uint32_t pass = 0;; ++pass) {

@@ -10,21 +10,23 @@
 //   * Thread t of a CTA owns RPT consecutive matrix rows (RPT = 2 only for even
 //     n, so both rows lie in one knot and share every vector load).  The rows
 //     of S (3 blocks) and of Phi^-1 (1 or 3 blocks) are held for the whole
-//     solve either in registers (register-tile matvec fed by vectorised
-//     shared-memory loads of the p / r window) or in shared memory (staged
-//     once per system); ST selects: 0 both in registers, 1 S in registers and
-//     Phi^-1 in shared memory, 2 both in shared memory.
+//     solve on chip; ST selects where: 0 both in registers, 1 S in registers
+//     and Phi^-1 in shared memory, 2 both in shared memory, 3 hybrid (two S
+//     blocks in registers, the third and Phi^-1 in shared memory), 4 tensor
+//     memory (the diagonal S block in registers, the others and Phi^-1 in the
+//     SM's TMEM).  Streamed rows (ST 5) are pcg_stream.cuh's kernel.
 //   * Vectors p and r live in shared memory with one halo knot on each side.
 //     Neighbour CTAs exchange boundary vectors through distributed shared
 //     memory (DSMEM): instead of re-publishing p and r after every update (as
 //     the reference does through global memory, include/pcg.cuh:175,205, with
 //     4 grid.sync per iteration), each CTA pushes its boundary upsilon = S p and
-//     z = Phi^-1 r together with its dot-product partial, and the receiver
-//     applies the same fused multiply-add to its halo copy that the owner
-//     applies to the original (r_h -= alpha upsilon_h; p_h = z_h + beta p_h),
-//     so the halos stay bit-identical with two cluster barriers per iteration.
-//   * Dot products: see cluster_allreduce.  All threads of the cluster hold
-//     identical alpha, beta and exit decisions.
+//     z = Phi^-1 r with its next reduction (st.async counted on the
+//     receiver's mbarrier), and the receiver applies the same fused
+//     multiply-add to its halo copy that the owner applies to the original
+//     (r_h -= alpha upsilon_h; p_h = z_h + beta p_h), so the halos stay
+//     bit-identical without a cluster barrier.
+//   * Dot products: see cluster_allreduce and cluster_allreduce_tx.  All
+//     threads of the cluster hold identical alpha, beta and exit decisions.
 // Arithmetic follows the reference: alpha = eta / p.Sp, lambda += alpha p,
 // r -= alpha Sp, beta = eta'/eta, p = z + beta p as fused multiply-adds; exit
 // on |r.z| < tol (include/pcg.cuh:195) or, optionally, on the relative
